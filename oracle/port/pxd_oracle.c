@@ -1,0 +1,1348 @@
+/*
+ * pxd_oracle.c -- TEST INFRASTRUCTURE: FP64 C restatement of the reference hot path.
+ * See pxd_oracle.h. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg use this file; it is the checker, never the product.
+ */
+#define _GNU_SOURCE
+#include "pxd_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/pxdock_gb300_vdw.h"
+
+#define EPS 1e-20 /* kParamEpsilon, math.h:128 */
+static const double kCoulomb = 332.0637141491396; /* kCoulombFactor, system.h:83 */
+static const double kPi = 3.141592653589793;      /* kMathPi, math.h:224 */
+
+/* ------------------------------------------------------------ small vectors */
+static inline void v_sub(const double* a, const double* b, double* c) {
+    c[0] = a[0] - b[0];
+    c[1] = a[1] - b[1];
+    c[2] = a[2] - b[2];
+}
+static inline void v_add(const double* a, const double* b, double* c) {
+    c[0] = a[0] + b[0];
+    c[1] = a[1] + b[1];
+    c[2] = a[2] + b[2];
+}
+static inline void v_addi(double* a, const double* b) {
+    a[0] += b[0];
+    a[1] += b[1];
+    a[2] += b[2];
+}
+static inline void v_subi(double* a, const double* b) {
+    a[0] -= b[0];
+    a[1] -= b[1];
+    a[2] -= b[2];
+}
+static inline void v_scale(const double* a, double f, double* c) {
+    c[0] = a[0] * f;
+    c[1] = a[1] * f;
+    c[2] = a[2] * f;
+}
+static inline void v_scalei(double* a, double f) {
+    a[0] *= f;
+    a[1] *= f;
+    a[2] *= f;
+}
+static inline double v_dot(const double* a, const double* b) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+static inline double v_sqsum(const double* a) {
+    double s = a[0] * a[0];
+    s += a[1] * a[1];
+    s += a[2] * a[2];
+    return s;
+}
+static inline double v_norm(const double* a) { return sqrt(v_sqsum(a)); }
+static inline void v_cross(const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+static inline void v_normalize(double* a) {
+    double n = v_norm(a);
+    a[0] /= n;
+    a[1] /= n;
+    a[2] /= n;
+}
+static inline void m_apply(const double* m, const double* v, double* out) {
+    out[0] = v_dot(m, v);
+    out[1] = v_dot(m + 3, v);
+    out[2] = v_dot(m + 6, v);
+}
+static inline void m_mul(const double* r, const double* s, double* o) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            o[3 * i + j] = r[3 * i] * s[j] + r[3 * i + 1] * s[3 + j] + r[3 * i + 2] * s[6 + j];
+}
+static inline double safe_div(double a, double b) { return a / (b + EPS); }
+
+/* ------------------------------------------------------------- math.cpp:22-167 */
+void po_rotation_quaternion(const double* q, double* m) {
+    const double aa = q[0] * q[0], ab = q[0] * q[1], ac = q[0] * q[2], ad = q[0] * q[3];
+    const double bb = q[1] * q[1], bc = q[1] * q[2], bd = q[1] * q[3];
+    const double cc = q[2] * q[2], cd = q[2] * q[3], dd = q[3] * q[3];
+    m[0] = aa + bb - cc - dd;
+    m[1] = 2 * (bc - ad);
+    m[2] = 2 * (ac + bd);
+    m[3] = 2 * (ad + bc);
+    m[4] = aa - bb + cc - dd;
+    m[5] = 2 * (cd - ab);
+    m[6] = 2 * (bd - ac);
+    m[7] = 2 * (ab + cd);
+    m[8] = aa - bb - cc + dd;
+}
+
+/* Rodrigues matrix about a unit axis (math.cpp:44-60). */
+static void rotation_axis_angle(const double* k, double theta, double* m) {
+    const double st = sin(theta), ct = cos(theta), omc = 1 - ct;
+    m[0] = ct + k[0] * k[0] * omc;
+    m[1] = k[0] * k[1] * omc - k[2] * st;
+    m[2] = k[1] * st + k[0] * k[2] * omc;
+    m[3] = k[2] * st + k[0] * k[1] * omc;
+    m[4] = ct + k[1] * k[1] * omc;
+    m[5] = k[1] * k[2] * omc - k[0] * st;
+    m[6] = k[0] * k[2] * omc - k[1] * st;
+    m[7] = k[0] * st + k[1] * k[2] * omc;
+    m[8] = ct + k[2] * k[2] * omc;
+}
+
+/* Rodrigues matrix and its theta-derivative (math.cpp:62-94). */
+void po_rotation_axis_angle(const double* k, double theta, double* m, double* j) {
+    const double st = sin(theta), ct = cos(theta), omc = 1 - ct;
+    const double kxo = k[0] * omc, kyo = k[1] * omc, kzo = k[2] * omc;
+    const double kxs = k[0] * st, kys = k[1] * st, kzs = k[2] * st;
+    m[0] = ct + k[0] * kxo;
+    m[1] = k[1] * kxo - kzs;
+    m[2] = kys + k[2] * kxo;
+    m[3] = kzs + k[0] * kyo;
+    m[4] = ct + k[1] * kyo;
+    m[5] = k[2] * kyo - kxs;
+    m[6] = k[0] * kzo - kys;
+    m[7] = kxs + k[1] * kzo;
+    m[8] = ct + k[2] * kzo;
+    j[0] = -st + k[0] * kxs;
+    j[1] = -k[2] * ct + k[0] * kys;
+    j[2] = k[1] * ct + k[0] * kzs;
+    j[3] = k[2] * ct + k[1] * kxs;
+    j[4] = -st + k[1] * kys;
+    j[5] = -k[0] * ct + k[1] * kzs;
+    j[6] = -k[1] * ct + k[2] * kxs;
+    j[7] = k[0] * ct + k[2] * kys;
+    j[8] = -st + k[2] * kzs;
+}
+
+/* Bond angle at j and its gradient on i and k (math.cpp:96-110). */
+double po_angle_and_gradient(const double* pi, const double* pj, const double* pk, double* gi,
+                             double* gk) {
+    double v0[3], v1[3], c[3];
+    v_sub(pj, pi, v0);
+    v_sub(pj, pk, v1);
+    v_cross(v0, v1, c);
+    const double rp = v_norm(c);
+    v_cross(v0, c, gi);
+    v_cross(c, v1, gk);
+    v_scalei(gi, -safe_div(1.0, v_sqsum(v0) * rp));
+    v_scalei(gk, -safe_div(1.0, v_sqsum(v1) * rp));
+    return atan2(rp, v_dot(v0, v1) + EPS);
+}
+
+/* Signed dihedral angle (math.cpp:112-128). */
+double po_dihedral(const double* pi, const double* pj, const double* pk, const double* pl) {
+    double rij[3], rkj[3], w[3], m[3], n[3];
+    v_sub(pj, pi, rij);
+    v_sub(pj, pk, rkj);
+    v_sub(pl, pk, w);
+    v_cross(rij, rkj, m);
+    v_cross(rkj, w, n);
+    v_cross(m, n, w);
+    const double wlen = v_norm(w);
+    const double s = v_dot(m, n);
+    const double phi = atan2(wlen, s + EPS);
+    const double ipr = v_dot(rij, n);
+    return ipr < 0.0 ? phi : -phi;
+}
+
+/* Dihedral angle and its gradient on the four atoms (math.cpp:130-167). */
+double po_dihedral_and_gradient(const double* pi, const double* pj, const double* pk,
+                                const double* pl, double* gi, double* gj, double* gk,
+                                double* gl) {
+    double rij[3], rkj[3], rkl[3], m[3], n[3], w[3];
+    v_sub(pj, pi, rij);
+    v_sub(pj, pk, rkj);
+    v_sub(pl, pk, rkl);
+    v_cross(rij, rkj, m);
+    v_cross(rkj, rkl, n);
+    v_cross(m, n, w);
+    const double wlen = v_norm(w);
+    const double s = v_dot(m, n);
+    const double phi = atan2(wlen, s + EPS);
+    const double ipr = v_dot(rij, n);
+    const double theta = ipr < 0.0 ? phi : -phi;
+    const double nrkj2 = v_sqsum(rkj);
+    const double nrkj_1 = safe_div(1.0, sqrt(nrkj2));
+    const double nrkj_2 = nrkj_1 * nrkj_1;
+    const double nrkj = nrkj2 * nrkj_1;
+    const double a = -nrkj / v_sqsum(m);
+    const double b = nrkj / v_sqsum(n);
+    v_scale(m, -a, gi);
+    v_scale(n, -b, gl);
+    const double p = v_dot(rij, rkj) * nrkj_2;
+    const double q = v_dot(rkj, rkl) * nrkj_2;
+    double uvec[3], vvec[3], svec[3];
+    v_scale(gi, p, uvec);
+    v_scale(gl, q, vvec);
+    v_sub(uvec, vvec, svec);
+    v_sub(gi, svec, gj);
+    v_add(gl, svec, gk);
+    v_scalei(gj, -1.0);
+    v_scalei(gk, -1.0);
+    return theta;
+}
+
+void po_vdw_type_table(double* sigma, double* epsilon) {
+    for (int i = 0; i < PXD_NUM_VDW_TYPES; ++i) {
+        sigma[i] = PXD_VDW_SIGMA[i];
+        epsilon[i] = PXD_VDW_EPSILON[i];
+    }
+}
+
+/* ------------------------------------------------------------- pair.h:25-60 */
+static inline double coul_pair(double qi, double qj, const double* rij, double d, double scale,
+                               double* gi, double* gj) {
+    const double qq = qi * qj * scale;
+    const double de_dr_r = -safe_div(qq, d * d * d) * kCoulomb;
+    double g[3];
+    v_scale(rij, de_dr_r, g);
+    v_subi(gi, g);
+    v_addi(gj, g);
+    return safe_div(qq, d) * kCoulomb;
+}
+
+static inline double vdw_pair(double si, double ei, double sj, double ej, const double* rij,
+                              double d, double scale, double* gi, double* gj) {
+    double fused = (si + sj) * 0.5;
+    const double u6 = pow(safe_div(fused, d), 6.0);
+    const double u12 = u6 * u6;
+    fused = sqrt(ei * ej) * scale * 4.0;
+    const double irsqr = safe_div(1.0, d * d);
+    const double de_dr_r = (-12.0 * u12 + 6.0 * u6) * irsqr * fused;
+    double g[3];
+    v_scale(rij, de_dr_r, g);
+    v_subi(gi, g);
+    v_addi(gj, g);
+    return (u12 - u6) * fused;
+}
+
+/* ------------------------------------------------- interaction.cpp:27-196 */
+static double bonds_energy(const pxd_topology* ff, const double* x, double* g) {
+    double e = 0.0;
+    for (int b = 0; b < ff->n_bonds; ++b) {
+        const int i = ff->bond_atoms[2 * b], j = ff->bond_atoms[2 * b + 1];
+        double d[3];
+        v_sub(x + 3 * j, x + 3 * i, d);
+        const double r = v_norm(d);
+        const double dr = r - ff->bond_length[b];
+        e += 0.5 * ff->bond_k[b] * (dr * dr);
+        const double de_dr = ff->bond_k[b] * (1 - safe_div(ff->bond_length[b], r));
+        v_scalei(d, de_dr);
+        v_subi(g + 3 * i, d);
+        v_addi(g + 3 * j, d);
+    }
+    return e;
+}
+
+static double angles_energy(const pxd_topology* ff, const double* x, double* g) {
+    double e = 0.0;
+    for (int a = 0; a < ff->n_angles; ++a) {
+        const int i = ff->angle_atoms[3 * a], j = ff->angle_atoms[3 * a + 1],
+                  k = ff->angle_atoms[3 * a + 2];
+        double fi[3], fk[3], fj[3];
+        const double theta = po_angle_and_gradient(x + 3 * i, x + 3 * j, x + 3 * k, fi, fk);
+        const double delta = theta - ff->angle_radian[a];
+        e += 0.5 * ff->angle_k[a] * (delta * delta);
+        const double de_dt = ff->angle_k[a] * delta;
+        v_scalei(fi, de_dt);
+        v_scalei(fk, de_dt);
+        v_addi(g + 3 * i, fi);
+        v_addi(g + 3 * k, fk);
+        v_add(fi, fk, fj);
+        v_subi(g + 3 * j, fj);
+    }
+    return e;
+}
+
+static double one_dihedral(const int32_t* ids, const int32_t* per, const double* phase,
+                           const double* kk, const double* x, double* g) {
+    const int i = ids[0], j = ids[1], k = ids[2], l = ids[3];
+    double gi[3], gj[3], gk[3], gl[3], gg[3];
+    const double theta =
+        po_dihedral_and_gradient(x + 3 * i, x + 3 * j, x + 3 * k, x + 3 * l, gi, gj, gk, gl);
+    double e = 0.0;
+    for (int t = 0; t < 6; ++t) {
+        if (per[t] == 0) break;
+        const double delta = theta * per[t] - phase[t];
+        e += kk[t] * (1 + cos(delta));
+        const double de_dt = kk[t] * per[t] * sin(delta);
+        v_scale(gi, -de_dt, gg);
+        v_addi(g + 3 * i, gg);
+        v_scale(gj, -de_dt, gg);
+        v_addi(g + 3 * j, gg);
+        v_scale(gk, -de_dt, gg);
+        v_addi(g + 3 * k, gg);
+        v_scale(gl, -de_dt, gg);
+        v_addi(g + 3 * l, gg);
+    }
+    return e;
+}
+
+static double dihedrals_energy(const pxd_topology* ff, const double* x, double* g) {
+    double e = 0.0;
+    for (int d = 0; d < ff->n_impropers; ++d)
+        e += one_dihedral(ff->improper_atoms + 4 * d, ff->improper_periodicity + 6 * d,
+                          ff->improper_phase + 6 * d, ff->improper_k + 6 * d, x, g);
+    for (int d = 0; d < ff->n_propers; ++d)
+        e += one_dihedral(ff->proper_atoms + 4 * d, ff->proper_periodicity + 6 * d,
+                          ff->proper_phase + 6 * d, ff->proper_k + 6 * d, x, g);
+    return e;
+}
+
+static double nonbonded_energy(const pxd_topology* ff, const double* x, double* g) {
+    const double coul14 = 0.833333333, vdw14 = 0.5; /* interaction.h:52-53 */
+    double e1 = 0.0, e2 = 0.0;
+    for (int p = 0; p < ff->n_pairs14; ++p) {
+        const int i = ff->pairs14[2 * p], j = ff->pairs14[2 * p + 1];
+        double rij[3];
+        v_sub(x + 3 * j, x + 3 * i, rij);
+        const double d = v_norm(rij);
+        e1 += coul_pair(ff->charge[i], ff->charge[j], rij, d, coul14, g + 3 * i, g + 3 * j);
+        e2 += vdw_pair(ff->sigma[i], ff->epsilon[i], ff->sigma[j], ff->epsilon[j], rij, d, vdw14,
+                       g + 3 * i, g + 3 * j);
+    }
+    for (int p = 0; p < ff->n_pairs; ++p) {
+        const int i = ff->pairs[2 * p], j = ff->pairs[2 * p + 1];
+        double rij[3];
+        v_sub(x + 3 * j, x + 3 * i, rij);
+        const double d = v_norm(rij);
+        e1 += coul_pair(ff->charge[i], ff->charge[j], rij, d, 1.0, g + 3 * i, g + 3 * j);
+        e2 += vdw_pair(ff->sigma[i], ff->epsilon[i], ff->sigma[j], ff->epsilon[j], rij, d, 1.0,
+                       g + 3 * i, g + 3 * j);
+    }
+    return e1 + e2;
+}
+
+double po_intra_energy(int which, const pxd_topology* ff, const double* x, double* g) {
+    switch (which) {
+        case 0: return bonds_energy(ff, x, g);
+        case 1: return angles_energy(ff, x, g);
+        case 2: return dihedrals_energy(ff, x, g);
+        case 3: return nonbonded_energy(ff, x, g);
+        default: {
+            double e = 0.0;
+            e += bonds_energy(ff, x, g);
+            e += angles_energy(ff, x, g);
+            e += dihedrals_energy(ff, x, g);
+            e += nonbonded_energy(ff, x, g);
+            return e;
+        }
+    }
+}
+
+/* ----------------------------------------------------------- owned copies */
+typedef struct {
+    pxd_topology t;
+    void* blocks[32];
+    int nblocks;
+} owned_topology;
+
+static void* dup_block(owned_topology* o, const void* src, size_t bytes) {
+    if (!src || bytes == 0) return NULL;
+    void* p = malloc(bytes);
+    memcpy(p, src, bytes);
+    o->blocks[o->nblocks++] = p;
+    return p;
+}
+
+static void own_topology(owned_topology* o, const pxd_topology* t) {
+    memset(o, 0, sizeof(*o));
+    o->t = *t;
+    const size_t n = (size_t)t->n_atoms;
+    o->t.charge = dup_block(o, t->charge, n * sizeof(double));
+    o->t.sigma = dup_block(o, t->sigma, n * sizeof(double));
+    o->t.epsilon = dup_block(o, t->epsilon, n * sizeof(double));
+    o->t.bond_atoms = dup_block(o, t->bond_atoms, (size_t)t->n_bonds * 2 * sizeof(int32_t));
+    o->t.bond_k = dup_block(o, t->bond_k, (size_t)t->n_bonds * sizeof(double));
+    o->t.bond_length = dup_block(o, t->bond_length, (size_t)t->n_bonds * sizeof(double));
+    o->t.angle_atoms = dup_block(o, t->angle_atoms, (size_t)t->n_angles * 3 * sizeof(int32_t));
+    o->t.angle_k = dup_block(o, t->angle_k, (size_t)t->n_angles * sizeof(double));
+    o->t.angle_radian = dup_block(o, t->angle_radian, (size_t)t->n_angles * sizeof(double));
+    o->t.improper_atoms =
+        dup_block(o, t->improper_atoms, (size_t)t->n_impropers * 4 * sizeof(int32_t));
+    o->t.improper_periodicity =
+        dup_block(o, t->improper_periodicity, (size_t)t->n_impropers * 6 * sizeof(int32_t));
+    o->t.improper_phase =
+        dup_block(o, t->improper_phase, (size_t)t->n_impropers * 6 * sizeof(double));
+    o->t.improper_k = dup_block(o, t->improper_k, (size_t)t->n_impropers * 6 * sizeof(double));
+    o->t.proper_atoms = dup_block(o, t->proper_atoms, (size_t)t->n_propers * 4 * sizeof(int32_t));
+    o->t.proper_periodicity =
+        dup_block(o, t->proper_periodicity, (size_t)t->n_propers * 6 * sizeof(int32_t));
+    o->t.proper_phase = dup_block(o, t->proper_phase, (size_t)t->n_propers * 6 * sizeof(double));
+    o->t.proper_k = dup_block(o, t->proper_k, (size_t)t->n_propers * 6 * sizeof(double));
+    o->t.pairs14 = dup_block(o, t->pairs14, (size_t)t->n_pairs14 * 2 * sizeof(int32_t));
+    o->t.pairs = dup_block(o, t->pairs, (size_t)t->n_pairs * 2 * sizeof(int32_t));
+}
+
+static void free_topology(owned_topology* o) {
+    for (int i = 0; i < o->nblocks; ++i) free(o->blocks[i]);
+    o->nblocks = 0;
+}
+
+/* ---------------------------------------------------------------- system */
+struct po_system {
+    /* receptor */
+    int n_rec;
+    double* rec_xyz0;    /* [n_rec][3] input coordinates */
+    owned_topology rec;
+    int n_rotors;
+    double* rotor_origin; /* [n_rotors][3] axis_origin */
+    double* rotor_axis;   /* [n_rotors][3] unit axis_vector */
+    int* mov_offsets;     /* [n_rotors+1] */
+    int* mov_atoms;       /* movable atoms, axis atom removed (data.cpp:358-361) */
+    int n_mov;
+    unsigned char* excluded; /* [n_rec] 1 for movable atoms */
+    int* excl_list;          /* sorted movable atoms (grid.cpp:118-123) */
+    int n_excl;
+    /* ligand */
+    int n_lig;
+    owned_topology lig;
+    int* lig_type;
+    /* torsion tree */
+    int n_frags, n_roots, n_tors;
+    int *frag_start, *frag_end, *perm, *rev, *roots;
+    int *tors_frag, *tors_parent, *tors_parent_atom, *tors_mine_atom;
+    int* frag_children_off; /* CSR of children per fragment, pre-order listing */
+    int* frag_children;
+    /* grid */
+    int has_grid;
+    pxd_box box;
+    double spacing_inv;
+    int npm1[3];
+    double slope;
+    double* maps[PXD_NUM_VDW_TYPES + 1]; /* [P][4] each; index 99 = Coulomb */
+};
+
+static int* dup_ints(const int32_t* src, size_t n) {
+    int* p = (int*)malloc((n ? n : 1) * sizeof(int));
+    for (size_t i = 0; i < n; ++i) p[i] = src[i];
+    return p;
+}
+
+po_system* po_system_create(const pxd_receptor_desc* rec, const pxd_ligand_desc* lig) {
+    po_system* s = (po_system*)calloc(1, sizeof(po_system));
+    /* receptor: torsional_receptor::parse post-processing (data.cpp:349-363) */
+    s->n_rec = rec->n_atoms;
+    s->rec_xyz0 = (double*)malloc((size_t)(s->n_rec ? s->n_rec : 1) * 3 * sizeof(double));
+    memcpy(s->rec_xyz0, rec->xyz, (size_t)s->n_rec * 3 * sizeof(double));
+    own_topology(&s->rec, &rec->ff);
+    s->n_rotors = rec->n_rotors;
+    s->rotor_origin = (double*)malloc((size_t)(s->n_rotors + 1) * 3 * sizeof(double));
+    s->rotor_axis = (double*)malloc((size_t)(s->n_rotors + 1) * 3 * sizeof(double));
+    s->mov_offsets = (int*)malloc((size_t)(s->n_rotors + 1) * sizeof(int));
+    const int total = s->n_rotors ? rec->rotor_offsets[s->n_rotors] : 0;
+    s->mov_atoms = (int*)malloc((size_t)(total + 1) * sizeof(int));
+    s->excluded = (unsigned char*)calloc((size_t)(s->n_rec + 1), 1);
+    s->n_mov = 0;
+    for (int r = 0; r < s->n_rotors; ++r) {
+        const int a0 = rec->rotor_axis[2 * r], a1 = rec->rotor_axis[2 * r + 1];
+        memcpy(s->rotor_origin + 3 * r, rec->xyz + 3 * a0, 3 * sizeof(double));
+        v_sub(rec->xyz + 3 * a1, s->rotor_origin + 3 * r, s->rotor_axis + 3 * r);
+        v_normalize(s->rotor_axis + 3 * r);
+        s->mov_offsets[r] = s->n_mov;
+        for (int k = rec->rotor_offsets[r]; k < rec->rotor_offsets[r + 1]; ++k) {
+            const int j = rec->rotor_atoms[k];
+            if (j != a1) {
+                s->mov_atoms[s->n_mov++] = j;
+                s->excluded[j] = 1;
+            }
+        }
+    }
+    s->mov_offsets[s->n_rotors] = s->n_mov;
+    s->excl_list = (int*)malloc((size_t)(s->n_mov + 1) * sizeof(int));
+    s->n_excl = 0;
+    for (int j = 0; j < s->n_rec; ++j)
+        if (s->excluded[j]) s->excl_list[s->n_excl++] = j;
+    /* ligand */
+    s->n_lig = lig->ff.n_atoms;
+    own_topology(&s->lig, &lig->ff);
+    s->lig_type = dup_ints(lig->vdw_type, (size_t)s->n_lig);
+    /* torsion tree (data.cpp:410-482 in flat form) */
+    const pxd_torsion_tree* t = &lig->tree;
+    s->n_frags = t->n_frags;
+    s->n_roots = t->n_roots;
+    s->n_tors = t->n_torsions;
+    if (t->n_frags > 0) {
+        s->frag_start = dup_ints(t->frag_start, (size_t)t->n_frags);
+        s->frag_end = dup_ints(t->frag_end, (size_t)t->n_frags);
+        s->perm = dup_ints(t->perm, (size_t)s->n_lig);
+        s->rev = (int*)malloc((size_t)(s->n_lig + 1) * sizeof(int));
+        for (int p = 0; p < s->n_lig; ++p) s->rev[s->perm[p]] = p;
+        s->roots = dup_ints(t->roots, (size_t)t->n_roots);
+        s->tors_frag = dup_ints(t->tors_frag, (size_t)t->n_torsions);
+        s->tors_parent = dup_ints(t->tors_parent, (size_t)t->n_torsions);
+        s->tors_parent_atom = dup_ints(t->tors_parent_atom, (size_t)t->n_torsions);
+        s->tors_mine_atom = dup_ints(t->tors_mine_atom, (size_t)t->n_torsions);
+    }
+    s->slope = 0.0;
+    return s;
+}
+
+void po_system_destroy(po_system* s) {
+    if (!s) return;
+    po_drop_grid(s);
+    free(s->rec_xyz0);
+    free_topology(&s->rec);
+    free(s->rotor_origin);
+    free(s->rotor_axis);
+    free(s->mov_offsets);
+    free(s->mov_atoms);
+    free(s->excluded);
+    free(s->excl_list);
+    free_topology(&s->lig);
+    free(s->lig_type);
+    free(s->frag_start);
+    free(s->frag_end);
+    free(s->perm);
+    free(s->rev);
+    free(s->roots);
+    free(s->tors_frag);
+    free(s->tors_parent);
+    free(s->tors_parent_atom);
+    free(s->tors_mine_atom);
+    free(s);
+}
+
+/* ------------------------------------------------------------ grid (grid.cpp) */
+typedef struct {
+    po_system* s;
+    const int* types;
+    int n_types;
+    int i0, i1;
+} grid_job;
+
+/* partial_worker::populate (grid.cpp:150-195) for the i-slab [i0, i1). */
+static void* grid_worker(void* arg) {
+    grid_job* job = (grid_job*)arg;
+    po_system* s = job->s;
+    const pxd_box* bc = &s->box;
+    const int ny = bc->npoints[1], nz = bc->npoints[2];
+    double point[3], vec[3], tmp[3];
+    double* acc = (double*)malloc((size_t)(job->n_types + 1) * 4 * sizeof(double));
+    for (int i = job->i0; i < job->i1; ++i) {
+        point[0] = bc->init_xyz[0] + bc->spacing * i;
+        for (int j = 0; j < ny; ++j) {
+            point[1] = bc->init_xyz[1] + bc->spacing * j;
+            for (int k = 0; k < nz; ++k) {
+                point[2] = bc->init_xyz[2] + bc->spacing * k;
+                memset(acc, 0, (size_t)(job->n_types + 1) * 4 * sizeof(double));
+                for (int a = 0; a < s->n_rec; ++a) {
+                    if (s->excluded[a]) continue;
+                    v_sub(s->rec_xyz0 + 3 * a, point, vec);
+                    const double d = v_norm(vec);
+                    acc[0] += coul_pair(1.0, s->rec.t.charge[a], vec, d, 1.0, acc + 1, tmp);
+                    for (int t = 0; t < job->n_types; ++t) {
+                        const int ty = job->types[t];
+                        double* at = acc + 4 * (t + 1);
+                        at[0] += vdw_pair(PXD_VDW_SIGMA[ty], PXD_VDW_EPSILON[ty], s->rec.t.sigma[a],
+                                          s->rec.t.epsilon[a], vec, d, 1.0, at + 1, tmp);
+                    }
+                }
+                const size_t off = ((size_t)i * ny + j) * nz + k;
+                memcpy(s->maps[PXD_NUM_VDW_TYPES] + 4 * off, acc, 4 * sizeof(double));
+                for (int t = 0; t < job->n_types; ++t)
+                    memcpy(s->maps[job->types[t]] + 4 * off, acc + 4 * (t + 1), 4 * sizeof(double));
+            }
+        }
+    }
+    free(acc);
+    return NULL;
+}
+
+int po_build_grid(po_system* s, const pxd_box* box, const int32_t* types, int32_t n_types,
+                  int nthreads) {
+    po_drop_grid(s);
+    s->box = *box;
+    s->spacing_inv = 1.0 / box->spacing;
+    for (int d = 0; d < 3; ++d) s->npm1[d] = box->npoints[d] - 1;
+    const size_t P = (size_t)box->npoints[0] * box->npoints[1] * box->npoints[2];
+    int all[PXD_NUM_VDW_TYPES];
+    int nt = 0;
+    if (n_types < 0) {
+        for (int t = 0; t < PXD_NUM_VDW_TYPES; ++t) all[nt++] = t;
+    } else {
+        for (int t = 0; t < n_types; ++t) {
+            int dup = 0;
+            for (int u = 0; u < nt; ++u) dup |= (all[u] == types[t]);
+            if (!dup) all[nt++] = types[t];
+        }
+    }
+    s->maps[PXD_NUM_VDW_TYPES] = (double*)calloc(P * 4, sizeof(double));
+    for (int t = 0; t < nt; ++t) s->maps[all[t]] = (double*)calloc(P * 4, sizeof(double));
+    const int ni = box->npoints[0];
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > ni) nthreads = ni;
+    pthread_t* th = (pthread_t*)malloc((size_t)nthreads * sizeof(pthread_t));
+    grid_job* jobs = (grid_job*)malloc((size_t)nthreads * sizeof(grid_job));
+    const int len = (ni + nthreads - 1) / nthreads;
+    for (int w = 0; w < nthreads; ++w) {
+        jobs[w].s = s;
+        jobs[w].types = all;
+        jobs[w].n_types = nt;
+        jobs[w].i0 = w * len < ni ? w * len : ni;
+        jobs[w].i1 = (w + 1) * len < ni ? (w + 1) * len : ni;
+        pthread_create(&th[w], NULL, grid_worker, &jobs[w]);
+    }
+    for (int w = 0; w < nthreads; ++w) pthread_join(th[w], NULL);
+    free(th);
+    free(jobs);
+    s->has_grid = 1;
+    return 0;
+}
+
+void po_set_slope(po_system* s, double slope) { s->slope = slope; }
+
+void po_drop_grid(po_system* s) {
+    for (int m = 0; m <= PXD_NUM_VDW_TYPES; ++m) {
+        free(s->maps[m]);
+        s->maps[m] = NULL;
+    }
+    s->has_grid = 0;
+}
+
+int po_grid_copy(const po_system* s, int map, double* out) {
+    if (map < 0 || map > PXD_NUM_VDW_TYPES || !s->maps[map]) return -1;
+    const size_t P = (size_t)s->box.npoints[0] * s->box.npoints[1] * s->box.npoints[2];
+    memcpy(out, s->maps[map], P * 4 * sizeof(double));
+    return 0;
+}
+
+static inline size_t grid_offset(const po_system* s, int i, int j, int k) {
+    return ((size_t)i * s->box.npoints[1] + j) * s->box.npoints[2] + k;
+}
+
+/* Trilinear blend of the stored {E, grad} records (grid.cpp:273-303). */
+static double trilinear(const double* m, const size_t* pidx, const double* w, double* grad) {
+    double acc[4] = {0, 0, 0, 0};
+    for (int c = 0; c < 8; ++c) {
+        const double* f = m + 4 * pidx[c];
+        double v[4] = {f[0] * w[c], f[1] * w[c], f[2] * w[c], f[3] * w[c]};
+        if (c == 0) {
+            memcpy(acc, v, sizeof(acc));
+        } else {
+            acc[0] += v[0];
+            acc[1] += v[1];
+            acc[2] += v[2];
+            acc[3] += v[3];
+        }
+    }
+    grad[0] = acc[1];
+    grad[1] = acc[2];
+    grad[2] = acc[3];
+    return acc[0];
+}
+
+/* receptor_cache::get (grid.cpp:197-262). Returns 1 when the atom is inside. */
+int po_grid_get(const po_system* s, int type, double q, const double* xyz, double* energy,
+                double* grad) {
+    double flb[3], gtmp[3], penalty = 0.0;
+    int lo[3], hi[3];
+    v_sub(xyz, s->box.init_xyz, flb);
+    v_scalei(flb, s->spacing_inv);
+    for (int d = 0; d < 3; ++d) {
+        if (flb[d] < 0.0) {
+            lo[d] = 0;
+            gtmp[d] = -1.0;
+            penalty -= flb[d];
+            flb[d] = 0.0;
+        } else if (flb[d] < s->npm1[d]) {
+            lo[d] = (int)flb[d];
+            gtmp[d] = 0.0;
+        } else {
+            lo[d] = s->npm1[d] - 1;
+            gtmp[d] = 1.0;
+            penalty += flb[d] - s->npm1[d];
+            flb[d] = s->npm1[d];
+        }
+        hi[d] = lo[d] + 1;
+    }
+    size_t pidx[8];
+    pidx[0] = grid_offset(s, lo[0], lo[1], lo[2]);
+    pidx[1] = grid_offset(s, hi[0], lo[1], lo[2]);
+    pidx[2] = grid_offset(s, lo[0], hi[1], lo[2]);
+    pidx[3] = grid_offset(s, hi[0], hi[1], lo[2]);
+    pidx[4] = grid_offset(s, lo[0], lo[1], hi[2]);
+    pidx[5] = grid_offset(s, hi[0], lo[1], hi[2]);
+    pidx[6] = grid_offset(s, lo[0], hi[1], hi[2]);
+    pidx[7] = grid_offset(s, hi[0], hi[1], hi[2]);
+    const double x = flb[0] - lo[0], y = flb[1] - lo[1], z = flb[2] - lo[2];
+    const double mx = 1.0 - x, my = 1.0 - y, mz = 1.0 - z;
+    const double w[8] = {mx * my * mz, x * my * mz, mx * y * mz, x * y * mz,
+                         mx * my * z,  x * my * z,  mx * y * z,  x * y * z};
+    int hit = 1;
+    if (penalty > 0.0) {
+        *energy += penalty * s->box.spacing * s->slope;
+        v_scalei(gtmp, s->slope);
+        v_addi(grad, gtmp);
+        hit = 0;
+    }
+    *energy += trilinear(s->maps[PXD_NUM_VDW_TYPES], pidx, w, gtmp) * q;
+    if (hit) {
+        v_scalei(gtmp, q);
+        v_addi(grad, gtmp);
+    }
+    *energy += trilinear(s->maps[type], pidx, w, gtmp);
+    if (hit) v_addi(grad, gtmp);
+    return hit;
+}
+
+/* ------------------------------------------- interaction.cpp:202-350 objective */
+typedef struct {
+    double* rec_xyz;  /* [n_rec][3] current receptor coordinates */
+    double* rec_grad; /* [n_rec][3] */
+    double* jac;      /* [n_mov][3] dR/dtheta . (x0 - origin) */
+} po_work;
+
+static void work_init(const po_system* s, po_work* w) {
+    const size_t n = (size_t)(s->n_rec ? s->n_rec : 1);
+    w->rec_xyz = (double*)malloc(n * 3 * sizeof(double));
+    memcpy(w->rec_xyz, s->rec_xyz0, (size_t)s->n_rec * 3 * sizeof(double));
+    w->rec_grad = (double*)malloc(n * 3 * sizeof(double));
+    w->jac = (double*)malloc((size_t)(s->n_mov + 1) * 3 * sizeof(double));
+}
+
+static void work_free(po_work* w) {
+    free(w->rec_xyz);
+    free(w->rec_grad);
+    free(w->jac);
+}
+
+static double score_grad_work(const po_system* s, po_work* w, const double* tors,
+                              const double* lig_xyz, double* tgrad, double* lgrad) {
+    /* receptor_torsion2xyz (interaction.cpp:316-336) */
+    int off = 0;
+    for (int r = 0; r < s->n_rotors; ++r) {
+        double rot[9], jr[9], tmp[3];
+        po_rotation_axis_angle(s->rotor_axis + 3 * r, tors[r], rot, jr);
+        for (int k = s->mov_offsets[r]; k < s->mov_offsets[r + 1]; ++k) {
+            const int j = s->mov_atoms[k];
+            v_sub(s->rec_xyz0 + 3 * j, s->rotor_origin + 3 * r, tmp);
+            m_apply(rot, tmp, w->rec_xyz + 3 * j);
+            v_addi(w->rec_xyz + 3 * j, s->rotor_origin + 3 * r);
+            m_apply(jr, tmp, w->jac + 3 * off);
+            ++off;
+        }
+    }
+    memset(w->rec_grad, 0, (size_t)s->n_rec * 3 * sizeof(double));
+    memset(lgrad, 0, (size_t)s->n_lig * 3 * sizeof(double));
+    double energy = 0.0;
+    energy += po_intra_energy(4, &s->rec.t, w->rec_xyz, w->rec_grad);
+    energy += po_intra_energy(4, &s->lig.t, lig_xyz, lgrad);
+    /* inter_molecular_interactions::put_gradients (interaction.cpp:202-257) */
+    double inter = 0.0;
+    for (int i = 0; i < s->n_lig; ++i) {
+        const double qi = s->lig.t.charge[i];
+        const int ty = s->lig_type[i];
+        const double si = PXD_VDW_SIGMA[ty], ei = PXD_VDW_EPSILON[ty];
+        const int* list = s->has_grid ? s->excl_list : NULL;
+        const int nlist = s->has_grid ? s->n_excl : s->n_rec;
+        if (s->has_grid) po_grid_get(s, ty, qi, lig_xyz + 3 * i, &inter, lgrad + 3 * i);
+        for (int k = 0; k < nlist; ++k) {
+            const int j = list ? list[k] : k;
+            double rij[3];
+            v_sub(w->rec_xyz + 3 * j, lig_xyz + 3 * i, rij);
+            const double d = v_norm(rij);
+            inter += coul_pair(qi, s->rec.t.charge[j], rij, d, 1.0, lgrad + 3 * i, w->rec_grad + 3 * j);
+            inter += vdw_pair(si, ei, s->rec.t.sigma[j], s->rec.t.epsilon[j], rij, d, 1.0,
+                              lgrad + 3 * i, w->rec_grad + 3 * j);
+        }
+    }
+    energy += inter;
+    /* receptor_xyz2torsion (interaction.cpp:338-350) */
+    off = 0;
+    for (int r = 0; r < s->n_rotors; ++r) {
+        tgrad[r] = 0.0;
+        for (int k = s->mov_offsets[r]; k < s->mov_offsets[r + 1]; ++k) {
+            tgrad[r] += v_dot(w->jac + 3 * off, w->rec_grad + 3 * s->mov_atoms[k]);
+            ++off;
+        }
+    }
+    return energy;
+}
+
+double po_score_grad(po_system* s, const double* tors, const double* lig_xyz, double* tgrad,
+                     double* lgrad) {
+    po_work w;
+    work_init(s, &w);
+    const double e = score_grad_work(s, &w, tors, lig_xyz, tgrad, lgrad);
+    work_free(&w);
+    return e;
+}
+
+/* ----------------------------------------------- L-BFGS (optimizer.cpp:56-560) */
+typedef struct {
+    const po_system* s;
+    po_work* w;
+    int D, n3, nt;
+    const double* x0;  /* start [3N | T] flat */
+    double* xt;        /* trial */
+    double* tgrad;
+    int32_t* nevals;
+} closure_t;
+
+static inline double vec_absmax(const double* a, int n) {
+    double v = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double t = fabs(a[i]);
+        if (t > v) v = t;
+    }
+    return v;
+}
+static inline double vec_abssum(const double* a, int n) {
+    double v = 0.0;
+    for (int i = 0; i < n; ++i) v += fabs(a[i]);
+    return v;
+}
+static inline double vec_dot(const double* a, const double* b, int n) {
+    double v = 0.0;
+    for (int i = 0; i < n; ++i) v += a[i] * b[i];
+    return v;
+}
+
+/* obj_func_closure::evaluate_direction (optimizer.cpp:155-167): f and flat gradient
+ * at x0 + t * d, with the flat layout [ligand xyz | receptor torsions]. */
+static double eval_dir(closure_t* c, double t, const double* d, double* g) {
+    for (int i = 0; i < c->D; ++i) c->xt[i] = c->x0[i] + d[i] * t;
+    const double e = score_grad_work(c->s, c->w, c->xt + c->n3, c->xt, c->tgrad, g);
+    memcpy(g + c->n3, c->tgrad, (size_t)c->nt * sizeof(double));
+    ++*c->nevals;
+    return e;
+}
+
+/* model.put_gradients at the current x (optimizer.cpp:434-436, 554-558) */
+static double eval_at_x(closure_t* c, double* g) {
+    const double e = score_grad_work(c->s, c->w, c->x0 + c->n3, c->x0, c->tgrad, g);
+    memcpy(g + c->n3, c->tgrad, (size_t)c->nt * sizeof(double));
+    ++*c->nevals;
+    return e;
+}
+
+/* cubic_interpolate (optimizer.cpp:205-233) */
+static double cubic_interpolate(double x1, double f1, double g1, double x2, double f2, double g2,
+                                double lo, double hi) {
+    double d1 = g1 + g2 - 3.0 * (f1 - f2) / (x1 - x2);
+    const double d2sq = d1 * d1 - g1 * g2;
+    if (d2sq >= 0.0) {
+        const double d2 = sqrt(d2sq);
+        if (x1 <= x2)
+            d1 = x2 - (x2 - x1) * ((g2 + d2 - d1) / (g2 - g1 + 2.0 * d2));
+        else
+            d1 = x1 - (x1 - x2) * ((g1 + d2 - d1) / (g1 - g2 + 2.0 * d2));
+        const double m = d1 > lo ? d1 : lo;
+        return m < hi ? m : hi;
+    }
+    return (lo + hi) / 2.0;
+}
+
+/* strong_wolfe (optimizer.cpp:235-427). g holds the current gradient on entry and the
+ * accepted one on exit; bufs provides 4 scratch gradient vectors. */
+static void strong_wolfe(closure_t* c, const pxd_lbfgs_params* p, double* t_io, const double* d,
+                         double* f_io, double* g, double gtd, double** bufs) {
+    const int D = c->D;
+    double t = *t_io, f = *f_io;
+    double* g_new = bufs[0];
+    double* g_prev = bufs[1];
+    double* bg[2] = {bufs[2], bufs[3]};
+    double br[2] = {0, 0}, bf[2] = {0, 0}, bgtd[2] = {0, 0};
+    double f_new = eval_dir(c, t, d, g_new);
+    if (isnan(f_new)) {
+        *f_io = f_new;
+        return;
+    }
+    double gtd_new = vec_dot(g_new, d, D);
+    if (fabs(gtd_new) > p->ls_gtd_threshold) {
+        *f_io = f_new;
+        memcpy(g, g_new, (size_t)D * sizeof(double));
+        *t_io = t;
+        return;
+    }
+    double t_prev = 0.0, f_prev = f, gtd_prev = gtd;
+    memcpy(g_prev, g, (size_t)D * sizeof(double));
+    int done = 0, ls_iter = 0;
+    while (ls_iter < p->ls_max) {
+        if ((f_new > f + p->ls_c1 * t * gtd) || (ls_iter > 1 && f_new >= f_prev)) {
+            br[0] = t_prev; br[1] = t; bf[0] = f_prev; bf[1] = f_new;
+            memcpy(bg[0], g_prev, (size_t)D * sizeof(double));
+            memcpy(bg[1], g_new, (size_t)D * sizeof(double));
+            bgtd[0] = gtd_prev; bgtd[1] = gtd_new;
+            break;
+        }
+        if (fabs(gtd_new) <= -p->ls_c2 * gtd) {
+            br[0] = t; bf[0] = f_new;
+            memcpy(bg[0], g_new, (size_t)D * sizeof(double));
+            done = 1;
+            break;
+        }
+        if (gtd_new >= 0) {
+            br[0] = t_prev; br[1] = t; bf[0] = f_prev; bf[1] = f_new;
+            memcpy(bg[0], g_prev, (size_t)D * sizeof(double));
+            memcpy(bg[1], g_new, (size_t)D * sizeof(double));
+            bgtd[0] = gtd_prev; bgtd[1] = gtd_new;
+            break;
+        }
+        const double min_step = t + 0.01 * (t - t_prev);
+        const double max_step = t * 10.0;
+        const double tmp = t;
+        t = cubic_interpolate(t_prev, f_prev, gtd_prev, t, f_new, gtd_new, min_step, max_step);
+        t_prev = tmp;
+        f_prev = f_new;
+        memcpy(g_prev, g_new, (size_t)D * sizeof(double));
+        gtd_prev = gtd_new;
+        f_new = eval_dir(c, t, d, g_new);
+        gtd_new = vec_dot(g_new, d, D);
+        ++ls_iter;
+    }
+    double d_norm = 0.0;
+    if (ls_iter == p->ls_max) {
+        br[0] = 0; br[1] = t; bf[0] = f; bf[1] = f_new;
+        memcpy(bg[0], g, (size_t)D * sizeof(double));
+        memcpy(bg[1], g_new, (size_t)D * sizeof(double));
+    } else {
+        d_norm = vec_absmax(d, D);
+    }
+    int insuf = 0, lo = 0, hi = 1;
+    if (!done && bf[0] > bf[1]) {
+        lo = 1;
+        hi = 0;
+    }
+    while (!done && ls_iter < p->ls_max) {
+        double min_step, max_step;
+        if (br[0] > br[1]) {
+            min_step = br[1];
+            max_step = br[0];
+        } else {
+            min_step = br[0];
+            max_step = br[1];
+        }
+        double eps = max_step - min_step;
+        if (eps * d_norm < p->ls_tolerance_change) break;
+        t = cubic_interpolate(br[0], bf[0], bgtd[0], br[1], bf[1], bgtd[1], min_step, max_step);
+        eps *= 0.1;
+        const double near = (max_step - t) < (t - min_step) ? (max_step - t) : (t - min_step);
+        if (near < eps) {
+            if (insuf || t >= max_step || t <= min_step) {
+                if (fabs(t - max_step) < fabs(t - min_step))
+                    t = max_step - eps;
+                else
+                    t = min_step + eps;
+                insuf = 0;
+            } else {
+                insuf = 1;
+            }
+        } else {
+            insuf = 0;
+        }
+        f_new = eval_dir(c, t, d, g_new);
+        gtd_new = vec_dot(g_new, d, D);
+        ++ls_iter;
+        if (f_new > (f + p->ls_c1 * t * gtd) || f_new >= bf[lo]) {
+            br[hi] = t;
+            bf[hi] = f_new;
+            memcpy(bg[hi], g_new, (size_t)D * sizeof(double));
+            bgtd[hi] = gtd_new;
+            if (bf[0] > bf[1]) {
+                lo = 1;
+                hi = 0;
+            } else {
+                lo = 0;
+                hi = 1;
+            }
+        } else {
+            if (fabs(gtd_new) <= -p->ls_c2 * gtd) {
+                done = 1;
+            } else if (gtd_new * (br[hi] - br[lo]) >= 0.0) {
+                br[hi] = br[lo];
+                bf[hi] = bf[lo];
+                memcpy(bg[hi], bg[lo], (size_t)D * sizeof(double));
+                bgtd[hi] = bgtd[lo];
+            }
+            br[lo] = t;
+            bf[lo] = f_new;
+            memcpy(bg[lo], g_new, (size_t)D * sizeof(double));
+            bgtd[lo] = gtd_new;
+        }
+    }
+    *t_io = br[lo];
+    *f_io = bf[lo];
+    memcpy(g, bg[lo], (size_t)D * sizeof(double));
+}
+
+static int lbfgs_work(const po_system* s, po_work* w, const pxd_lbfgs_params* p, double* tors,
+                      double* lig_xyz, double* energy, int32_t* nevals) {
+    const int n3 = 3 * s->n_lig, nt = s->n_rotors, D = n3 + nt;
+    const int m = p->history;
+    const int max_eval = p->max_eval > 0 ? p->max_eval : p->max_iter * 5 / 4;
+    double* mem = (double*)calloc((size_t)D * (12 + 2 * (size_t)m) + 2 * (size_t)m + 8, sizeof(double));
+    double* x = mem;           /* current [xyz | tors] */
+    double* g = x + D;         /* flat gradient */
+    double* gp = g + D;        /* previous flat gradient */
+    double* d = gp + D;
+    double* q = d + D;
+    double* xt = q + D;
+    double* tg = xt + D;
+    double* bufs[4] = {tg + D, tg + 2 * D, tg + 3 * D, tg + 4 * D};
+    double* S = tg + 5 * D;    /* [m][D] old_stps ring */
+    double* Y = S + (size_t)m * D; /* [m][D] old_dirs ring */
+    double* ro = Y + (size_t)m * D;
+    double* al = ro + m;
+    double* sv = al + m;       /* s = d * t */
+    memcpy(x, lig_xyz, (size_t)n3 * sizeof(double));
+    memcpy(x + n3, tors, (size_t)nt * sizeof(double));
+    closure_t c = {s, w, D, n3, nt, x, xt, tg, nevals};
+    *nevals = 0;
+    /* initial f(x), df/dx */
+    double loss = eval_at_x(&c, g);
+    *energy = loss;
+    int status = PXD_POSE_NOT_CONVERGED;
+    if (vec_absmax(g, D) < p->tolerance_grad) {
+        free(mem);
+        return PXD_POSE_CONVERGED;
+    }
+    int head = 0, count = 0; /* ring buffer of the history deque */
+    double H_diag = 1.0, t = 0.0, prev_loss;
+    int n_iter = 0, updated = 0, high_change = 0;
+    while (n_iter < p->max_iter && *nevals < max_eval) {
+        ++n_iter;
+        if (n_iter > 1) {
+            for (int i = 0; i < D; ++i) q[i] = g[i] - gp[i]; /* y */
+            high_change = vec_absmax(q, D) > p->reset_threshold;
+        }
+        if (n_iter == 1 || high_change) {
+            for (int i = 0; i < D; ++i) d[i] = -g[i];
+            head = count = 0;
+            H_diag = 1.0;
+        } else {
+            double* y = q;
+            for (int i = 0; i < D; ++i) sv[i] = d[i] * t;
+            const double ys = vec_dot(y, sv, D);
+            if (ys > 1e-10) {
+                int slot;
+                if (count == m) {
+                    slot = head;
+                    head = (head + 1) % m;
+                } else {
+                    slot = (head + count) % m;
+                    ++count;
+                }
+                H_diag = ys / vec_dot(y, y, D);
+                memcpy(Y + (size_t)slot * D, y, (size_t)D * sizeof(double));
+                memcpy(S + (size_t)slot * D, sv, (size_t)D * sizeof(double));
+                ro[slot] = 1.0 / ys;
+            }
+            for (int i = 0; i < D; ++i) q[i] = -g[i];
+            for (int k = count - 1; k > -1; --k) {
+                const int slot = (head + k) % m;
+                al[k] = vec_dot(S + (size_t)slot * D, q, D) * ro[slot];
+                const double* yy = Y + (size_t)slot * D;
+                for (int i = 0; i < D; ++i) q[i] += yy[i] * (-al[k]);
+            }
+            for (int i = 0; i < D; ++i) d[i] = q[i] * H_diag;
+            for (int k = 0; k < count; ++k) {
+                const int slot = (head + k) % m;
+                const double be = vec_dot(Y + (size_t)slot * D, d, D) * ro[slot];
+                const double* ss = S + (size_t)slot * D;
+                for (int i = 0; i < D; ++i) d[i] += ss[i] * (al[k] - be);
+            }
+        }
+        memcpy(gp, g, (size_t)D * sizeof(double));
+        prev_loss = loss;
+        if (n_iter == 1 || high_change) {
+            const double inv = 1.0 / vec_abssum(g, D);
+            t = (1.0 < inv ? 1.0 : inv) * p->lr * 0.1;
+        } else {
+            t = p->lr;
+        }
+        const double gtd = vec_dot(g, d, D);
+        if (gtd > -p->tolerance_change) {
+            status = PXD_POSE_CONVERGED;
+            break;
+        }
+        strong_wolfe(&c, p, &t, d, &loss, g, gtd, bufs);
+        if (isnan(loss)) {
+            status = PXD_POSE_NAN;
+            break;
+        }
+        for (int i = 0; i < D; ++i) x[i] += d[i] * t;
+        updated = 1;
+        if (vec_absmax(g, D) <= p->tolerance_grad) {
+            status = PXD_POSE_CONVERGED;
+            break;
+        }
+        double smax = 0.0;
+        for (int i = 0; i < D; ++i) {
+            const double v = fabs(d[i] * t);
+            if (v > smax) smax = v;
+        }
+        if (smax <= p->tolerance_change) {
+            status = PXD_POSE_CONVERGED;
+            break;
+        }
+        if (fabs(loss - prev_loss) < p->tolerance_change) {
+            status = PXD_POSE_CONVERGED;
+            break;
+        }
+    }
+    if (updated) {
+        *energy = eval_at_x(&c, bufs[0]);
+    }
+    memcpy(lig_xyz, x, (size_t)n3 * sizeof(double));
+    memcpy(tors, x + n3, (size_t)nt * sizeof(double));
+    free(mem);
+    return status;
+}
+
+int po_lbfgs(po_system* s, const pxd_lbfgs_params* p, double* tors, double* lig_xyz,
+             double* energy, int32_t* nevals) {
+    po_work w;
+    work_init(s, &w);
+    const int st = lbfgs_work(s, &w, p, tors, lig_xyz, energy, nevals);
+    work_free(&w);
+    return st;
+}
+
+typedef struct {
+    po_system* s;
+    const pxd_lbfgs_params* p;
+    int n_poses;
+    double *tors, *xyz, *energy;
+    int32_t *nevals, *status;
+    int next;
+    pthread_mutex_t mtx;
+} batch_job;
+
+static void* batch_worker(void* arg) {
+    batch_job* b = (batch_job*)arg;
+    po_work w;
+    work_init(b->s, &w);
+    const int n3 = 3 * b->s->n_lig, nt = b->s->n_rotors;
+    while (1) {
+        pthread_mutex_lock(&b->mtx);
+        const int i = b->next++;
+        pthread_mutex_unlock(&b->mtx);
+        if (i >= b->n_poses) break;
+        b->status[i] = lbfgs_work(b->s, &w, b->p, b->tors + (size_t)i * nt,
+                                  b->xyz + (size_t)i * n3, b->energy + i, b->nevals + i);
+    }
+    work_free(&w);
+    return NULL;
+}
+
+int po_lbfgs_batch(po_system* s, const pxd_lbfgs_params* p, int32_t n_poses, double* tors,
+                   double* xyz, double* energy, int32_t* nevals, int32_t* status, int nthreads) {
+    batch_job b = {s, p, n_poses, tors, xyz, energy, nevals, status, 0, PTHREAD_MUTEX_INITIALIZER};
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)malloc((size_t)nthreads * sizeof(pthread_t));
+    for (int i = 0; i < nthreads; ++i) pthread_create(&th[i], NULL, batch_worker, &b);
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    free(th);
+    return 0;
+}
+
+/* ------------------------------------------------------------ kinematics */
+/* torsional_receptor::apply_parameters (data.cpp:366-385) */
+void po_receptor_apply(const po_system* s, const double* tors, double* out) {
+    memcpy(out, s->rec_xyz0, (size_t)s->n_rec * 3 * sizeof(double));
+    for (int r = 0; r < s->n_rotors; ++r) {
+        double rot[9], tmp[3];
+        rotation_axis_angle(s->rotor_axis + 3 * r, tors[r], rot);
+        for (int k = s->mov_offsets[r]; k < s->mov_offsets[r + 1]; ++k) {
+            double* p = out + 3 * s->mov_atoms[k];
+            v_sub(p, s->rotor_origin + 3 * r, tmp);
+            m_apply(rot, tmp, p);
+            v_addi(p, s->rotor_origin + 3 * r);
+        }
+    }
+}
+
+/* free_ligand::apply_parameters (data.cpp:592-641). The reference walks the fragment
+ * tree recursively; the flat torsion list is in the same pre-order, so one pass over
+ * it with per-fragment frames reproduces the same arithmetic:
+ *   rel_i   = x_i - x_mine(f)           (post-order pass, data.cpp:544-559)
+ *   fused_f = Rot(axis_f, theta_f) * fused_parent, fused_root = R
+ *   world_i = fused_f * rel_i + origin_f, origin_f = world(x_mine(f)). */
+void po_ligand_apply(const po_system* s, const double* xyz, const double* center,
+                     const double* rot, const double* tors, double* out) {
+    const int n = s->n_lig;
+    double* c = (double*)malloc((size_t)n * 3 * sizeof(double));
+    for (int p = 0; p < n; ++p) memcpy(c + 3 * p, xyz + 3 * s->perm[p], 3 * sizeof(double));
+    const int F = s->n_frags;
+    double* axes = (double*)calloc((size_t)F * 3, sizeof(double));
+    double* fused = (double*)calloc((size_t)F * 9, sizeof(double));
+    double* origin = (double*)calloc((size_t)F * 3, sizeof(double));
+    int* is_root = (int*)calloc((size_t)F, sizeof(int));
+    int* mine = (int*)malloc((size_t)F * sizeof(int));
+    for (int r = 0; r < s->n_roots; ++r) is_root[s->roots[r]] = 1;
+    for (int f = 0; f < F; ++f) mine[f] = -1;
+    /* axes from the input pose (data.cpp:530-537) */
+    for (int k = 0; k < s->n_tors; ++k) {
+        const int f = s->tors_frag[k];
+        mine[f] = s->tors_mine_atom[k];
+        v_sub(c + 3 * s->tors_mine_atom[k], c + 3 * s->tors_parent_atom[k], axes + 3 * f);
+        v_normalize(axes + 3 * f);
+    }
+    /* geometric centre over permuted order (data.h:101-106) */
+    double old_center[3] = {0, 0, 0};
+    for (int p = 0; p < n; ++p) v_addi(old_center, c + 3 * p);
+    v_scalei(old_center, 1.0 / n);
+    /* Relative coordinates (post_order_traverse, data.cpp:540-559). Every subtraction
+     * there reads a mine atom that is still in input coordinates, so: first each
+     * fragment's own atoms minus its mine atom, then each mine atom minus its parent's
+     * mine atom (or the old centre under a root), children before parents. */
+    for (int k = 0; k < s->n_tors; ++k) {
+        const int f = s->tors_frag[k];
+        for (int i = s->frag_start[f]; i < s->frag_end[f]; ++i)
+            if (i != mine[f]) v_subi(c + 3 * i, c + 3 * mine[f]);
+    }
+    for (int k = s->n_tors - 1; k >= 0; --k) {
+        const int f = s->tors_frag[k];
+        const int pf = s->tors_parent[k];
+        if (is_root[pf])
+            v_subi(c + 3 * mine[f], old_center);
+        else
+            v_subi(c + 3 * mine[f], c + 3 * mine[pf]);
+    }
+    for (int r = 0; r < s->n_roots; ++r) {
+        const int f = s->roots[r];
+        for (int i = s->frag_start[f]; i < s->frag_end[f]; ++i) v_subi(c + 3 * i, old_center);
+    }
+    /* root frames (data.cpp:614-630) */
+    double tmp[3];
+    for (int r = 0; r < s->n_roots; ++r) {
+        const int f = s->roots[r];
+        memcpy(fused + 9 * f, rot, 9 * sizeof(double));
+        memcpy(origin + 3 * f, center, 3 * sizeof(double));
+        for (int i = s->frag_start[f]; i < s->frag_end[f]; ++i) {
+            m_apply(rot, c + 3 * i, tmp);
+            v_add(tmp, center, c + 3 * i);
+        }
+    }
+    /* pre-order torsions (data.cpp:562-590, 632-638) */
+    for (int k = 0; k < s->n_tors; ++k) {
+        const int f = s->tors_frag[k];
+        const int pf = s->tors_parent[k];
+        /* the parent's frame moves this fragment's axis and mine atom */
+        m_apply(fused + 9 * pf, axes + 3 * f, tmp);
+        memcpy(axes + 3 * f, tmp, sizeof(tmp));
+        m_apply(fused + 9 * pf, c + 3 * mine[f], tmp);
+        v_add(tmp, origin + 3 * pf, c + 3 * mine[f]);
+        double cur[9];
+        rotation_axis_angle(axes + 3 * f, tors[k], cur);
+        m_mul(cur, fused + 9 * pf, fused + 9 * f);
+        memcpy(origin + 3 * f, c + 3 * mine[f], 3 * sizeof(double));
+        for (int i = s->frag_start[f]; i < s->frag_end[f]; ++i) {
+            if (i == mine[f]) continue;
+            m_apply(fused + 9 * f, c + 3 * i, tmp);
+            v_add(tmp, origin + 3 * f, c + 3 * i);
+        }
+    }
+    for (int a = 0; a < n; ++a) memcpy(out + 3 * a, c + 3 * s->rev[a], 3 * sizeof(double));
+    free(c);
+    free(axes);
+    free(fused);
+    free(origin);
+    free(is_root);
+    free(mine);
+}
+
+/* ------------------------------------------------------- RNG (random.h:33-63) */
+void po_rng_seed(po_rng* r, uint32_t seed) {
+    r->mt[0] = seed;
+    for (int i = 1; i < 624; ++i)
+        r->mt[i] = 1812433253u * (r->mt[i - 1] ^ (r->mt[i - 1] >> 30)) + (uint32_t)i;
+    r->idx = 624;
+}
+
+/* MT19937 (Matsumoto & Nishimura 1998) */
+uint32_t po_rng_next(po_rng* r) {
+    if (r->idx >= 624) {
+        for (int i = 0; i < 624; ++i) {
+            const uint32_t y = (r->mt[i] & 0x80000000u) | (r->mt[(i + 1) % 624] & 0x7fffffffu);
+            r->mt[i] = r->mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        r->idx = 0;
+    }
+    uint32_t y = r->mt[r->idx++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+}
+
+/* std::uniform_int_distribution<int> over a 32-bit engine: libstdc++ reduces with
+ * Lemire's multiply-and-reject method (arXiv:1805.10941). */
+int po_rng_uniform_int(po_rng* r, int a, int b) {
+    const uint32_t range = (uint32_t)b - (uint32_t)a + 1u;
+    if (range == 0u) return (int)((uint32_t)a + po_rng_next(r));
+    uint64_t prod = (uint64_t)po_rng_next(r) * range;
+    uint32_t low = (uint32_t)prod;
+    if (low < range) {
+        const uint32_t threshold = (uint32_t)(-range) % range;
+        while (low < threshold) {
+            prod = (uint64_t)po_rng_next(r) * range;
+            low = (uint32_t)prod;
+        }
+    }
+    return (int)((uint32_t)a + (uint32_t)(prod >> 32));
+}
+
+/* std::generate_canonical<double, 53> over mt19937: two draws, (lo + hi * 2^32) / 2^64. */
+static double canonical(po_rng* r) {
+    double sum = (double)po_rng_next(r);
+    sum += (double)po_rng_next(r) * 4294967296.0;
+    double v = sum / 18446744073709551616.0;
+    if (v >= 1.0) v = nextafter(1.0, 0.0);
+    return v;
+}
+
+double po_rng_uniform_real(po_rng* r, double a, double b) { return canonical(r) * (b - a) + a; }
+double po_rng_torsion(po_rng* r) { return canonical(r) * (kPi - -kPi) + -kPi; }
+
+void po_rng_in_box(po_rng* r, const double* lo, const double* hi, double* out) {
+    for (int d = 0; d < 3; ++d) out[d] = po_rng_uniform_real(r, lo[d], hi[d]);
+}
+
+/* random_orientation (random.cpp:29-40): uniform quaternion (Shoemake). */
+void po_rng_orientation(po_rng* r, double* q) {
+    const double two_pi = 2 * kPi;
+    const double u1 = canonical(r) * (1.0 - 0.0) + 0.0;
+    const double u2 = (canonical(r) * (1.0 - 0.0) + 0.0) * two_pi;
+    const double u3 = (canonical(r) * (1.0 - 0.0) + 0.0) * two_pi;
+    const double a = sqrt(1.0 - u1), b = sqrt(u1);
+    q[0] = a * sin(u2);
+    q[1] = a * cos(u2);
+    q[2] = b * sin(u3);
+    q[3] = b * cos(u3);
+}
+
+/* random_in_sphere (random.cpp:42-49): rejection in the cube [-1, 1)^3. */
+void po_rng_in_sphere(po_rng* r, double* out) {
+    while (1) {
+        out[0] = canonical(r) * (1.0 - -1.0) + -1.0;
+        out[1] = canonical(r) * (1.0 - -1.0) + -1.0;
+        out[2] = canonical(r) * (1.0 - -1.0) + -1.0;
+        if (v_sqsum(out) < 1.0) break;
+    }
+}

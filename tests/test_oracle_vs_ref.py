@@ -1,0 +1,149 @@
+"""The FP64 port against the reference engine compiled from its own sources.
+
+Runs only where oracle/_ref/liboracle_ref.so could be built (the reference checkout is
+present); elsewhere the committed golden fixtures (tests/golden/ref_*.npz) carry the
+reference's answers instead (test_oracle_golden.py).
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from pxdock_gb300 import abi, model, synth
+
+pytestmark = pytest.mark.skipif(not O.ref_available(), reason="reference oracle not built here")
+
+
+@pytest.fixture(scope="module")
+def system(tmp_path_factory):
+    d = tmp_path_factory.mktemp("sys")
+    rj = synth.make_receptor(seed=0, n_heavy=400, cube=18.0, cavity=5.0, n_rotors=3)
+    lj = synth.make_ligand(seed=1)
+    rp, lp = str(d / "rec.json"), str(d / "lig.json")
+    json.dump(rj, open(rp, "w"))
+    json.dump(lj, open(lp, "w"))
+    rec, lig = model.Receptor.from_json(rj), model.Ligand.from_json(lj)
+    return rec, lig, O.PortSystem(rec, lig), O.RefSystem(rp, lp)
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.max(np.abs(a - b)) / max(1.0, np.max(np.abs(b)))
+
+
+def test_ligand_kinematics(system):
+    rec, lig, port, ref = system
+    rng = np.random.default_rng(5)
+    for _ in range(5):
+        q = synth.random_quaternions(rng, 1)
+        R = synth.quaternion_matrix(q)[0]
+        c = rng.normal(size=3)
+        t = rng.uniform(-math.pi, math.pi, size=lig.n_torsions)
+        a = port.ligand_apply(lig.poses[0], c, R, t)
+        b = ref.ligand_apply(lig.poses[0], c, R, t)
+        assert rel(a, b) < 1e-13
+        v = synth.apply_parameters(lig.tree, lig.poses[0], c[None], R[None], t[None])[0]
+        assert rel(v, b) < 1e-12
+
+
+def test_receptor_kinematics(system):
+    rec, lig, port, ref = system
+    t = [0.3, -1.2, 2.5]
+    assert rel(port.receptor_apply(t), ref.receptor_apply(t)) < 1e-13
+
+
+def test_score_grad_brute_force(system):
+    rec, lig, port, ref = system
+    ref.drop_grid()
+    port.drop_grid()
+    rng = np.random.default_rng(3)
+    for _ in range(3):
+        x = lig.poses[0] + rng.normal(scale=0.2, size=lig.poses[0].shape)
+        t = rng.uniform(-3, 3, size=3)
+        e1, tg1, g1 = port.score_grad(t, x)
+        e2, tg2, g2 = ref.score_grad(t, x)
+        assert abs(e1 - e2) <= 1e-12 * max(1, abs(e2))
+        assert rel(g1, g2) < 1e-12 and rel(tg1, tg2) < 1e-12
+
+
+def test_grid_maps_and_score(system):
+    rec, lig, port, ref = system
+    center, size, spacing = (0.0, 0.0, 0.0), (8.0, 8.0, 8.0), 1.0
+    ref.build_grid(center, size, spacing)
+    box = model.make_box(center, size, spacing)
+    types = sorted(set(int(t) for t in lig.vdw_type))
+    port.build_grid(box, types)
+    for m in types + [abi.COULOMB_MAP]:
+        a, b = port.grid_map(m, box), ref.grid_map(m)
+        assert rel(a, b) < 1e-13, m
+    for slope in (0.0, 1e6):
+        ref.set_slope(slope)
+        port.set_slope(slope)
+        rng = np.random.default_rng(4)
+        for _ in range(4):
+            x = lig.poses[0] + rng.normal(scale=1.5, size=lig.poses[0].shape)
+            t = rng.uniform(-3, 3, size=3)
+            e1, tg1, g1 = port.score_grad(t, x)
+            e2, tg2, g2 = ref.score_grad(t, x)
+            assert abs(e1 - e2) <= 1e-12 * max(1, abs(e2))
+            assert rel(g1, g2) < 1e-12 and rel(tg1, tg2) < 1e-12
+
+
+def test_lbfgs_trajectory(system):
+    rec, lig, port, ref = system
+    center, size, spacing = (0.0, 0.0, 0.0), (8.0, 8.0, 8.0), 1.0
+    ref.build_grid(center, size, spacing)
+    port.build_grid(model.make_box(center, size, spacing),
+                    sorted(set(int(t) for t in lig.vdw_type)))
+    ref.set_slope(1e6)
+    port.set_slope(1e6)
+    rng = np.random.default_rng(9)
+    for _ in range(3):
+        x = lig.poses[0] + rng.normal(scale=0.3, size=lig.poses[0].shape)
+        t = rng.uniform(-1, 1, size=3)
+        a = port.lbfgs(abi.lbfgs_params(max_iter=60), t, x)
+        b = ref.lbfgs(60, 0, t, x)
+        assert a["nevals"] == b["nevals"]
+        assert (a["status"] == abi.POSE_CONVERGED) == b["converged"]
+        assert abs(a["energy"] - b["energy"]) <= 1e-9 * max(1, abs(b["energy"]))
+        assert rel(a["xyz"], b["xyz"]) < 1e-9
+
+
+def test_rng_streams():
+    import ctypes as C
+
+    lib, rl = O.port_lib(), O.ref_lib()
+
+    class Rng(C.Structure):
+        _fields_ = [("mt", C.c_uint32 * 624), ("idx", C.c_int)]
+
+    for seed in (0, 7, 12345):
+        r = Rng()
+        lib.po_rng_seed(C.byref(r), seed)
+        h = rl.ref_rng_create(seed)
+        for k in range(300):
+            op = k % 5
+            if op == 0:
+                a = lib.po_rng_uniform_int(C.byref(r), 0, 6)
+                b = rl.ref_rng_uniform_int(h, 0, 6)
+            elif op == 1:
+                a = lib.po_rng_torsion(C.byref(r))
+                b = rl.ref_rng_torsion(h)
+            elif op == 2:
+                x, y = np.zeros(4), np.zeros(4)
+                lib.po_rng_orientation(C.byref(r), x.ctypes.data_as(abi.f64p))
+                rl.ref_rng_orientation(h, y.ctypes.data_as(abi.f64p))
+                a, b = tuple(x), tuple(y)
+            elif op == 3:
+                x, y = np.zeros(3), np.zeros(3)
+                lib.po_rng_in_sphere(C.byref(r), x.ctypes.data_as(abi.f64p))
+                rl.ref_rng_in_sphere(h, y.ctypes.data_as(abi.f64p))
+                a, b = tuple(x), tuple(y)
+            else:
+                a = lib.po_rng_uniform_real(C.byref(r), -2.0, 5.0)
+                b = rl.ref_rng_uniform_real(h, -2.0, 5.0)
+            assert a == b, (seed, k, a, b)
+        rl.ref_rng_destroy(h)
