@@ -1,0 +1,382 @@
+"""Benchmark: batched L-BFGS pose optimisation on one GB300 (and N independent replicas).
+
+Workload (the configuration the headline metric is quoted on): one seeded synthetic
+pocket (1,500 heavy atoms + polar H), a 30 A box at 0.375 A (81^3 FP32 maps), the
+24-heavy-atom / 5-torsion ligand in 65,536 poses (random centre in the box, uniform
+orientation, torsions U[-pi, pi)), L-BFGS with m = 8, at most 300 iterations, gradient
+tolerance 1e-3 (the other constants as the reference optimiser).
+
+A step is one batched L-BFGS pass over all 65,536 poses. Start poses are restored and
+L2 is flushed (a 256 MiB write) between steps, outside the timed kernel.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's CPU implementation of the path (the reference
+engine compiled from its sources when present, else the FP64 C port of it) on all host
+threads, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _sub in ("protenix-dock_gb300", "oracle"):
+    sys.path.insert(0, os.path.join(REPO, _sub))
+
+import numpy as np  # noqa: E402
+
+N_POSES = 65536
+BOX_SIZE = 30.0
+SPACING = 0.375
+HISTORY = 8
+MAX_ITER = 300
+TOL_GRAD = 1e-3
+SLOPE = 1e6
+METRIC = "L-BFGS-optimised poses/s, batched vs plain GPU, at |dE|<=1e-3 kcal/mol"
+UNIT = "poses/s"
+
+
+def workload(seed_poses=2, n_poses=N_POSES):
+    from pxdock_gb300 import model, synth
+
+    rec = model.Receptor.from_json(synth.make_receptor(seed=0))
+    lig = model.Ligand.from_json(synth.make_ligand(seed=1))
+    box = model.make_box((0.0, 0.0, 0.0), (BOX_SIZE,) * 3, SPACING)
+    lo = np.array(box.init_xyz)
+    hi = lo + (np.array(box.npoints) - 1) * box.spacing
+    poses = synth.random_poses(lig, lo, hi, n_poses, seed=seed_poses)
+    return rec, lig, box, poses
+
+
+def config_dict(lig, box):
+    return {
+        "workload": "batched L-BFGS pose optimisation: 1 ligand (%d atoms, %d torsions) x %d "
+                    "poses, %dx%dx%d FP32 maps (%.0f A box @ %.3f A), m=%d, max_iter=%d, "
+                    "tol_grad=%g" % (lig.n_atoms, lig.n_torsions, N_POSES, box.npoints[0],
+                                     box.npoints[1], box.npoints[2], BOX_SIZE, SPACING, HISTORY,
+                                     MAX_ITER, TOL_GRAD),
+        "poses": N_POSES,
+        "ligand_atoms": lig.n_atoms,
+        "grid_points": int(np.prod(list(box.npoints))),
+        "l2": "flushed between steps (256 MiB write); inputs ~100 MB < L2",
+        "parallelism": "replicas",
+    }
+
+
+def lbfgs_params():
+    from pxdock_gb300 import native
+
+    return native.lbfgs_params(max_iter=MAX_ITER, history=HISTORY, tolerance_grad=TOL_GRAD)
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return None
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_eval():
+    """DRAM bytes per score+gradient evaluation from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "lbfgs_kernel_ncu.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_eval:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(rec, lig, box, poses, target_s=15.0, use_ref=False):
+    """The reference algorithm on the host cores over a bounded sample of poses."""
+    import oracle
+    from pxdock_gb300 import abi
+
+    threads = cpu_threads()
+    port = oracle.PortSystem(rec, lig)
+    types = sorted(set(int(t) for t in lig.vdw_type))
+    port.build_grid(box, types, nthreads=threads)
+    port.set_slope(SLOPE)
+    p = abi.lbfgs_params(max_iter=MAX_ITER, history=HISTORY, tolerance_grad=TOL_GRAD)
+    n = max(threads, 16)
+    while True:
+        t0 = time.perf_counter()
+        port.lbfgs_batch(p, np.zeros((n, 0)), poses[:n], threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= len(poses):
+            break
+        n = min(len(poses), int(n * max(2.0, target_s / max(dt, 1e-3) * 1.1)))
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of the %d poses, FP64 C port of the reference optimiser, %d threads, "
+                      "%.1f s" % (n, N_POSES, threads, dt)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    rec, lig, box, poses = workload()
+    threads = cpu_threads()
+    kind = "port"
+    steps = []
+    import oracle
+
+    if oracle.ref_available():
+        kind = "reference"
+    t_per_step = 20.0 / max(1, args.steps)
+    samples = []
+    for s in range(args.warmup + args.steps):
+        if kind == "reference":
+            r = _ref_sample(rec, lig, box, poses, threads, t_per_step)
+        else:
+            r = cpu_baseline(rec, lig, box, poses, target_s=t_per_step)
+        if s >= args.warmup:
+            steps.append(r["value"])
+            samples.append(r["sample"])
+    value = float(np.mean(steps))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * N_POSES / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference", "config": config_dict(lig, box),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": samples[-1]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def _ref_sample(rec, lig, box, poses, threads, target_s):
+    """The reference engine itself (oracle/_ref): lbfgs_step per pose on host threads."""
+    import concurrent.futures
+    import tempfile
+
+    import oracle
+
+    d = tempfile.mkdtemp()
+    rp, lp = os.path.join(d, "r.json"), os.path.join(d, "l.json")
+    json.dump(rec.raw, open(rp, "w"))
+    json.dump(lig.raw, open(lp, "w"))
+    systems = [oracle.RefSystem(rp, lp) for _ in range(threads)]
+    c = (0.0, 0.0, 0.0)
+    for s in systems:
+        s.build_grid(c, (BOX_SIZE,) * 3, SPACING, nthreads=threads)
+        s.set_slope(SLOPE)
+    # the reference hard-codes m = 100 and tol_grad = 0.5 (optimizer.h:61-66); it runs
+    # with its own constants and max_iter 300
+    n = threads * 2
+    while True:
+        t0 = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda i: systems[i % threads].lbfgs(MAX_ITER, 0, [], poses[i]), range(n)))
+        dt = time.perf_counter() - t0
+        if dt >= target_s or n >= len(poses):
+            break
+        n = min(len(poses), int(n * max(2.0, target_s / max(dt, 1e-3) * 1.1)))
+    return {"value": n / dt, "sample": "%d poses, reference engine (m=100, tol_grad=0.5 as "
+                                       "hard-coded), %d threads" % (n, threads)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--poses", type=int, default=N_POSES,
+                    help="poses per step (smaller only for profiling captures)")
+    args = ap.parse_args()
+    global N_POSES
+    N_POSES = args.poses
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    from pxdock_gb300 import native
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    native.load(auto_build=True)
+    rec, lig, box, poses = workload(seed_poses=2 + rank)
+    ctx = native.Context(local)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)))
+    ctx.set_slope(SLOPE)
+    lid = ctx.add_ligand(lig)
+    N = lig.n_atoms
+    dev = torch.device("cuda", local)
+    start = torch.from_numpy(poses.astype(np.float32)).to(dev)
+    xyz = start.clone()
+    ids = torch.full((N_POSES,), lid, dtype=torch.int32, device=dev)
+    tors = torch.zeros(1, device=dev)
+    energy = torch.zeros(N_POSES, dtype=torch.float64, device=dev)
+    nevals = torch.zeros(N_POSES, dtype=torch.int32, device=dev)
+    status = torch.zeros(N_POSES, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    p = lbfgs_params()
+    stream = torch.cuda.Stream(dev)
+    sptr = stream.cuda_stream
+
+    def step(ev=None):
+        with torch.cuda.stream(stream):
+            xyz.copy_(start)
+            flush.fill_(1.0)
+            if ev:
+                ev[0].record(stream)
+            ctx.lbfgs_dev(p, N_POSES, N, ids.data_ptr(), xyz.data_ptr(), tors.data_ptr(),
+                          energy.data_ptr(), nevals.data_ptr(), status.data_ptr(), sptr)
+            if ev:
+                ev[1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    evals_total = 0
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            step(events[k])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    kernel_ms = [a.elapsed_time(b) for a, b in events]
+    evals_step = int(nevals.sum().item())
+    evals_total = evals_step * args.steps
+    st = status.cpu().numpy()
+    e_final = energy.cpu().numpy()
+    t_dev = sum(kernel_ms) / 1000.0
+    if dist:
+        tt = torch.tensor([t_dev], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = world * N_POSES * args.steps / t_dev
+    # end to end through the host-buffer C-ABI call (copies in the timed region)
+    e2e_times = []
+    for k in range(max(1, min(args.steps, 3))):
+        t1 = time.perf_counter()
+        out = ctx.lbfgs(p, lid, poses)
+        e2e_times.append(time.perf_counter() - t1)
+    e2e_value = world * N_POSES / float(np.mean(e2e_times))
+    # plain per-pose path: one call per pose
+    n_plain = 64
+    t1 = time.perf_counter()
+    for i in range(n_plain):
+        ctx.lbfgs(p, lid, poses[i:i + 1])
+    plain_value = n_plain / (time.perf_counter() - t1)
+    peak, peak_kind = measured_peak()
+    bytes_per_eval = (256 + 24) * N
+    achieved = evals_step * bytes_per_eval / (np.mean(kernel_ms) / 1000.0) / 1e9
+    tpe = ncu_traffic_per_eval()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": float(np.mean(kernel_ms)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": config_dict(lig, box),
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": N_POSES * (N * 3 * 4 + 4),
+                "d2h_bytes_per_step": N_POSES * (N * 3 * 4 + 8 + 4 + 4)},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": None if tpe is None else tpe * evals_step,
+                     "algorithmic_bytes_per_eval": bytes_per_eval},
+        "plain_gpu": {"value": plain_value, "unit": UNIT, "poses": n_plain,
+                      "batched_over_plain": value / world / plain_value},
+        "evals_per_s": world * evals_total / t_dev,
+        "evals_per_pose": evals_step / N_POSES,
+        "status_counts": {str(k): int((st == k).sum()) for k in range(4)},
+        "final_energy_median": float(np.median(e_final)),
+        "wall_s": wall,
+    }
+    clocks = clk.summary()
+    if clocks:
+        line["clocks"] = clocks
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(rec, lig, box, poses)
+    del out
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

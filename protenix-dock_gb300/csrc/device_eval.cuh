@@ -1,0 +1,484 @@
+// Warp-cooperative energy + gradient of one pose (device code shared by the score,
+// L-BFGS and Monte-Carlo kernels).
+//
+// One warp owns one pose. Ligand and receptor-local coordinates and gradient
+// accumulators live in the warp's shared-memory slice; term lists are walked 32 at a
+// time (one term per lane; the host ordered them so that no atom repeats within a
+// 32-term round) and gradients are added with shared-memory atomics. Energies are
+// summed per lane in a compensated FP32 pair (two-sum) and reduced across the warp,
+// then returned as double.
+//
+// Each block restates one reference routine in FP32:
+//   bonds / angles / dihedrals / pairs   interaction.cpp:27-168, pair.h:25-60, math.cpp:96-167
+//   grid lookup with out-of-box penalty  grid.cpp:197-303
+//   explicit inter pairs                 interaction.cpp:202-257
+//   receptor rotors and chain rule       interaction.cpp:316-350, math.cpp:62-94
+#pragma once
+
+#include "pxd_internal.h"
+
+namespace pxd {
+
+constexpr float kCoulombF = 332.0637141491396f;
+constexpr float kEpsF = 1e-20f;  // kParamEpsilon, math.h:128
+constexpr unsigned kFull = 0xffffffffu;
+
+// ----------------------------------------------------------- compensated sums
+struct DS {
+    float hi, lo;
+};
+
+__device__ __forceinline__ void ds_add(DS& a, float b) {
+    // Knuth two-sum: s + err == a.hi + b exactly
+    const float s = a.hi + b;
+    const float bb = s - a.hi;
+    const float err = (a.hi - (s - bb)) + (b - bb);
+    a.hi = s;
+    a.lo += err;
+}
+
+__device__ __forceinline__ void ds_add_ds(DS& a, const DS& b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    const float err = (a.hi - (s - bb)) + (b.hi - bb);
+    a.hi = s;
+    a.lo = a.lo + b.lo + err;
+}
+
+// Sum over the warp; every lane returns lane 0's result.
+__device__ __forceinline__ double ds_warp_sum(DS v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        DS o;
+        o.hi = __shfl_xor_sync(kFull, v.hi, off);
+        o.lo = __shfl_xor_sync(kFull, v.lo, off);
+        ds_add_ds(v, o);
+    }
+    v.hi = __shfl_sync(kFull, v.hi, 0);
+    v.lo = __shfl_sync(kFull, v.lo, 0);
+    return static_cast<double>(v.hi) + static_cast<double>(v.lo);
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, off));
+    return __shfl_sync(kFull, v, 0);
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
+    return __shfl_sync(kFull, v, 0);
+}
+
+// Dot product of two D-vectors with exact FP32 products (fma) accumulated as a
+// compensated pair: ~44 significant bits, on the FP32 pipe.
+__device__ __forceinline__ double vdot(const float* a, const float* b, int D, int lane) {
+    DS acc{0.f, 0.f};
+    for (int e = lane; e < D; e += kWarp) {
+        const float x = a[e], y = b[e];
+        const float p = x * y;
+        const float pe = fmaf(x, y, -p);
+        ds_add(acc, p);
+        acc.lo += pe;
+    }
+    return ds_warp_sum(acc);
+}
+
+__device__ __forceinline__ double vabssum(const float* a, int D, int lane) {
+    DS acc{0.f, 0.f};
+    for (int e = lane; e < D; e += kWarp) ds_add(acc, fabsf(a[e]));
+    return ds_warp_sum(acc);
+}
+
+__device__ __forceinline__ float vabsmax(const float* a, int D, int lane) {
+    float m = 0.f;
+    for (int e = lane; e < D; e += kWarp) m = fmaxf(m, fabsf(a[e]));
+    return warp_max(m);
+}
+
+__device__ __forceinline__ void vcopy(float* dst, const float* src, int D, int lane) {
+    for (int e = lane; e < D; e += kWarp) dst[e] = src[e];
+    __syncwarp();
+}
+
+// ------------------------------------------------------------------ vectors
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) {
+    return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+__device__ __forceinline__ float3 add3(float3 a, float3 b) {
+    return make_float3(a.x + b.x, a.y + b.y, a.z + b.z);
+}
+__device__ __forceinline__ float3 mul3(float3 a, float s) {
+    return make_float3(a.x * s, a.y * s, a.z * s);
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 xyz(float4 v) { return make_float3(v.x, v.y, v.z); }
+
+__device__ __forceinline__ void atomic_add3(float4* p, float3 g) {
+    atomicAdd(&p->x, g.x);
+    atomicAdd(&p->y, g.y);
+    atomicAdd(&p->z, g.z);
+}
+__device__ __forceinline__ void atomic_sub3(float4* p, float3 g) {
+    atomicAdd(&p->x, -g.x);
+    atomicAdd(&p->y, -g.y);
+    atomicAdd(&p->z, -g.z);
+}
+
+// Rodrigues rotation and its theta-derivative (math.cpp:62-94), rows of 3.
+struct Mat3 {
+    float3 r0, r1, r2;
+};
+__device__ __forceinline__ float3 mat_apply(const Mat3& m, float3 v) {
+    return make_float3(dot3(m.r0, v), dot3(m.r1, v), dot3(m.r2, v));
+}
+__device__ __forceinline__ void rotation_and_jacobian(float3 k, float theta, Mat3& R, Mat3& J) {
+    float st, ct;
+    sincosf(theta, &st, &ct);
+    const float omc = 1.f - ct;
+    const float kxo = k.x * omc, kyo = k.y * omc, kzo = k.z * omc;
+    const float kxs = k.x * st, kys = k.y * st, kzs = k.z * st;
+    R.r0 = make_float3(ct + k.x * kxo, k.y * kxo - kzs, kys + k.z * kxo);
+    R.r1 = make_float3(kzs + k.x * kyo, ct + k.y * kyo, k.z * kyo - kxs);
+    R.r2 = make_float3(k.x * kzo - kys, kxs + k.y * kzo, ct + k.z * kzo);
+    J.r0 = make_float3(-st + k.x * kxs, -k.z * ct + k.x * kys, k.y * ct + k.x * kzs);
+    J.r1 = make_float3(k.z * ct + k.y * kxs, -st + k.y * kys, -k.x * ct + k.y * kzs);
+    J.r2 = make_float3(-k.y * ct + k.z * kxs, k.x * ct + k.z * kys, -st + k.z * kzs);
+}
+
+// ------------------------------------------------------------- term kernels
+// Adds the bonded and non-bonded terms of `t` over coordinates `X`; gradients go to
+// `G` (shared memory, atomics). Matches intra_molecular_interactions::put_gradients.
+__device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, float4* G, DS& e,
+                                           int lane) {
+    // harmonic bonds (interaction.cpp:27-47)
+    for (int s = lane; s < t.n_bond_slots; s += kWarp) {
+        const int2 ij = __ldg(&t.bond_ij[s]);
+        if (ij.x < 0) continue;
+        const float2 p = __ldg(&t.bond_p[s]);
+        const float3 d = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
+        const float r = sqrtf(dot3(d, d));
+        const float dr = r - p.y;
+        ds_add(e, 0.5f * p.x * (dr * dr));
+        const float de_dr = p.x * (1.f - p.y / (r + kEpsF));
+        const float3 g = mul3(d, de_dr);
+        atomic_sub3(&G[ij.x], g);
+        atomic_add3(&G[ij.y], g);
+    }
+    // harmonic angles (interaction.cpp:49-74, math.cpp:96-110)
+    for (int s = lane; s < t.n_angle_slots; s += kWarp) {
+        const int4 ijk = __ldg(&t.angle_ijk[s]);
+        if (ijk.x < 0) continue;
+        const float2 p = __ldg(&t.angle_p[s]);
+        const float3 xi = xyz(X[ijk.x]), xj = xyz(X[ijk.y]), xk = xyz(X[ijk.z]);
+        const float3 v0 = sub3(xj, xi), v1 = sub3(xj, xk);
+        const float3 c = cross3(v0, v1);
+        const float rp = sqrtf(dot3(c, c));
+        float3 gi = cross3(v0, c), gk = cross3(c, v1);
+        gi = mul3(gi, -1.f / (dot3(v0, v0) * rp + kEpsF));
+        gk = mul3(gk, -1.f / (dot3(v1, v1) * rp + kEpsF));
+        const float theta = atan2f(rp, dot3(v0, v1) + kEpsF);
+        const float delta = theta - p.y;
+        ds_add(e, 0.5f * p.x * (delta * delta));
+        const float de = p.x * delta;
+        const float3 fi = mul3(gi, de), fk = mul3(gk, de);
+        atomic_add3(&G[ijk.x], fi);
+        atomic_add3(&G[ijk.z], fk);
+        atomic_sub3(&G[ijk.y], add3(fi, fk));
+    }
+    // Fourier dihedrals, impropers then propers (interaction.cpp:76-117, math.cpp:130-167)
+    for (int s = lane; s < t.n_dih_slots; s += kWarp) {
+        const int4 q = __ldg(&t.dih_ijkl[s]);
+        if (q.x < 0) continue;
+        const float3 pi = xyz(X[q.x]), pj = xyz(X[q.y]), pk = xyz(X[q.z]), pl = xyz(X[q.w]);
+        const float3 rij = sub3(pj, pi), rkj = sub3(pj, pk), rkl = sub3(pl, pk);
+        const float3 m = cross3(rij, rkj), n = cross3(rkj, rkl);
+        const float3 w = cross3(m, n);
+        const float wlen = sqrtf(dot3(w, w));
+        const float phi = atan2f(wlen, dot3(m, n) + kEpsF);
+        const float theta = dot3(rij, n) < 0.f ? phi : -phi;
+        const float nrkj2 = dot3(rkj, rkj);
+        const float nrkj_1 = 1.f / (sqrtf(nrkj2) + kEpsF);
+        const float nrkj_2 = nrkj_1 * nrkj_1;
+        const float nrkj = nrkj2 * nrkj_1;
+        const float a = -nrkj / dot3(m, m);
+        const float b = nrkj / dot3(n, n);
+        const float3 gi = mul3(m, -a), gl = mul3(n, -b);
+        const float pp = dot3(rij, rkj) * nrkj_2, qq = dot3(rkj, rkl) * nrkj_2;
+        const float3 sv = sub3(mul3(gi, pp), mul3(gl, qq));
+        const float3 gj = mul3(sub3(gi, sv), -1.f), gk = mul3(add3(gl, sv), -1.f);
+        const int2 tr = __ldg(&t.dih_terms[s]);
+        float de = 0.f;
+        for (int u = 0; u < tr.y; ++u) {
+            const float4 term = __ldg(&t.dih_term[tr.x + u]);
+            const float delta = theta * term.y - term.z;
+            float sd, cd;
+            sincosf(delta, &sd, &cd);
+            ds_add(e, term.x * (1.f + cd));
+            de += term.x * term.y * sd;
+        }
+        atomic_add3(&G[q.x], mul3(gi, -de));
+        atomic_add3(&G[q.y], mul3(gj, -de));
+        atomic_add3(&G[q.z], mul3(gk, -de));
+        atomic_add3(&G[q.w], mul3(gl, -de));
+    }
+    // 1-4 and all other pairs: Coulomb + LJ 12-6 (interaction.cpp:127-168, pair.h:25-60)
+    for (int s = lane; s < t.n_pair_slots; s += kWarp) {
+        const int2 ij = __ldg(&t.pair_ij[s]);
+        if (ij.x < 0) continue;
+        const float4 p = __ldg(&t.pair_p[s]);
+        const float3 rij = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
+        const float r2 = dot3(rij, rij);
+        const float rinv = rsqrtf(r2);
+        const float rinv2 = rinv * rinv;
+        const float x = p.z * rinv2;
+        const float u6 = x * x * x;
+        const float u12 = u6 * u6;
+        const float ec = p.x * rinv;
+        ds_add(e, ec);
+        ds_add(e, p.y * (u12 - u6));
+        const float de_dr_r = (p.y * (6.f * u6 - 12.f * u12) - ec) * rinv2;
+        const float3 g = mul3(rij, de_dr_r);
+        atomic_sub3(&G[ij.x], g);
+        atomic_add3(&G[ij.y], g);
+    }
+}
+
+// Trilinear blend of the stored {E, grad} records of one map (grid.cpp:273-303).
+__device__ __forceinline__ float4 trilinear(const float4* __restrict__ m, const int* off,
+                                            const float* w) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const float4 v = __ldg(&m[off[c]]);
+        acc.x = fmaf(v.x, w[c], acc.x);
+        acc.y = fmaf(v.y, w[c], acc.y);
+        acc.z = fmaf(v.z, w[c], acc.z);
+        acc.w = fmaf(v.w, w[c], acc.w);
+    }
+    return acc;
+}
+
+// receptor_cache::get (grid.cpp:197-262) in FP32. Returns energy; adds the gradient.
+__device__ __forceinline__ float grid_lookup(const DevGrid& g, int slot, float q, float3 p,
+                                             float3& grad) {
+    float f[3] = {(p.x - g.init.x) * g.spacing_inv, (p.y - g.init.y) * g.spacing_inv,
+                  (p.z - g.init.z) * g.spacing_inv};
+    const int npm1[3] = {g.npts.x - 1, g.npts.y - 1, g.npts.z - 1};
+    int lo[3];
+    float gs[3];
+    float penalty = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (f[d] < 0.f) {
+            lo[d] = 0;
+            gs[d] = -1.f;
+            penalty -= f[d];
+            f[d] = 0.f;
+        } else if (f[d] < static_cast<float>(npm1[d])) {
+            lo[d] = static_cast<int>(f[d]);
+            gs[d] = 0.f;
+        } else {
+            lo[d] = npm1[d] - 1;
+            gs[d] = 1.f;
+            penalty += f[d] - static_cast<float>(npm1[d]);
+            f[d] = static_cast<float>(npm1[d]);
+        }
+    }
+    const int sy = g.npts.z, sx = g.npts.y * g.npts.z;
+    const int base = lo[0] * sx + lo[1] * sy + lo[2];
+    const int off[8] = {base,          base + sx,          base + sy,      base + sx + sy,
+                        base + 1,      base + sx + 1,      base + sy + 1,  base + sx + sy + 1};
+    const float x = f[0] - lo[0], y = f[1] - lo[1], z = f[2] - lo[2];
+    const float mx = 1.f - x, my = 1.f - y, mz = 1.f - z;
+    const float w[8] = {mx * my * mz, x * my * mz, mx * y * mz, x * y * mz,
+                        mx * my * z,  x * my * z,  mx * y * z,  x * y * z};
+    float e = 0.f;
+    bool hit = true;
+    if (penalty > 0.f) {
+        e += penalty * g.spacing * g.slope;
+        grad.x += gs[0] * g.slope;
+        grad.y += gs[1] * g.slope;
+        grad.z += gs[2] * g.slope;
+        hit = false;
+    }
+    const float4 c = trilinear(g.maps, off, w);
+    e += c.x * q;
+    const float4 v = slot > 0 ? trilinear(g.maps + static_cast<size_t>(slot) * g.P, off, w)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+    e += v.x;
+    if (hit) {
+        grad.x += c.y * q + v.y;
+        grad.y += c.z * q + v.z;
+        grad.z += c.w * q + v.w;
+    }
+    return e;
+}
+
+// Per-warp shared-memory slice for one pose evaluation.
+struct PoseBufs {
+    float4* lig_xyz;   // [N]
+    float4* lig_grad;  // [N]
+    float4* loc_xyz;   // [n_local]
+    float4* loc_grad;  // [n_local]
+    float4* mov_jac;   // [n_mov]
+};
+
+struct EvalEnv {
+    DevReceptor rec;
+    DevGrid grid;
+};
+
+// Energy and flat gradient [dE/dxyz (3N) | dE/dtorsion (R)] at x0 + t * d (d may be
+// null: evaluate at x0). Replaces binding_system_interactions::put_gradients as the
+// optimiser's closure calls it (optimizer.cpp:155-167).
+static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const float* x0,
+                            const float* d, float t, float* gout, const PoseBufs& b, int lane) {
+    const int N = L.n_atoms;
+    const int n3 = 3 * N;
+    const DevReceptor& R = env.rec;
+    for (int a = lane; a < N; a += kWarp) {
+        float px = x0[3 * a], py = x0[3 * a + 1], pz = x0[3 * a + 2];
+        if (d) {
+            px = fmaf(d[3 * a], t, px);
+            py = fmaf(d[3 * a + 1], t, py);
+            pz = fmaf(d[3 * a + 2], t, pz);
+        }
+        b.lig_xyz[a] = make_float4(px, py, pz, 0.f);
+        b.lig_grad[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    // receptor rotors (receptor_torsion2xyz, interaction.cpp:316-336)
+    for (int l = lane; l < R.n_local; l += kWarp) {
+        const float4 v = __ldg(&R.local_xyz0[l]);
+        if (l < R.n_mov) {
+            const int r = __float_as_int(v.w);
+            float th = x0[n3 + r];
+            if (d) th = fmaf(d[n3 + r], t, th);
+            Mat3 Rm, Jm;
+            rotation_and_jacobian(xyz(__ldg(&R.rotor_axis[r])), th, Rm, Jm);
+            const float3 rel = xyz(v);
+            const float3 pos = add3(mat_apply(Rm, rel), xyz(__ldg(&R.rotor_origin[r])));
+            b.loc_xyz[l] = make_float4(pos.x, pos.y, pos.z, 0.f);
+            const float3 jac = mat_apply(Jm, rel);
+            b.mov_jac[l] = make_float4(jac.x, jac.y, jac.z, 0.f);
+        } else {
+            b.loc_xyz[l] = v;
+        }
+        b.loc_grad[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncwarp();
+    DS e{0.f, 0.f};
+    topo_terms(L.topo, b.lig_xyz, b.lig_grad, e, lane);
+    if (R.n_local > 0) topo_terms(R.intra, b.loc_xyz, b.loc_grad, e, lane);
+    // grid lookups (inter_molecular_interactions, cached branch)
+    if (env.grid.has_grid) {
+        for (int a = lane; a < N; a += kWarp) {
+            float3 g = make_float3(0.f, 0.f, 0.f);
+            const float ea = grid_lookup(env.grid, __ldg(&L.map_slot[a]), __ldg(&L.charge[a]),
+                                         xyz(b.lig_xyz[a]), g);
+            ds_add(e, ea);
+            atomic_add3(&b.lig_grad[a], g);
+        }
+    }
+    // explicit inter pairs (rotor atoms with maps, every receptor atom without)
+    const int M = R.n_explicit;
+    if (M >= kWarp) {
+        for (int i = 0; i < N; ++i) {
+            const float3 xi = xyz(b.lig_xyz[i]);
+            const float qi = __ldg(&L.charge[i]);
+            const float2 sei = __ldg(&L.se[i]);
+            float3 gi = make_float3(0.f, 0.f, 0.f);
+            for (int j = lane; j < M; j += kWarp) {
+                const int loc = __ldg(&R.ex_local[j]);
+                const float4 rj = __ldg(&R.ex_xyzq[j]);
+                const float3 xj = loc >= 0 ? xyz(b.loc_xyz[loc]) : xyz(rj);
+                const float2 sej = __ldg(&R.ex_se[j]);
+                const float3 rij = sub3(xj, xi);
+                const float r2 = dot3(rij, rij);
+                const float rinv = rsqrtf(r2);
+                const float rinv2 = rinv * rinv;
+                const float s = (sei.x + sej.x) * 0.5f;
+                const float xx = s * s * rinv2;
+                const float u6 = xx * xx * xx, u12 = u6 * u6;
+                const float C = sqrtf(sei.y * sej.y) * 4.f;
+                const float ec = kCoulombF * qi * rj.w * rinv;
+                ds_add(e, ec);
+                ds_add(e, C * (u12 - u6));
+                const float3 g = mul3(rij, (C * (6.f * u6 - 12.f * u12) - ec) * rinv2);
+                gi = sub3(gi, g);
+                if (loc >= 0) atomic_add3(&b.loc_grad[loc], g);
+            }
+            gi.x = warp_sum_f(gi.x);
+            gi.y = warp_sum_f(gi.y);
+            gi.z = warp_sum_f(gi.z);
+            if (lane == 0) atomic_add3(&b.lig_grad[i], gi);
+        }
+    } else if (M > 0) {
+        for (int i = lane; i < N; i += kWarp) {
+            const float3 xi = xyz(b.lig_xyz[i]);
+            const float qi = __ldg(&L.charge[i]);
+            const float2 sei = __ldg(&L.se[i]);
+            float3 gi = make_float3(0.f, 0.f, 0.f);
+            for (int j = 0; j < M; ++j) {
+                const int loc = __ldg(&R.ex_local[j]);
+                const float4 rj = __ldg(&R.ex_xyzq[j]);
+                const float3 xj = loc >= 0 ? xyz(b.loc_xyz[loc]) : xyz(rj);
+                const float2 sej = __ldg(&R.ex_se[j]);
+                const float3 rij = sub3(xj, xi);
+                const float r2 = dot3(rij, rij);
+                const float rinv = rsqrtf(r2);
+                const float rinv2 = rinv * rinv;
+                const float s = (sei.x + sej.x) * 0.5f;
+                const float xx = s * s * rinv2;
+                const float u6 = xx * xx * xx, u12 = u6 * u6;
+                const float C = sqrtf(sei.y * sej.y) * 4.f;
+                const float ec = kCoulombF * qi * rj.w * rinv;
+                ds_add(e, ec);
+                ds_add(e, C * (u12 - u6));
+                const float3 g = mul3(rij, (C * (6.f * u6 - 12.f * u12) - ec) * rinv2);
+                gi = sub3(gi, g);
+                if (loc >= 0) atomic_add3(&b.loc_grad[loc], g);
+            }
+            atomic_add3(&b.lig_grad[i], gi);
+        }
+    }
+    __syncwarp();
+    // flat gradient and the receptor-torsion chain rule (interaction.cpp:338-350)
+    for (int a = lane; a < N; a += kWarp) {
+        const float4 g = b.lig_grad[a];
+        gout[3 * a] = g.x;
+        gout[3 * a + 1] = g.y;
+        gout[3 * a + 2] = g.z;
+    }
+    for (int r = lane; r < R.n_rotors; r += kWarp) {
+        float acc = 0.f;
+        const int l0 = __ldg(&R.rotor_mov[r]), l1 = __ldg(&R.rotor_mov[r + 1]);
+        for (int l = l0; l < l1; ++l) acc += dot3(xyz(b.mov_jac[l]), xyz(b.loc_grad[l]));
+        gout[n3 + r] = acc;
+    }
+    __syncwarp();
+    return ds_warp_sum(e) + R.e_const;
+}
+
+// Shared-memory floats needed by PoseBufs for a ligand of up to n_atoms atoms.
+__host__ __device__ inline int pose_bufs_floats(int n_atoms, int n_local) {
+    return 8 * n_atoms + 12 * n_local;
+}
+
+__device__ inline PoseBufs carve_pose_bufs(float* base, int n_atoms, int n_local) {
+    PoseBufs b;
+    b.lig_xyz = reinterpret_cast<float4*>(base);
+    b.lig_grad = b.lig_xyz + n_atoms;
+    b.loc_xyz = b.lig_grad + n_atoms;
+    b.loc_grad = b.loc_xyz + n_local;
+    b.mov_jac = b.loc_grad + n_local;
+    return b;
+}
+
+}  // namespace pxd

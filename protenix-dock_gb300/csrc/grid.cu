@@ -1,0 +1,145 @@
+// Receptor map build on the GPU: replaces receptor_cache::populate and
+// partial_worker::populate (grid.cpp:115-195).
+//
+// One thread per (grid point, map); a block covers 128 consecutive points (k fastest)
+// of one map, so all its threads read the same receptor-atom tile from shared memory
+// (broadcast). Pair terms are FP32; each 256-atom tile's partial sums are folded into
+// FP64 accumulators, which keeps the Coulomb sum over ~2k atoms of mixed sign accurate.
+// The squared distance is floored at 1e-4 A^2 so that a grid point sitting on an atom
+// cannot overflow FP32, and records are clamped to +-1e30 before the FP32 store.
+#include "device_eval.cuh"
+#include "../../include/pxdock_gb300_vdw.h"
+
+namespace pxd {
+
+constexpr int kGridThreads = 128;
+constexpr int kGridTile = 256;
+constexpr float kR2Floor = 1e-4f;
+constexpr double kRecordCeil = 1e30;
+
+struct GridArgs {
+    const float4* atoms;   // x, y, z, charge of every non-rotor receptor atom
+    const float2* se;      // sigma, epsilon
+    int n_atoms;
+    int3 npts;
+    double3 init;
+    double spacing;
+    const int* slot_type;  // [n_slots] ligand type, or -1 for the Coulomb map
+    const float2* type_se; // [99] sigma, epsilon of the ligand types
+    float4* maps;
+    int P;
+};
+
+__device__ __forceinline__ float clampf_rec(double v) {
+    return static_cast<float>(fmin(fmax(v, -kRecordCeil), kRecordCeil));
+}
+
+__global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs a) {
+    __shared__ float4 s_xyzq[kGridTile];
+    __shared__ float2 s_se[kGridTile];
+    const int p = blockIdx.x * kGridThreads + threadIdx.x;
+    const int slot = blockIdx.y;
+    const int type = a.slot_type[slot];
+    const bool coul = type < 0;
+    const float2 tse = coul ? make_float2(0.f, 0.f) : a.type_se[type];
+    const int nz = a.npts.z, ny = a.npts.y;
+    const int k = p % nz;
+    const int j = (p / nz) % ny;
+    const int i = p / (nz * ny);
+    // grid.cpp:159-163: point = init + spacing * index, formed in FP64
+    const float3 pt = make_float3(static_cast<float>(a.init.x + a.spacing * i),
+                                  static_cast<float>(a.init.y + a.spacing * j),
+                                  static_cast<float>(a.init.z + a.spacing * k));
+    double E = 0.0, GX = 0.0, GY = 0.0, GZ = 0.0;
+    for (int t0 = 0; t0 < a.n_atoms; t0 += kGridTile) {
+        const int n = min(kGridTile, a.n_atoms - t0);
+        __syncthreads();
+        for (int u = threadIdx.x; u < n; u += kGridThreads) {
+            s_xyzq[u] = a.atoms[t0 + u];
+            s_se[u] = a.se[t0 + u];
+        }
+        __syncthreads();
+        float e = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+        if (coul) {
+            for (int u = 0; u < n; ++u) {
+                const float4 at = s_xyzq[u];
+                const float vx = at.x - pt.x, vy = at.y - pt.y, vz = at.z - pt.z;
+                const float r2 = fmaxf(vx * vx + vy * vy + vz * vz, kR2Floor);
+                const float rinv = rsqrtf(r2);
+                const float qr = at.w * rinv;
+                e += qr;
+                // dE/dpoint = q (atom - point) / r^3 (pair.h:25-40 with grad_i -= ...)
+                const float w = qr * rinv * rinv;
+                gx = fmaf(vx, w, gx);
+                gy = fmaf(vy, w, gy);
+                gz = fmaf(vz, w, gz);
+            }
+            E += static_cast<double>(e) * kCoulombF;
+            GX += static_cast<double>(gx) * kCoulombF;
+            GY += static_cast<double>(gy) * kCoulombF;
+            GZ += static_cast<double>(gz) * kCoulombF;
+        } else {
+            for (int u = 0; u < n; ++u) {
+                const float4 at = s_xyzq[u];
+                const float2 se = s_se[u];
+                const float vx = at.x - pt.x, vy = at.y - pt.y, vz = at.z - pt.z;
+                const float r2 = fmaxf(vx * vx + vy * vy + vz * vz, kR2Floor);
+                const float rinv2 = 1.f / r2;
+                const float s = (tse.x + se.x) * 0.5f;
+                const float x = s * s * rinv2;
+                const float u6 = x * x * x;
+                const float u12 = u6 * u6;
+                const float C = sqrtf(tse.y * se.y) * 4.f;
+                e = fmaf(C, u12 - u6, e);
+                // grad_point -= vec * de_dr_r, de_dr_r = C(-12 u12 + 6 u6) / r^2 (pair.h:42-60)
+                const float w = C * (12.f * u12 - 6.f * u6) * rinv2;
+                gx = fmaf(vx, w, gx);
+                gy = fmaf(vy, w, gy);
+                gz = fmaf(vz, w, gz);
+            }
+            E += e;
+            GX += gx;
+            GY += gy;
+            GZ += gz;
+        }
+    }
+    if (p < a.P) {
+        a.maps[static_cast<size_t>(slot) * a.P + p] =
+            make_float4(clampf_rec(E), clampf_rec(GX), clampf_rec(GY), clampf_rec(GZ));
+    }
+}
+
+int launch_grid_build(pxd_context* ctx, const float4* atoms, const float2* se, int n_atoms,
+                      const int* slot_type, int n_slots, float4* maps) {
+    GridArgs a;
+    a.atoms = atoms;
+    a.se = se;
+    a.n_atoms = n_atoms;
+    a.npts = make_int3(ctx->box.npoints[0], ctx->box.npoints[1], ctx->box.npoints[2]);
+    a.init = make_double3(ctx->box.init_xyz[0], ctx->box.init_xyz[1], ctx->box.init_xyz[2]);
+    a.spacing = ctx->box.spacing;
+    a.slot_type = slot_type;
+    a.maps = maps;
+    a.P = ctx->grid.P;
+    // ligand type table on the device (sigma, epsilon)
+    float2 table[PXD_NUM_VDW_TYPES];
+    for (int t = 0; t < PXD_NUM_VDW_TYPES; ++t)
+        table[t] = make_float2(static_cast<float>(PXD_VDW_SIGMA[t]),
+                               static_cast<float>(PXD_VDW_EPSILON[t]));
+    float2* d_table = nullptr;
+    int rc = cuda_check(ctx, cudaMallocAsync(&d_table, sizeof(table), ctx->stream), "type table");
+    if (rc) return rc;
+    rc = cuda_check(ctx, cudaMemcpyAsync(d_table, table, sizeof(table), cudaMemcpyHostToDevice,
+                                         ctx->stream),
+                    "type table copy");
+    if (rc) return rc;
+    a.type_se = d_table;
+    dim3 grid((a.P + kGridThreads - 1) / kGridThreads, n_slots);
+    grid_build_kernel<<<grid, kGridThreads, 0, ctx->stream>>>(a);
+    rc = cuda_check(ctx, cudaGetLastError(), "grid_build_kernel launch");
+    cudaFreeAsync(d_table, ctx->stream);
+    if (rc) return rc;
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "grid build");
+}
+
+}  // namespace pxd

@@ -1,0 +1,154 @@
+// Internal host/device declarations of the GB300 docking library.
+//
+// Device layout (all FP32 unless noted; one allocation per ligand / receptor):
+//   maps      float4 [n_slots][P]   {E, dE/dx, dE/dy, dE/dz}, k fastest; slot 0 = Coulomb
+//   ligand    term lists reordered into "rounds" of 32 slots in which no atom occurs
+//             twice, so that the 32 lanes of a warp add gradients to distinct atoms;
+//             unused slots carry atom index -1 and are skipped.
+//   receptor  explicit-pair atoms (rotor atoms when maps exist, every atom otherwise),
+//             rotor tables, and the receptor intra terms that touch a rotor atom over a
+//             compact local atom space [rotor atoms | fixed atoms they reference].
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pxdock_gb300.h"
+
+namespace pxd {
+
+constexpr int kWarp = 32;
+constexpr int kMaxDihTerms = 6;
+
+// Molecule terms on the device (ligand, or the receptor's rotor-touching terms).
+struct DevTopo {
+    int n_atoms;
+    int n_bond_slots, n_angle_slots, n_dih_slots, n_pair_slots;  // multiples of 32
+    const int2* bond_ij;      // -1 = empty slot
+    const float2* bond_p;     // k, r0
+    const int4* angle_ijk;    // i, j (vertex), k, -
+    const float2* angle_p;    // k, theta0
+    const int4* dih_ijkl;
+    const int2* dih_terms;    // first term, number of terms
+    const float4* dih_term;   // k, periodicity, phase, -
+    const int2* pair_ij;
+    const float4* pair_p;     // A = 332.06 qi qj s_c, C = 4 sqrt(ei ej) s_v, S2 = ((si+sj)/2)^2
+};
+
+struct DevLigand {
+    DevTopo topo;
+    int n_atoms;
+    const float* charge;      // [N]
+    const int* map_slot;      // [N] vdW map slot of the atom's type (-1: no map)
+    const float2* se;         // [N] sigma, epsilon (explicit inter pairs)
+    // torsion tree (forward kinematics, data.cpp:592-641)
+    int n_frags, n_tors;
+    const int* perm;          // [N]
+    const int* frag_range;    // [2*F]
+    const int4* tors;         // [T] frag, parent frag, parent atom, mine atom (positions)
+    const int* is_root;       // [F]
+};
+
+struct DevReceptor {
+    int n_explicit;           // atoms paired explicitly with every ligand atom
+    const float4* ex_xyzq;    // fixed position, charge
+    const float2* ex_se;      // sigma, epsilon
+    const int* ex_local;      // local index of a rotor atom (< n_mov) or -1 if fixed
+    int n_rotors, n_mov, n_local;
+    const float4* rotor_origin;   // [R]
+    const float4* rotor_axis;     // [R] unit
+    const int* rotor_mov;         // [R+1] rotor atoms are local [rotor_mov[r], rotor_mov[r+1])
+    const float4* local_xyz0;     // [n_local] input coordinates (rotor atoms: x0 - origin)
+    DevTopo intra;                // rotor-touching receptor terms over local atoms
+    double e_const;               // energy of the receptor terms that touch no rotor atom
+};
+
+struct DevGrid {
+    int has_grid;
+    float3 init;
+    int3 npts;                // points per axis
+    float spacing, spacing_inv;
+    float slope;
+    int P;
+    const float4* maps;
+};
+
+// Flat DOF layout of a pose: [ligand xyz (3N) | receptor torsions (T_r)] (optimizer.cpp:56-76)
+struct HostTopoBuffers;
+
+struct LigandEntry {
+    DevLigand dev;
+    void* mem = nullptr;      // single device allocation
+    int n_atoms = 0;
+    int n_tors = 0;
+    std::vector<int32_t> types;
+};
+
+}  // namespace pxd
+
+struct pxd_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string error;
+    int n_sm = 0;
+    // receptor
+    bool has_receptor = false;
+    int n_rec = 0;
+    std::vector<double> rec_xyz;          // [M][3]
+    std::vector<double> rec_charge, rec_sigma, rec_epsilon;
+    std::vector<int> mov_atoms;           // rotor atoms (axis atom removed), grouped by rotor
+    std::vector<int> mov_rotor;
+    std::vector<int> rotor_mov_off;       // [R+1]
+    std::vector<double> rotor_origin, rotor_axis;
+    std::vector<uint8_t> is_mov;
+    pxd::DevReceptor rec{};
+    void* rec_mem = nullptr;
+    void* rec_ex_all = nullptr;           // explicit list with every receptor atom (no maps)
+    void* rec_ex_mov = nullptr;           // explicit list with rotor atoms (maps present)
+    int n_ex_all = 0, n_ex_mov = 0;
+    size_t ex_all_off[3] = {0, 0, 0}, ex_mov_off[3] = {0, 0, 0};
+    // maps
+    pxd::DevGrid grid{};
+    pxd_box box{};
+    double slope = 0.0;
+    float4* maps = nullptr;
+    int type_slot[PXD_NUM_VDW_TYPES];
+    int n_slots = 0;
+    // ligands
+    std::vector<pxd::LigandEntry> ligands;
+    pxd::DevLigand* d_ligands = nullptr;  // device copy of every entry's DevLigand
+    int d_ligands_cap = 0;
+    bool ligands_dirty = true;
+    // scratch
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int* d_counter = nullptr;
+};
+
+namespace pxd {
+
+int set_error(pxd_context* ctx, int code, const std::string& msg);
+int cuda_check(pxd_context* ctx, cudaError_t e, const char* what);
+int ensure_scratch(pxd_context* ctx, size_t bytes);
+int sync_ligand_table(pxd_context* ctx);
+int refresh_ligand_slots(pxd_context* ctx);
+
+// kernels (launchers), one per translation unit
+int launch_grid_build(pxd_context* ctx, const float4* atoms_xyzq, const float2* atoms_se,
+                      int n_atoms, const int* slot_types, int n_slots, float4* maps);
+int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_ids,
+                 const float* xyz, const float* tors, double* energy, float* lig_grad,
+                 float* tors_grad, cudaStream_t s);
+int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int max_atoms,
+                 const int* lig_ids, float* xyz, float* tors, double* energy, int* nevals,
+                 int* status, cudaStream_t s);
+int launch_ligand_kinematics(pxd_context* ctx, int lig, int n_poses, const float* xyz_in,
+                             const float* centers, const float* rots, const float* tors,
+                             float* xyz_out, cudaStream_t s);
+int launch_receptor_kinematics(pxd_context* ctx, int n_poses, const float* tors, float* out,
+                               cudaStream_t s);
+
+}  // namespace pxd

@@ -1,0 +1,221 @@
+"""ctypes binding of libpxdock_gb300.so (the C ABI in include/pxdock_gb300.h).
+
+The library is required: importing this module without a built library raises, and
+every call that reports an error status raises NativeError with the library's message.
+There is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi, build
+
+_lib = None
+
+
+class NativeError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("pxdock_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load(auto_build=False):
+    """Loads the native library (building it first when auto_build is set)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = build.lib_path()
+    if auto_build:
+        path = build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("native library %s is missing: run build() first" % path)
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    lib.pxd_abi_version.restype = C.c_int32
+    lib.pxd_version.restype = C.c_char_p
+    lib.pxd_context_create.argtypes = [C.c_int32, C.POINTER(vp)]
+    lib.pxd_context_destroy.argtypes = [vp]
+    lib.pxd_last_error.argtypes = [vp]
+    lib.pxd_last_error.restype = C.c_char_p
+    lib.pxd_context_stream.argtypes = [vp]
+    lib.pxd_context_stream.restype = vp
+    lib.pxd_lbfgs_defaults.argtypes = [C.POINTER(abi.LbfgsParams)]
+    lib.pxd_set_receptor.argtypes = [vp, C.POINTER(abi.ReceptorDesc)]
+    lib.pxd_decide_grid_dims.argtypes = [C.c_double] * 7 + [C.POINTER(abi.Box)]
+    lib.pxd_grid_build.argtypes = [vp, C.POINTER(abi.Box), abi.i32p, C.c_int32]
+    lib.pxd_grid_set_slope.argtypes = [vp, C.c_double]
+    lib.pxd_grid_drop.argtypes = [vp]
+    lib.pxd_grid_info.argtypes = [vp, C.POINTER(abi.Box), abi.i32p]
+    lib.pxd_grid_read_map.argtypes = [vp, C.c_int32, abi.f32p]
+    lib.pxd_grid_write_map.argtypes = [vp, C.POINTER(abi.Box), C.c_int32, abi.f32p]
+    lib.pxd_add_ligand.argtypes = [vp, C.POINTER(abi.LigandDesc), abi.i32p]
+    lib.pxd_clear_ligands.argtypes = [vp]
+    lib.pxd_score_grad_dev.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp]
+    lib.pxd_score_grad.argtypes = [vp, C.c_int32, C.c_int32, abi.f64p, abi.f64p, abi.f64p,
+                                   abi.f64p, abi.f64p]
+    lib.pxd_lbfgs_dev.argtypes = [vp, C.POINTER(abi.LbfgsParams), C.c_int32, C.c_int32, vp, vp, vp,
+                                  vp, vp, vp, vp]
+    lib.pxd_lbfgs.argtypes = [vp, C.POINTER(abi.LbfgsParams), C.c_int32, C.c_int32, abi.f64p,
+                              abi.f64p, abi.f64p, abi.i32p, abi.i32p]
+    lib.pxd_ligand_kinematics.argtypes = [vp, C.c_int32, C.c_int32, abi.f64p, abi.f64p, abi.f64p,
+                                          abi.f64p, abi.f64p]
+    lib.pxd_receptor_kinematics.argtypes = [vp, C.c_int32, abi.f64p, abi.f64p]
+    _lib = lib
+    return lib
+
+
+def _p(a, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def _f64(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+class Context:
+    """One receptor on one GPU (pxd_context)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.pxd_context_create(device, C.byref(h))
+        if rc != 0:
+            raise NativeError(rc, "cannot create a context on CUDA device %d" % device)
+        self.h = h
+        self._keep = []
+        self.ligands = []
+        self.n_rotors = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pxd_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise NativeError(rc, self.lib.pxd_last_error(self.h).decode())
+
+    @property
+    def stream(self):
+        return self.lib.pxd_context_stream(self.h)
+
+    def set_receptor(self, receptor):
+        keep = []
+        desc = receptor.to_c(keep)
+        self._check(self.lib.pxd_set_receptor(self.h, C.byref(desc)))
+        self.n_rotors = receptor.n_rotors
+        self.receptor = receptor
+
+    def build_grid(self, box, types=None):
+        if types is None:
+            self._check(self.lib.pxd_grid_build(self.h, C.byref(box), None, -1))
+        else:
+            t = np.ascontiguousarray(np.asarray(sorted(set(int(x) for x in types)), np.int32))
+            self._check(self.lib.pxd_grid_build(self.h, C.byref(box), _p(t, C.c_int32), len(t)))
+        self.box = box
+
+    def set_slope(self, slope):
+        self._check(self.lib.pxd_grid_set_slope(self.h, slope))
+
+    def drop_grid(self):
+        self._check(self.lib.pxd_grid_drop(self.h))
+
+    def read_map(self, m):
+        box = abi.Box()
+        n = C.c_int32()
+        self._check(self.lib.pxd_grid_info(self.h, C.byref(box), C.byref(n)))
+        P = box.npoints[0] * box.npoints[1] * box.npoints[2]
+        out = np.zeros((P, 4), np.float32)
+        self._check(self.lib.pxd_grid_read_map(self.h, m, _p(out, C.c_float)))
+        return out
+
+    def write_map(self, box, m, records):
+        r = np.ascontiguousarray(np.asarray(records, np.float32))
+        self._check(self.lib.pxd_grid_write_map(self.h, C.byref(box), m, _p(r, C.c_float)))
+
+    def add_ligand(self, ligand):
+        keep = []
+        desc = ligand.to_c(keep)
+        lid = C.c_int32()
+        self._check(self.lib.pxd_add_ligand(self.h, C.byref(desc), C.byref(lid)))
+        self.ligands.append(ligand)
+        return lid.value
+
+    def clear_ligands(self):
+        self._check(self.lib.pxd_clear_ligands(self.h))
+        self.ligands = []
+
+    def score_grad(self, lig, xyz, tors=None):
+        xyz = _f64(xyz)
+        n = xyz.shape[0] if xyz.ndim == 3 else 1
+        N = self.ligands[lig].n_atoms
+        xyz = xyz.reshape(n, N, 3)
+        tors = _f64(np.zeros((n, self.n_rotors)) if tors is None else tors).reshape(n, self.n_rotors)
+        e = np.zeros(n)
+        g = np.zeros((n, N, 3))
+        tg = np.zeros((n, self.n_rotors))
+        dummy = np.zeros(1)
+        self._check(self.lib.pxd_score_grad(self.h, lig, n, _p(xyz), _p(tors if tors.size else dummy),
+                                            _p(e), _p(g), _p(tg if tg.size else dummy)))
+        return e, g, tg
+
+    def lbfgs(self, params, lig, xyz, tors=None):
+        xyz = _f64(xyz)
+        n = xyz.shape[0] if xyz.ndim == 3 else 1
+        N = self.ligands[lig].n_atoms
+        xyz = xyz.reshape(n, N, 3).copy()
+        tors = _f64(np.zeros((n, self.n_rotors)) if tors is None else tors).reshape(n, self.n_rotors).copy()
+        e = np.zeros(n)
+        nev = np.zeros(n, np.int32)
+        st = np.zeros(n, np.int32)
+        dummy = np.zeros(1)
+        self._check(self.lib.pxd_lbfgs(self.h, C.byref(params), lig, n, _p(xyz),
+                                       _p(tors if tors.size else dummy), _p(e), _p(nev, C.c_int32),
+                                       _p(st, C.c_int32)))
+        return dict(xyz=xyz, torsions=tors, energy=e, nevals=nev, status=st)
+
+    def score_grad_dev(self, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
+                       lig_grad_ptr, tors_grad_ptr, stream=None):
+        """Device-pointer call; pointers are integer device addresses."""
+        self._check(self.lib.pxd_score_grad_dev(self.h, n_poses, max_atoms, ids_ptr, xyz_ptr,
+                                                tors_ptr, energy_ptr, lig_grad_ptr, tors_grad_ptr,
+                                                stream))
+
+    def lbfgs_dev(self, params, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
+                  nevals_ptr, status_ptr, stream=None):
+        self._check(self.lib.pxd_lbfgs_dev(self.h, C.byref(params), n_poses, max_atoms, ids_ptr,
+                                           xyz_ptr, tors_ptr, energy_ptr, nevals_ptr, status_ptr,
+                                           stream))
+
+    def ligand_kinematics(self, lig, xyz, centers, rots, torsions):
+        centers = _f64(centers).reshape(-1, 3)
+        n = centers.shape[0]
+        N = self.ligands[lig].n_atoms
+        T = self.ligands[lig].n_torsions
+        rots = _f64(rots).reshape(n, 9)
+        tors = _f64(torsions).reshape(n, T) if T else np.zeros((n, 1))
+        out = np.zeros((n, N, 3))
+        self._check(self.lib.pxd_ligand_kinematics(self.h, lig, n, _p(_f64(xyz).reshape(-1)),
+                                                   _p(centers), _p(rots), _p(tors), _p(out)))
+        return out
+
+    def receptor_kinematics(self, torsions):
+        t = _f64(torsions).reshape(-1, self.n_rotors)
+        n = t.shape[0]
+        out = np.zeros((n, self.receptor.n_atoms, 3))
+        self._check(self.lib.pxd_receptor_kinematics(self.h, n, _p(t if t.size else np.zeros(1)),
+                                                     _p(out)))
+        return out
+
+
+def lbfgs_params(**kw):
+    """pxd_lbfgs_params with the reference defaults (pxd_lbfgs_defaults) overridden by kw."""
+    p = abi.LbfgsParams()
+    load().pxd_lbfgs_defaults(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
