@@ -56,6 +56,11 @@ enum pxd_pose_status {
     PXD_POSE_BAD_INPUT = 3      /* pose rejected before optimisation (bad ligand id) */
 };
 
+/* ------------------------------------------------------------------ limits */
+#define PXD_NUM_VDW_TYPES 99          /* ligand vdW types (kNumVdwTypes, constant.h:26) */
+#define PXD_MAX_LIGAND_ATOMS 256
+#define PXD_MAX_RECEPTOR_TORSIONS 64
+
 /* --------------------------------------------------------------- data model */
 
 /* Force-field terms of one molecule; the layout follows force_field_params
@@ -96,6 +101,63 @@ typedef struct pxd_topology {
     const int32_t* pairs;        /* [n][2]  all other non-bonded pairs, scale 1 */
 } pxd_topology;
 
+/* Interaction atom lists of one molecule used by the empirical scores (the pscore /
+ * bscore fields of force_field_params, system.h:95-108). Rings are [n][6] atom ids,
+ * padded with -1 after the ring's last atom. Donors are (heavy atom, hydrogen). The
+ * torsion-strain lists are ligand-only: entry e has coefficients tstrain_coefs[e][4] and
+ * the matched quadruples tstrain_quads[tstrain_offsets[e] .. tstrain_offsets[e+1]). */
+typedef struct pxd_score_lists {
+    int32_t n_hydrophobic; const int32_t* hydrophobic;
+    int32_t n_cation; const int32_t* cation;
+    int32_t n_anion; const int32_t* anion;
+    int32_t n_ring5; const int32_t* ring5;
+    int32_t n_ring6; const int32_t* ring6;
+    int32_t n_don_charged; const int32_t* don_charged;
+    int32_t n_don_neutral; const int32_t* don_neutral;
+    int32_t n_acc_charged; const int32_t* acc_charged;
+    int32_t n_acc_neutral; const int32_t* acc_neutral;
+    int32_t n_tstrain; const double* tstrain_coefs; const int32_t* tstrain_offsets;
+    const int32_t* tstrain_quads;
+    int32_t n_rotatable;
+    const int32_t* atomic_numbers;   /* [n_atoms], may be NULL when GBSA is off */
+    int32_t n_all_bonds; const int32_t* all_bonds;
+} pxd_score_lists;
+
+/* Empirical score terms, in the order of their coefficients in pxd_sf_params. */
+enum pxd_score_term {
+    PXD_TERM_COULOMB = 0,     /* InteractionCoulomb_oriEnergy */
+    PXD_TERM_VDW = 1,         /* InteractionVDW_Energy */
+    PXD_TERM_IONIC = 2,       /* Ionic_Energy */
+    PXD_TERM_PI_CATION = 3,   /* Pi_Cationic_Energy */
+    PXD_TERM_F2F = 4,         /* F2FPiStacking_Energy */
+    PXD_TERM_E2F = 5,         /* E2FPiStacking_Energy */
+    PXD_TERM_HBOND = 6,       /* Hbond_Energy */
+    PXD_TERM_HYDROPHOBIC = 7, /* Hydrophobic_Energy */
+    PXD_TERM_TSTRAIN = 8,     /* TorsionStrain_Penalty */
+    PXD_TERM_ROTATABLE = 9,   /* rotatable_energy */
+    PXD_TERM_GBSA = 10,       /* Gbsa_Com_Energy-Gbsa_Lig_Energy-Gbsa_Pro_Energy */
+    PXD_NUM_TERMS = 11
+};
+
+/* One scoring function (ScoringFunctionParams, conf.h:122-150) with the parameters of
+ * its active terms. coef[t] is the weight of term t as root_scorer::combine applies it
+ * (scorer.cpp:117-126); a term is active when |coef| > 1e-5 (utility.h:26). */
+typedef struct pxd_sf_params {
+    double coef[PXD_NUM_TERMS];
+    double vdw_scale, vdw_cutoff;
+    double vdw_sigma_scale[PXD_NUM_VDW_TYPES], vdw_epsilon_scale[PXD_NUM_VDW_TYPES];
+    double ionic_coef[2];              /* lc, pc */
+    double ionic[2][2];                /* dist_min, dist_max */
+    double picat_coef[4];              /* lc5, lc6, pc5, pc6 */
+    double picat[4][2];                /* dist_min, dist_max */
+    double stack_coef[2][4];           /* [f2f, e2f][l5r5, l5r6, l6r5, l6r6] */
+    double stack[2][4][6];             /* dist_min, dist_max, angle_min, angle_max, sigma_min, sigma_max */
+    double hbond_scale;
+    double hbond_coef[8];              /* hldcc hldcn hldnc hldnn hpdcc hpdcn hpdnc hpdnn */
+    double hbond[8][6];                /* dist_min, dist_max, angle_min, angle_max, dist_center, angle_center */
+    double hydro_scale, hydro_dist_min, hydro_dist_max, hydro_scale_factor;
+} pxd_sf_params;
+
 /* Ligand torsion tree (fragment_tree, system.h:135-154) in a flat form. Fragments
  * are numbered as in the ligand file. Atom positions are "permuted" positions:
  * position p holds atom perm[p], and fragment f owns positions
@@ -121,6 +183,7 @@ typedef struct pxd_ligand_desc {
     pxd_topology ff;             /* sigma/epsilon taken from the ligand vdW type table */
     const int32_t* vdw_type;     /* [n_atoms] ligand vdW type 0..98 (kVdwTypeTags order) */
     pxd_torsion_tree tree;       /* may have n_frags == 0 for optimisation-only use */
+    const pxd_score_lists* lists;/* NULL: the ligand cannot be scored by pxd_score_* */
 } pxd_ligand_desc;
 
 /* The receptor (torsional_receptor, data.h:34-67). Rotor r turns the atoms
@@ -135,6 +198,7 @@ typedef struct pxd_receptor_desc {
     const int32_t* rotor_axis;   /* [n_rotors][2] */
     const int32_t* rotor_offsets;/* [n_rotors+1] */
     const int32_t* rotor_atoms;  /* [rotor_offsets[n_rotors]] */
+    const pxd_score_lists* lists;/* NULL: no empirical scores for this receptor */
 } pxd_receptor_desc;
 
 /* Grid box (box_config, grid.h:31-40). */
@@ -162,9 +226,6 @@ typedef struct pxd_lbfgs_params {
 } pxd_lbfgs_params;
 
 #define PXD_MAX_HISTORY 128
-#define PXD_NUM_VDW_TYPES 99
-#define PXD_MAX_LIGAND_ATOMS 256
-#define PXD_MAX_RECEPTOR_TORSIONS 64
 
 /* ------------------------------------------------------------------ context */
 typedef struct pxd_context pxd_context;
@@ -264,6 +325,31 @@ int pxd_ligand_kinematics(pxd_context* ctx, int32_t ligand_id, int32_t n_poses,
  * (data.cpp:366-385). out: [n_poses][n_atoms][3]. */
 int pxd_receptor_kinematics(pxd_context* ctx, int32_t n_poses, const double* torsions,
                             double* xyz_out);
+
+/* ------------------------------------------------------- empirical scores */
+
+/* Installs a scoring function: which = 0 pose selection (pscore), 1 affinity (bscore).
+ * Replaces scoring_function_factory (factory.cpp:213-238) for the device scorers. */
+int pxd_set_scoring_function(pxd_context* ctx, int32_t which, const pxd_sf_params* params);
+
+/* Empirical score of a batch (root_scorer::combine with precalculate,
+ * scorer.h:92-136), one warp per pose. terms_dev [n_poses][PXD_NUM_TERMS] receives the
+ * unweighted term values (may be NULL). The GB/SA term is evaluated by
+ * pxd_score_gbsa and contributes 0 here. */
+int pxd_score_dev(pxd_context* ctx, int32_t which, int32_t n_poses, int32_t max_atoms,
+                  const int32_t* ligand_ids_dev, const float* lig_xyz_dev,
+                  const float* rec_tors_dev, double* score_dev, double* terms_dev, void* stream);
+
+/* Host-buffer version for one ligand; the GB/SA term is included when its weight is
+ * non-zero. */
+int pxd_score(pxd_context* ctx, int32_t which, int32_t ligand_id, int32_t n_poses,
+              const double* lig_xyz, const double* rec_tors, double* score, double* terms);
+
+/* Generalised-Born / surface-area energy difference complex - ligand - receptor
+ * (gbsa_total_energy::summary, scorer.cpp:737-866) of one pose, FP64 on the device.
+ * parts[3] (may be NULL) receives the complex, ligand and receptor energies. */
+int pxd_score_gbsa(pxd_context* ctx, int32_t ligand_id, const double* lig_xyz,
+                   const double* rec_tors, double* delta, double* parts);
 
 #ifdef __cplusplus
 }

@@ -77,6 +77,18 @@ def port_lib():
                                        f64p, f64p, i32p, i32p, C.c_int]
         lib.po_ligand_apply.argtypes = [C.c_void_p, f64p, f64p, f64p, f64p, f64p]
         lib.po_receptor_apply.argtypes = [C.c_void_p, f64p, f64p]
+        lib.po_score.restype = C.c_double
+        lib.po_score.argtypes = [C.POINTER(abi.SfParams), C.c_int, f64p, f64p, f64p, f64p,
+                                 C.POINTER(abi.ScoreLists), C.c_int, f64p, f64p, i32p,
+                                 C.POINTER(abi.ScoreLists), f64p]
+        lib.po_vdw_check.restype = C.c_double
+        lib.po_vdw_check.argtypes = [C.POINTER(abi.SfParams), C.c_int, f64p, f64p, f64p, C.c_int,
+                                     f64p, i32p]
+        lib.po_torsion_strain.restype = C.c_double
+        lib.po_torsion_strain.argtypes = [C.POINTER(abi.ScoreLists), f64p]
+        lib.po_gbsa_parts.restype = C.c_double
+        lib.po_gbsa_parts.argtypes = [C.c_int, f64p, f64p, C.POINTER(abi.ScoreLists), C.c_int,
+                                      f64p, f64p, C.POINTER(abi.ScoreLists), f64p]
         lib.po_rng_uniform_int.restype = C.c_int
         lib.po_rng_uniform_real.restype = C.c_double
         lib.po_rng_uniform_real.argtypes = [C.c_void_p, C.c_double, C.c_double]
@@ -235,6 +247,25 @@ class PortSystem:
         t = _d(torsions).reshape(-1)
         self.lib.po_receptor_apply(self.h, _p(t) if t.size else _p(np.zeros(1)), _p(out))
         return out.reshape(-1, 3)
+
+    def score(self, sf, rec_xyz, lig_xyz):
+        """root_scorer::combine with the scoring function sf; returns (score, terms[11])."""
+        return port_score(sf, self.receptor, self.ligand, rec_xyz, lig_xyz)
+
+
+def port_score(sf, receptor, ligand, rec_xyz, lig_xyz):
+    lib = port_lib()
+    keep = []
+    rl = receptor.lists.to_c(keep)
+    ll = ligand.lists.to_c(keep)
+    rx = _d(rec_xyz).reshape(-1)
+    lx = _d(lig_xyz).reshape(-1)
+    terms = np.zeros(11)
+    v = lib.po_score(C.byref(sf), receptor.n_atoms, _p(rx), _p(receptor.ff.charge),
+                     _p(receptor.ff.sigma), _p(receptor.ff.epsilon), C.byref(rl), ligand.n_atoms,
+                     _p(lx), _p(ligand.ff.charge), _p(ligand.vdw_type, C.c_int32), C.byref(ll),
+                     _p(terms))
+    return v, terms
 
 
 class RefSystem:

@@ -1346,3 +1346,417 @@ void po_rng_in_sphere(po_rng* r, double* out) {
         if (v_sqsum(out) < 1.0) break;
     }
 }
+
+/* ============================================ empirical scores (scorer.cpp) */
+static double ramp_down(double v, double lo, double hi) { /* math.h:196-206 */
+    if (v < lo) return 1.0;
+    if (v <= hi) return 1.0 - (v - lo) / (hi - lo);
+    return 0.0;
+}
+static double ramp_down_c(double v, double c, double lo, double hi) { /* math.h:208-215 */
+    return v < c ? ramp_down(c - v, lo, hi) : ramp_down(v - c, lo, hi);
+}
+static double clampd(double v, double lo, double hi) {
+    const double m = v > lo ? v : lo;
+    return m < hi ? m : hi;
+}
+static double dist(const double* a, const double* b) {
+    double t = 0.0;
+    t += (a[0] - b[0]) * (a[0] - b[0]);
+    t += (a[1] - b[1]) * (a[1] - b[1]);
+    t += (a[2] - b[2]) * (a[2] - b[2]);
+    return sqrt(t);
+}
+static int ring_size(const int32_t* r) {
+    int n = 0;
+    while (n < 6 && r[n] >= 0) ++n;
+    return n;
+}
+/* to_ring_centroid / to_ring_normal (scorer.cpp:128-172) */
+static void ring_centroid(const double* x, const int32_t* r, double* c) {
+    const int n = ring_size(r);
+    c[0] = c[1] = c[2] = 0.0;
+    for (int i = 0; i < n; ++i) v_addi(c, x + 3 * r[i]);
+    c[0] /= n;
+    c[1] /= n;
+    c[2] /= n;
+}
+static void ring_normal(const double* x, const int32_t* r, double* nrm) {
+    double e1[3], e2[3];
+    v_sub(x + 3 * r[1], x + 3 * r[0], e1);
+    v_sub(x + 3 * r[1], x + 3 * r[2], e2);
+    v_cross(e1, e2, nrm);
+    v_normalize(nrm);
+}
+
+typedef struct {
+    int n;
+    const double* xyz;
+    const double* q;
+    const double* sigma;   /* receptor: FF sigma; ligand: type table sigma */
+    const double* eps;
+    const int32_t* type;   /* ligand vdW types, NULL for the receptor */
+    const pxd_score_lists* l;
+} po_mol;
+
+/* mm_interaction_vdw_energy::report (scorer.cpp:222-252) */
+static double term_vdw(const pxd_sf_params* sf, const po_mol* R, const po_mol* L) {
+    double e = 0.0;
+    for (int i = 0; i < L->n; ++i) {
+        const int t = L->type[i];
+        const double s1 = PXD_VDW_SIGMA[t] * sf->vdw_sigma_scale[t];
+        const double e1 = PXD_VDW_EPSILON[t] * sf->vdw_epsilon_scale[t];
+        for (int j = 0; j < R->n; ++j) {
+            const double d = dist(L->xyz + 3 * i, R->xyz + 3 * j);
+            double fused = (s1 + R->sigma[j]) * 0.5;
+            const double u6 = pow(safe_div(fused, d), 6.0);
+            fused = sqrt(e1 * R->eps[j]) * 4.0;
+            const double v = (u6 * u6 - u6) * fused;
+            e += clampd(v, -sf->vdw_cutoff, sf->vdw_cutoff);
+        }
+    }
+    return e * sf->vdw_scale;
+}
+
+/* mm_interaction_coulomb_energy::report (scorer.cpp:254-276) */
+static double term_coulomb(const po_mol* R, const po_mol* L) {
+    double e = 0.0;
+    for (int i = 0; i < L->n; ++i)
+        for (int j = 0; j < R->n; ++j)
+            e += safe_div(L->q[i] * R->q[j], dist(L->xyz + 3 * i, R->xyz + 3 * j)) * kCoulomb;
+    return e;
+}
+
+/* hydrophobic_energy::report (scorer.cpp:278-311) */
+static double term_hydrophobic(const pxd_sf_params* sf, const po_mol* R, const po_mol* L) {
+    double e = 0.0;
+    for (int a = 0; a < L->l->n_hydrophobic; ++a) {
+        const int i = L->l->hydrophobic[a];
+        const double s1 = PXD_VDW_SIGMA[L->type[i]];
+        for (int b = 0; b < R->l->n_hydrophobic; ++b) {
+            const int j = R->l->hydrophobic[b];
+            const double r1 = (s1 + R->sigma[j]) * sf->hydro_scale_factor + sf->hydro_dist_min;
+            const double r2 = r1 + sf->hydro_dist_max;
+            e -= ramp_down(dist(L->xyz + 3 * i, R->xyz + 3 * j), r1, r2);
+        }
+    }
+    return e * sf->hydro_scale;
+}
+
+/* ionic_interaction_batch::calculate (scorer.cpp:337-368) */
+static double ionic_batch(const double* cx, const int32_t* cat, int nc, const double* ax,
+                          const int32_t* an, int na, const double* p) {
+    double e = 0.0;
+    for (int i = 0; i < nc; ++i)
+        for (int j = 0; j < na; ++j) e -= ramp_down(dist(cx + 3 * cat[i], ax + 3 * an[j]), p[0], p[1]);
+    return e;
+}
+
+static double term_ionic(const pxd_sf_params* sf, const po_mol* R, const po_mol* L) {
+    double e = 0.0;
+    e += sf->ionic_coef[0] * ionic_batch(L->xyz, L->l->cation, L->l->n_cation, R->xyz, R->l->anion,
+                                         R->l->n_anion, sf->ionic[0]);
+    e += sf->ionic_coef[1] * ionic_batch(R->xyz, R->l->cation, R->l->n_cation, L->xyz, L->l->anion,
+                                         L->l->n_anion, sf->ionic[1]);
+    return e;
+}
+
+/* cation_pi_interaction_batch::calculate (scorer.cpp:426-462) */
+static double picat_batch(const double* cx, const int32_t* cat, int nc, const double* rx,
+                          const int32_t* rings, int nr, const double* p) {
+    double e = 0.0;
+    for (int r = 0; r < nr; ++r) {
+        double c[3];
+        ring_centroid(rx, rings + 6 * r, c);
+        for (int j = 0; j < nc; ++j) e -= ramp_down(dist(c, cx + 3 * cat[j]), p[0], p[1]);
+    }
+    return e;
+}
+
+static double term_picat(const pxd_sf_params* sf, const po_mol* R, const po_mol* L) {
+    double e = 0.0;
+    e += sf->picat_coef[0] * picat_batch(L->xyz, L->l->cation, L->l->n_cation, R->xyz, R->l->ring5,
+                                         R->l->n_ring5, sf->picat[0]);
+    e += sf->picat_coef[1] * picat_batch(L->xyz, L->l->cation, L->l->n_cation, R->xyz, R->l->ring6,
+                                         R->l->n_ring6, sf->picat[1]);
+    e += sf->picat_coef[2] * picat_batch(R->xyz, R->l->cation, R->l->n_cation, L->xyz, L->l->ring5,
+                                         L->l->n_ring5, sf->picat[2]);
+    e += sf->picat_coef[3] * picat_batch(R->xyz, R->l->cation, R->l->n_cation, L->xyz, L->l->ring6,
+                                         L->l->n_ring6, sf->picat[3]);
+    return e;
+}
+
+/* get_projected_centroid_distance / get_sigma_distance (scorer.cpp:615-636) */
+static double projected(const double* n1, const double* c1, const double* c2) {
+    double t[3];
+    v_sub(c2, c1, t);
+    const double dp = v_dot(n1, t);
+    return sqrt(v_sqsum(t) - dp * dp);
+}
+
+/* pi_stacking_batch::calculate (scorer.cpp:698-724); p: dmin dmax amin amax smin smax */
+static double stack_batch(const double* rx, const int32_t* rr, int nrr, const double* lx,
+                          const int32_t* lr, int nlr, const double* p, double center) {
+    double e = 0.0;
+    for (int i = 0; i < nrr; ++i) {
+        double rc[3], rn[3];
+        ring_centroid(rx, rr + 6 * i, rc);
+        ring_normal(rx, rr + 6 * i, rn);
+        for (int j = 0; j < nlr; ++j) {
+            double lc[3], ln[3];
+            ring_centroid(lx, lr + 6 * j, lc);
+            ring_normal(lx, lr + 6 * j, ln);
+            double d = dist(rc, lc);
+            if (d > p[1]) continue;
+            d = ramp_down(d, p[0], p[1]);
+            const double s1 = projected(rn, rc, lc), s2 = projected(ln, lc, rc);
+            double sg = s1 < s2 ? s1 : s2;
+            if (sg > p[5]) continue;
+            sg = ramp_down(sg, p[4], p[5]);
+            double th = acos(clampd(v_dot(rn, ln), -1.0, 1.0)) / kPi * 180.0;
+            th = th < 180.0 - th ? th : 180.0 - th;
+            th = ramp_down_c(th, center, p[2], p[3]);
+            e -= d * sg * th;
+        }
+    }
+    return e;
+}
+
+static double term_stack(const pxd_sf_params* sf, int which, const po_mol* R, const po_mol* L) {
+    const double center = which == 0 ? 0.0 : 90.0;
+    const double* c = sf->stack_coef[which];
+    double e = 0.0;
+    e += c[0] * stack_batch(R->xyz, R->l->ring5, R->l->n_ring5, L->xyz, L->l->ring5, L->l->n_ring5,
+                            sf->stack[which][0], center);
+    e += c[1] * stack_batch(R->xyz, R->l->ring6, R->l->n_ring6, L->xyz, L->l->ring5, L->l->n_ring5,
+                            sf->stack[which][1], center);
+    e += c[2] * stack_batch(R->xyz, R->l->ring5, R->l->n_ring5, L->xyz, L->l->ring6, L->l->n_ring6,
+                            sf->stack[which][2], center);
+    e += c[3] * stack_batch(R->xyz, R->l->ring6, R->l->n_ring6, L->xyz, L->l->ring6, L->l->n_ring6,
+                            sf->stack[which][3], center);
+    return e;
+}
+
+/* hbond_interactions_ga_tuning_param::calculate (scorer.cpp:546-577);
+ * p: dist_min dist_max angle_min angle_max dist_center angle_center */
+static double hbond_batch(const double* dx, const int32_t* don, int nd, const double* ax,
+                          const int32_t* acc, int na, const double* p) {
+    double e = 0.0;
+    for (int i = 0; i < nd; ++i) {
+        const double* dpos = dx + 3 * don[2 * i];
+        const double* hpos = dx + 3 * don[2 * i + 1];
+        for (int j = 0; j < na; ++j) {
+            const double* apos = ax + 3 * acc[j];
+            const double dd = ramp_down_c(dist(hpos, apos), p[4], p[0], p[1]);
+            if (dd < EPS) continue;
+            double h2d[3], h2a[3];
+            v_sub(dpos, hpos, h2d);
+            v_sub(apos, hpos, h2a);
+            const double dp = clampd(safe_div(v_dot(h2d, h2a), v_norm(h2d) * v_norm(h2a)), -1.0, 1.0);
+            const double ang = acos(dp) / kPi * 180.0;
+            e -= dd * ramp_down_c(ang, p[5], p[2], p[3]);
+        }
+    }
+    return e;
+}
+
+static double term_hbond(const pxd_sf_params* sf, const po_mol* R, const po_mol* L) {
+    const pxd_score_lists *rl = R->l, *ll = L->l;
+    const double* c = sf->hbond_coef;
+    double e = 0.0;
+    e += c[0] * hbond_batch(L->xyz, ll->don_charged, ll->n_don_charged, R->xyz, rl->acc_charged, rl->n_acc_charged, sf->hbond[0]);
+    e += c[1] * hbond_batch(L->xyz, ll->don_charged, ll->n_don_charged, R->xyz, rl->acc_neutral, rl->n_acc_neutral, sf->hbond[1]);
+    e += c[2] * hbond_batch(L->xyz, ll->don_neutral, ll->n_don_neutral, R->xyz, rl->acc_charged, rl->n_acc_charged, sf->hbond[2]);
+    e += c[3] * hbond_batch(L->xyz, ll->don_neutral, ll->n_don_neutral, R->xyz, rl->acc_neutral, rl->n_acc_neutral, sf->hbond[3]);
+    e += c[4] * hbond_batch(R->xyz, rl->don_charged, rl->n_don_charged, L->xyz, ll->acc_charged, ll->n_acc_charged, sf->hbond[4]);
+    e += c[5] * hbond_batch(R->xyz, rl->don_charged, rl->n_don_charged, L->xyz, ll->acc_neutral, ll->n_acc_neutral, sf->hbond[5]);
+    e += c[6] * hbond_batch(R->xyz, rl->don_neutral, rl->n_don_neutral, L->xyz, ll->acc_charged, ll->n_acc_charged, sf->hbond[6]);
+    e += c[7] * hbond_batch(R->xyz, rl->don_neutral, rl->n_don_neutral, L->xyz, ll->acc_neutral, ll->n_acc_neutral, sf->hbond[7]);
+    return e * sf->hbond_scale;
+}
+
+/* torsion_strain_penalty_scorer::report (scorer.cpp:579-613) */
+double po_torsion_strain(const pxd_score_lists* l, const double* x) {
+    static const double per[4] = {1.0, 2.0, 3.0, 4.0};
+    static const double ph[4] = {0.0, 3.141592653589793, 0.0, 3.141592653589793};
+    double score = 0.0;
+    for (int e = 0; e < l->n_tstrain; ++e) {
+        const double* co = l->tstrain_coefs + 4 * e;
+        double tmp = 0.0;
+        int j = 0;
+        for (int q = l->tstrain_offsets[e]; q < l->tstrain_offsets[e + 1]; ++q, ++j) {
+            const int32_t* a = l->tstrain_quads + 4 * q;
+            if (a[0] == a[1]) break;
+            const double th = po_dihedral(x + 3 * a[0], x + 3 * a[1], x + 3 * a[2], x + 3 * a[3]);
+            tmp += (1 + cos(th * per[0] - ph[0])) * co[0] + (1 + cos(th * per[1] - ph[1])) * co[1] +
+                   (1 + cos(th * per[2] - ph[2])) * co[2] + (1 + cos(th * per[3] - ph[3])) * co[3];
+        }
+        if (j > 0) score += tmp / j;
+    }
+    return score;
+}
+
+/* GBSA (scorer.cpp:737-866): radii and screens by element, Born radii, GB + SA. */
+static const double kRadius[18] = {1.5, 1.2, 1.5, 1.5, 1.5, 1.5, 1.7, 1.55, 1.5,
+                                   1.5, 1.5, 1.5, 1.5, 1.5, 2.1, 1.85, 1.8, 1.7};
+static const double kScreen[17] = {0.8, 0.85, 0.8, 0.8, 0.8, 0.8, 0.72, 0.79, 0.85,
+                                   0.88, 0.8, 0.8, 0.8, 0.8, 0.8, 0.86, 0.96};
+
+static void gbsa_props(const po_mol* M, double* radii, double* screens) {
+    const int n = M->n;
+    for (int i = 0; i < n; ++i) radii[i] = -1.0;
+    for (int b = 0; b < M->l->n_all_bonds; ++b) {
+        const int i = M->l->all_bonds[2 * b], j = M->l->all_bonds[2 * b + 1];
+        const int ea = M->l->atomic_numbers[i], eb = M->l->atomic_numbers[j];
+        if (ea == 1 && eb == 7) radii[i] = 1.3;
+        else if (ea == 7 && eb == 1) radii[j] = 1.3;
+    }
+    for (int i = 0; i < n; ++i) {
+        const int e = M->l->atomic_numbers[i];
+        if (radii[i] < 0.0) radii[i] = e <= 17 ? kRadius[e] : kRadius[0];
+        screens[i] = e <= 16 ? kScreen[e] : kScreen[0];
+    }
+}
+
+/* gbsa_total_energy::calculate (scorer.cpp:798-866) with the reference constants
+ * (gbsa_total_energy constructor, scorer.h:400-408: solvent 78.5, solute 1, offset 0.09,
+ * alpha 1, beta 0.8, gamma 4.85, probe 1.4, surface 0.0678584012906,
+ * kappa 0.09293963686178248). */
+static double gbsa_calc(int n, const double* x, const double* q, const double* radii,
+                        const double* screens) {
+    const double offset = 0.09, alpha = 1.0, beta = 0.8, gamma_ = 4.85;
+    const double solute = 1.0, solvent = 78.5, kappa = 0.09293963686178248, probe = 1.4;
+    const double surface = 0.0678584012906;
+    double* orad = (double*)malloc((size_t)(n ? n : 1) * sizeof(double));
+    double* sumI = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+    double* born = (double*)malloc((size_t)(n ? n : 1) * sizeof(double));
+    for (int i = 0; i < n; ++i) orad[i] = radii[i] - offset;
+    for (int i = 0; i < n; ++i) {
+        const double sr = orad[i] * screens[i], sr2 = sr * sr;
+        for (int j = 0; j < n; ++j) {
+            if (i == j) continue;
+            const double r12 = dist(x + 3 * i, x + 3 * j);
+            const double U = r12 + sr;
+            if (U < orad[j]) continue;
+            const double r12i = 1.0 / r12;
+            double D = fabs(r12 - sr);
+            const double L = orad[j] > D ? orad[j] : D;
+            const double Ui = 1.0 / U, Li = 1.0 / L;
+            D = 0.25 * (r12 - sr2 * r12i) * (Ui * Ui - Li * Li);
+            D += (Li - Ui + 0.5 * log(L * Ui + EPS) * r12i);
+            D *= 0.5;
+            sumI[j] += D;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        const double U = sumI[i] * orad[i];
+        const double D = U * U;
+        const double L = tanh(alpha * U - beta * D + gamma_ * U * D);
+        born[i] = 1.0 / (1.0 / orad[i] - L / radii[i]);
+    }
+    double egb = 0.0;
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+            double f;
+            if (i == j) {
+                f = born[i];
+            } else {
+                double t = 0.0;
+                t += (x[3 * i] - x[3 * j]) * (x[3 * i] - x[3 * j]);
+                t += (x[3 * i + 1] - x[3 * j + 1]) * (x[3 * i + 1] - x[3 * j + 1]);
+                t += (x[3 * i + 2] - x[3 * j + 2]) * (x[3 * i + 2] - x[3 * j + 2]);
+                const double bp = born[i] * born[j];
+                f = sqrt(t + bp * exp(-0.25 * t / bp) + EPS);
+            }
+            const double pref = 0.5 * kCoulomb * (1.0 / solute - exp(-kappa * f) / solvent);
+            egb -= q[i] * q[j] / f * pref;
+        }
+    }
+    double esa = 0.0;
+    for (int i = 0; i < n; ++i)
+        esa += (radii[i] + probe) * (radii[i] + probe) * pow(radii[i] / born[i], 6.0);
+    free(orad);
+    free(sumI);
+    free(born);
+    return egb + esa * surface;
+}
+
+/* gbsa_total_energy::summary: complex - ligand - receptor (scorer.cpp:755-796) */
+static double term_gbsa(const po_mol* R, const po_mol* L, double* parts) {
+    const int nr = R->n, nl = L->n, n = nr + nl;
+    double* rr = (double*)malloc((size_t)(nr + 1) * sizeof(double));
+    double* rs = (double*)malloc((size_t)(nr + 1) * sizeof(double));
+    double* lr = (double*)malloc((size_t)(n + 1) * sizeof(double));
+    double* ls = (double*)malloc((size_t)(n + 1) * sizeof(double));
+    gbsa_props(R, rr, rs);
+    const double e_pro = gbsa_calc(nr, R->xyz, R->q, rr, rs);
+    gbsa_props(L, lr, ls);
+    const double e_lig = gbsa_calc(nl, L->xyz, L->q, lr, ls);
+    double* cx = (double*)malloc((size_t)(n + 1) * 3 * sizeof(double));
+    double* cq = (double*)malloc((size_t)(n + 1) * sizeof(double));
+    memcpy(cx, L->xyz, (size_t)nl * 3 * sizeof(double));
+    memcpy(cx + 3 * nl, R->xyz, (size_t)nr * 3 * sizeof(double));
+    memcpy(cq, L->q, (size_t)nl * sizeof(double));
+    memcpy(cq + nl, R->q, (size_t)nr * sizeof(double));
+    memcpy(lr + nl, rr, (size_t)nr * sizeof(double));
+    memcpy(ls + nl, rs, (size_t)nr * sizeof(double));
+    const double e_com = gbsa_calc(n, cx, cq, lr, ls);
+    if (parts) {
+        parts[0] = e_com;
+        parts[1] = e_lig;
+        parts[2] = e_pro;
+    }
+    free(rr);
+    free(rs);
+    free(lr);
+    free(ls);
+    free(cx);
+    free(cq);
+    return e_com - e_lig - e_pro;
+}
+
+/* root_scorer::combine over the active terms (scorer.cpp:53-126). terms[11] gets the
+ * raw value of every active term (0 otherwise); returns sum(coef * term). */
+double po_score(const pxd_sf_params* sf, int n_rec, const double* rec_xyz, const double* rec_q,
+                const double* rec_sigma, const double* rec_eps, const pxd_score_lists* rec_l,
+                int n_lig, const double* lig_xyz, const double* lig_q, const int32_t* lig_type,
+                const pxd_score_lists* lig_l, double* terms) {
+    po_mol R = {n_rec, rec_xyz, rec_q, rec_sigma, rec_eps, NULL, rec_l};
+    po_mol L = {n_lig, lig_xyz, lig_q, NULL, NULL, lig_type, lig_l};
+    double t[PXD_NUM_TERMS] = {0};
+#define ACTIVE(k) (sf->coef[k] > 1e-5 || sf->coef[k] < -1e-5)
+    if (ACTIVE(PXD_TERM_COULOMB)) t[PXD_TERM_COULOMB] = term_coulomb(&R, &L);
+    if (ACTIVE(PXD_TERM_VDW)) t[PXD_TERM_VDW] = term_vdw(sf, &R, &L);
+    if (ACTIVE(PXD_TERM_IONIC)) t[PXD_TERM_IONIC] = term_ionic(sf, &R, &L);
+    if (ACTIVE(PXD_TERM_PI_CATION)) t[PXD_TERM_PI_CATION] = term_picat(sf, &R, &L);
+    if (ACTIVE(PXD_TERM_F2F)) t[PXD_TERM_F2F] = term_stack(sf, 0, &R, &L);
+    if (ACTIVE(PXD_TERM_E2F)) t[PXD_TERM_E2F] = term_stack(sf, 1, &R, &L);
+    if (ACTIVE(PXD_TERM_HBOND)) t[PXD_TERM_HBOND] = term_hbond(sf, &R, &L);
+    if (ACTIVE(PXD_TERM_HYDROPHOBIC)) t[PXD_TERM_HYDROPHOBIC] = term_hydrophobic(sf, &R, &L);
+    if (ACTIVE(PXD_TERM_TSTRAIN)) t[PXD_TERM_TSTRAIN] = po_torsion_strain(lig_l, lig_xyz);
+    if (ACTIVE(PXD_TERM_ROTATABLE)) t[PXD_TERM_ROTATABLE] = -1.0 / (2.620643 + lig_l->n_rotatable);
+    if (ACTIVE(PXD_TERM_GBSA)) t[PXD_TERM_GBSA] = term_gbsa(&R, &L, NULL);
+#undef ACTIVE
+    double s = 0.0;
+    for (int k = 0; k < PXD_NUM_TERMS; ++k) {
+        if (terms) terms[k] = t[k];
+        s += sf->coef[k] * t[k];
+    }
+    return s;
+}
+
+/* mm_interaction_vdw_energy::report alone: the randomize() clash check (searcher.cpp:76) */
+double po_vdw_check(const pxd_sf_params* sf, int n_rec, const double* rec_xyz, const double* rec_sigma,
+                    const double* rec_eps, int n_lig, const double* lig_xyz, const int32_t* lig_type) {
+    po_mol R = {n_rec, rec_xyz, NULL, rec_sigma, rec_eps, NULL, NULL};
+    po_mol L = {n_lig, lig_xyz, NULL, NULL, NULL, lig_type, NULL};
+    return term_vdw(sf, &R, &L);
+}
+
+double po_gbsa_parts(int n_rec, const double* rec_xyz, const double* rec_q, const pxd_score_lists* rec_l,
+                     int n_lig, const double* lig_xyz, const double* lig_q, const pxd_score_lists* lig_l,
+                     double* parts) {
+    po_mol R = {n_rec, rec_xyz, rec_q, NULL, NULL, NULL, rec_l};
+    po_mol L = {n_lig, lig_xyz, lig_q, NULL, NULL, NULL, lig_l};
+    return term_gbsa(&R, &L, parts);
+}

@@ -63,6 +63,19 @@ void po_ligand_apply(const po_system* s, const double* xyz, const double* center
                      const double* rot9, const double* torsions, double* out);
 void po_receptor_apply(const po_system* s, const double* torsions, double* out);
 
+/* ---- empirical scores (engine/src/core/scorer.cpp:53-866) ---- */
+double po_score(const pxd_sf_params* sf, int n_rec, const double* rec_xyz, const double* rec_q,
+                const double* rec_sigma, const double* rec_eps, const pxd_score_lists* rec_l,
+                int n_lig, const double* lig_xyz, const double* lig_q, const int32_t* lig_type,
+                const pxd_score_lists* lig_l, double* terms);
+double po_vdw_check(const pxd_sf_params* sf, int n_rec, const double* rec_xyz,
+                    const double* rec_sigma, const double* rec_eps, int n_lig,
+                    const double* lig_xyz, const int32_t* lig_type);
+double po_torsion_strain(const pxd_score_lists* l, const double* x);
+double po_gbsa_parts(int n_rec, const double* rec_xyz, const double* rec_q,
+                     const pxd_score_lists* rec_l, int n_lig, const double* lig_xyz,
+                     const double* lig_q, const pxd_score_lists* lig_l, double* parts);
+
 /* ---- mt19937 + libstdc++ distributions as random_generator uses them
  *      (engine/include/bytedock/lib/random.h:33-63, engine/src/lib/random.cpp) ---- */
 typedef struct po_rng {

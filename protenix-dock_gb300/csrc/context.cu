@@ -344,7 +344,9 @@ void free_receptor(pxd_context* ctx) {
     if (ctx->rec_mem) cudaFree(ctx->rec_mem);
     if (ctx->rec_ex_all) cudaFree(ctx->rec_ex_all);
     if (ctx->rec_ex_mov) cudaFree(ctx->rec_ex_mov);
-    ctx->rec_mem = ctx->rec_ex_all = ctx->rec_ex_mov = nullptr;
+    if (ctx->rec_score_mem) cudaFree(ctx->rec_score_mem);
+    ctx->rec_mem = ctx->rec_ex_all = ctx->rec_ex_mov = ctx->rec_score_mem = nullptr;
+    ctx->rec_score = DevRecScore{};
     ctx->rec = DevReceptor{};
     ctx->has_receptor = false;
 }
@@ -485,6 +487,8 @@ void pxd_context_destroy(pxd_context* ctx) {
     pxd_grid_drop(ctx);
     free_receptor(ctx);
     if (ctx->d_ligands) cudaFree(ctx->d_ligands);
+    for (int k = 0; k < 2; ++k)
+        if (ctx->d_sf[k]) cudaFree(ctx->d_sf[k]);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     cudaStreamDestroy(ctx->stream);
@@ -669,6 +673,8 @@ int pxd_set_receptor(pxd_context* ctx, const pxd_receptor_desc* r) {
     ctx->n_ex_all = M;
     ctx->n_ex_mov = static_cast<int>(movs.size());
     point_explicit(ctx, false);
+    rc = upload_receptor_scoring(ctx, r->lists);
+    if (rc) return rc;
     ctx->has_receptor = true;
     ctx->ligands_dirty = true;
     return PXD_OK;
@@ -877,7 +883,7 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
                 return set_error(ctx, PXD_ERR_STATE, std::string("no map for ligand vdW type ") + PXD_VDW_TAGS[types[a]]);
         }
     }
-    const size_t o_q = pk.put(q), o_slot = pk.put(slots), o_se = pk.put(se);
+    const size_t o_q = pk.put(q), o_slot = pk.put(slots), o_se = pk.put(se), o_type = pk.put(types);
     // torsion tree
     const pxd_torsion_tree& tr = lig->tree;
     if (tr.n_frags > 0) {
@@ -928,12 +934,19 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
     d.charge = at<float>(e.mem, o_q);
     d.map_slot = at<int>(e.mem, o_slot);
     d.se = at<float2>(e.mem, o_se);
+    d.type = at<int>(e.mem, o_type);
     d.n_frags = tr.n_frags;
     d.n_tors = tr.n_torsions;
     d.perm = at<int>(e.mem, o_perm);
     d.frag_range = at<int>(e.mem, o_fr);
     d.tors = at<int4>(e.mem, o_tors);
     d.is_root = at<int>(e.mem, o_root);
+    e.charge.assign(lig->ff.charge, lig->ff.charge + N);
+    rc = upload_ligand_scoring(ctx, e, lig->lists);
+    if (rc) {
+        cudaFree(e.mem);
+        return rc;
+    }
     *ligand_id = static_cast<int32_t>(ctx->ligands.size());
     ctx->ligands.push_back(e);
     ctx->ligands_dirty = true;
@@ -943,8 +956,10 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
 int pxd_clear_ligands(pxd_context* ctx) {
     if (!ctx) return PXD_ERR_INVALID;
     cudaStreamSynchronize(ctx->stream);
-    for (auto& e : ctx->ligands)
+    for (auto& e : ctx->ligands) {
         if (e.mem) cudaFree(e.mem);
+        if (e.score_mem) cudaFree(e.score_mem);
+    }
     ctx->ligands.clear();
     ctx->ligands_dirty = true;
     return PXD_OK;

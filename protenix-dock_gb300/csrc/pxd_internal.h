@@ -38,12 +38,63 @@ struct DevTopo {
     const float4* pair_p;     // A = 332.06 qi qj s_c, C = 4 sqrt(ei ej) s_v, S2 = ((si+sj)/2)^2
 };
 
+struct DevSf {
+    float coef[PXD_NUM_TERMS];
+    float vdw_scale, vdw_cutoff;
+    float2 vdw_type[PXD_NUM_VDW_TYPES];  // scaled sigma, epsilon per ligand type
+    float vdw_sigma_raw[PXD_NUM_VDW_TYPES];  // unscaled sigma (hydrophobic thresholds)
+    float ionic_coef[2], ionic[2][2];
+    float picat_coef[4], picat[4][2];
+    float stack_coef[2][4], stack[2][4][6];
+    float hbond_scale, hbond_coef[8], hbond[8][6];
+    float hydro_scale, hydro_min, hydro_max, hydro_factor;
+};
+
+struct DevRecScore {
+    int has;
+    int n_all;
+    const float4* all_xyzq;    // every receptor atom: position, charge
+    const float2* all_se;      // sigma, epsilon
+    const int* all_local;      // rotor-atom local index or -1
+    int n_hyd, n_cat, n_an, n_r5, n_r6, n_donc, n_donn, n_accc, n_accn;
+    const int* hyd;
+    const int* cat;
+    const int* an;
+    const float4* r5c;         // ring centroid
+    const float4* r5n;         // ring normal
+    const float4* r6c;
+    const float4* r6n;
+    const int2* donc;
+    const int2* donn;
+    const int* accc;
+    const int* accn;
+};
+
+struct DevLigScore {
+    int has;
+    int n_hyd, n_cat, n_an, n_r5, n_r6, n_donc, n_donn, n_accc, n_accn, n_ts, n_rot;
+    const int* hyd;
+    const int* cat;
+    const int* an;
+    const int* r5;             // [n][6], -1 padded
+    const int* r6;
+    const int2* donc;
+    const int2* donn;
+    const int* accc;
+    const int* accn;
+    const float4* ts_coef;     // torsion-strain coefficients
+    const int2* ts_range;      // quads [first, first + count)
+    const int4* ts_quad;
+};
+
 struct DevLigand {
     DevTopo topo;
+    DevLigScore score;        // interaction lists (score.has == 0: not scorable)
     int n_atoms;
     const float* charge;      // [N]
     const int* map_slot;      // [N] vdW map slot of the atom's type (-1: no map)
     const float2* se;         // [N] sigma, epsilon (explicit inter pairs)
+    const int* type;          // [N] ligand vdW type
     // torsion tree (forward kinematics, data.cpp:592-641)
     int n_frags, n_tors;
     const int* perm;          // [N]
@@ -85,6 +136,9 @@ struct LigandEntry {
     int n_atoms = 0;
     int n_tors = 0;
     std::vector<int32_t> types;
+    void* score_mem = nullptr;                // interaction lists allocation
+    std::vector<double> charge;               // FP64 copies for the GB/SA term
+    std::vector<double> gb_radius, gb_screen;
 };
 
 }  // namespace pxd
@@ -122,6 +176,13 @@ struct pxd_context {
     pxd::DevLigand* d_ligands = nullptr;  // device copy of every entry's DevLigand
     int d_ligands_cap = 0;
     bool ligands_dirty = true;
+    // empirical scores
+    pxd::DevRecScore rec_score{};
+    void* rec_score_mem = nullptr;
+    std::vector<double> rec_gb_radius, rec_gb_screen;
+    pxd::DevSf* d_sf[2] = {nullptr, nullptr};
+    pxd_sf_params sf_host[2];
+    bool sf_set[2] = {false, false};
     // scratch
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -150,5 +211,9 @@ int launch_ligand_kinematics(pxd_context* ctx, int lig, int n_poses, const float
                              float* xyz_out, cudaStream_t s);
 int launch_receptor_kinematics(pxd_context* ctx, int n_poses, const float* tors, float* out,
                                cudaStream_t s);
+int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l);
+int upload_ligand_scoring(pxd_context* ctx, LigandEntry& e, const pxd_score_lists* l);
+void gbsa_properties(const pxd_score_lists* l, int n, std::vector<double>& radius,
+                     std::vector<double>& screen);
 
 }  // namespace pxd

@@ -61,8 +61,30 @@ class TorsionTree(C.Structure):
     ]
 
 
+class ScoreLists(C.Structure):
+    """pxd_score_lists: interaction atom lists of one molecule."""
+
+    _fields_ = [
+        ("n_hydrophobic", C.c_int32), ("hydrophobic", i32p),
+        ("n_cation", C.c_int32), ("cation", i32p),
+        ("n_anion", C.c_int32), ("anion", i32p),
+        ("n_ring5", C.c_int32), ("ring5", i32p),
+        ("n_ring6", C.c_int32), ("ring6", i32p),
+        ("n_don_charged", C.c_int32), ("don_charged", i32p),
+        ("n_don_neutral", C.c_int32), ("don_neutral", i32p),
+        ("n_acc_charged", C.c_int32), ("acc_charged", i32p),
+        ("n_acc_neutral", C.c_int32), ("acc_neutral", i32p),
+        ("n_tstrain", C.c_int32), ("tstrain_coefs", f64p), ("tstrain_offsets", i32p),
+        ("tstrain_quads", i32p),
+        ("n_rotatable", C.c_int32),
+        ("atomic_numbers", i32p),
+        ("n_all_bonds", C.c_int32), ("all_bonds", i32p),
+    ]
+
+
 class LigandDesc(C.Structure):
-    _fields_ = [("ff", Topology), ("vdw_type", i32p), ("tree", TorsionTree)]
+    _fields_ = [("ff", Topology), ("vdw_type", i32p), ("tree", TorsionTree),
+                ("lists", C.POINTER(ScoreLists))]
 
 
 class ReceptorDesc(C.Structure):
@@ -74,6 +96,7 @@ class ReceptorDesc(C.Structure):
         ("rotor_axis", i32p),
         ("rotor_offsets", i32p),
         ("rotor_atoms", i32p),
+        ("lists", C.POINTER(ScoreLists)),
     ]
 
 
@@ -131,3 +154,26 @@ POSE_NAN = 2
 POSE_BAD_INPUT = 3
 NUM_VDW_TYPES = 99
 COULOMB_MAP = 99
+
+
+class SfParams(C.Structure):
+    """pxd_sf_params: one scoring function (ScoringFunctionParams, conf.h:122-150)."""
+
+    _fields_ = [
+        ("coef", C.c_double * 11),
+        ("vdw_scale", C.c_double), ("vdw_cutoff", C.c_double),
+        ("vdw_sigma_scale", C.c_double * 99), ("vdw_epsilon_scale", C.c_double * 99),
+        ("ionic_coef", C.c_double * 2), ("ionic", (C.c_double * 2) * 2),
+        ("picat_coef", C.c_double * 4), ("picat", (C.c_double * 2) * 4),
+        ("stack_coef", (C.c_double * 4) * 2), ("stack", ((C.c_double * 6) * 4) * 2),
+        ("hbond_scale", C.c_double), ("hbond_coef", C.c_double * 8),
+        ("hbond", (C.c_double * 6) * 8),
+        ("hydro_scale", C.c_double), ("hydro_dist_min", C.c_double),
+        ("hydro_dist_max", C.c_double), ("hydro_scale_factor", C.c_double),
+    ]
+
+
+TERM_NAMES = ["InteractionCoulomb_oriEnergy", "InteractionVDW_Energy", "Ionic_Energy",
+              "Pi_Cationic_Energy", "F2FPiStacking_Energy", "E2FPiStacking_Energy",
+              "Hbond_Energy", "Hydrophobic_Energy", "TorsionStrain_Penalty", "rotatable_energy",
+              "Gbsa_Com_Energy-Gbsa_Lig_Energy-Gbsa_Pro_Energy"]

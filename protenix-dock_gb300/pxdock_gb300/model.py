@@ -210,7 +210,9 @@ class Receptor:
         sigma = _per_atom([float(v) for v in ff["FF_vdW_sigma"]], n)
         eps = _per_atom([float(v) for v in ff["FF_vdW_epsilon"]], n)
         top = Topology.from_ffdata(ff, n, sigma, eps)
-        return cls(xyz, top, axes, groups, raw=d)
+        r = cls(xyz, top, axes, groups, raw=d)
+        r.lists = ScoreLists(ff, n, ligand=False)
+        return r
 
     @classmethod
     def from_file(cls, path):
@@ -228,6 +230,11 @@ class Receptor:
             arr = getattr(self, name)
             keep.append(arr)
             setattr(r, name, arr.ctypes.data_as(abi.i32p) if arr.size else C.cast(None, abi.i32p))
+        lists = getattr(self, "lists", None)
+        if lists is not None:
+            lc = lists.to_c(keep)
+            keep.append(lc)
+            r.lists = C.pointer(lc)
         return r
 
     def movable_atoms(self):
@@ -345,7 +352,9 @@ class Ligand:
         top = Topology.from_ffdata(ff, n, sig[types] if n else [], eps[types] if n else [])
         tree = TorsionTree.from_json(d["geometry"]) if geometry and "geometry" in d else None
         poses = np.array(d["xyz"], dtype=np.float64).reshape(-1, n, 3)
-        return cls(top, types, tree, poses, d.get("mapped_smiles", ""), raw=d)
+        lig = cls(top, types, tree, poses, d.get("mapped_smiles", ""), raw=d)
+        lig.lists = ScoreLists(ff, n, ligand=True)
+        return lig
 
     @classmethod
     def from_file(cls, path, geometry=True):
@@ -359,6 +368,11 @@ class Ligand:
         lig.vdw_type = self.vdw_type.ctypes.data_as(abi.i32p)
         if self.tree is not None:
             lig.tree = self.tree.to_c(keep)
+        lists = getattr(self, "lists", None)
+        if lists is not None:
+            lc = lists.to_c(keep)
+            keep.append(lc)
+            lig.lists = C.pointer(lc)
         return lig
 
 
@@ -383,3 +397,151 @@ def make_box(center, size, spacing):
         b.npoints[d] = npts[d]
     b.spacing = spacing
     return b
+
+
+# ---------------------------------------------------------------- empirical scores
+class ScoreLists:
+    """Interaction atom lists of one molecule (the pscore / bscore fields of the engine
+    JSON, parsed as data.cpp:271-295 does)."""
+
+    def __init__(self, ff, n_atoms, ligand):
+        def idx(key):
+            return _i32(ff.get(key, [])).reshape(-1)
+
+        def pairs(key):
+            return _i32(ff.get(key, [])).reshape(-1, 2)
+
+        def rings(key):
+            rs = ff.get(key, [])
+            out = -np.ones((len(rs), 6), np.int32)
+            for k, r in enumerate(rs):
+                out[k, : len(r)] = r
+            return out
+
+        self.hydrophobic = idx("hydrophobic_atomidx")
+        self.cation = idx("cation_atomidx")
+        self.anion = idx("anion_atomidx")
+        self.ring5 = rings("piring5_atomidx")
+        self.ring6 = rings("piring6_atomidx")
+        self.don_charged = pairs("hbonddon_charged_atomidx")
+        self.don_neutral = pairs("hbonddon_neut_atomidx")
+        self.acc_charged = idx("hbondacc_charged_atomidx")
+        self.acc_neutral = idx("hbondacc_neut_atomidx")
+        coefs, offs, quads = [], [0], []
+        if ligand:  # data.cpp:201-219
+            for entry, params in zip(ff.get("tstrain_atomidx_pose_selection", []),
+                                     ff.get("tstrain_params_pose_selection", [])):
+                coefs.append([float(v) for v in params])
+                for q in entry:
+                    quads.append([int(v) for v in q])
+                offs.append(len(quads))
+        self.tstrain_coefs = _f64(coefs).reshape(-1, 4)
+        self.tstrain_offsets = _i32(offs)
+        self.tstrain_quads = _i32(quads).reshape(-1, 4)
+        self.n_rotatable = len(ff.get("rotatable_bond_index", [])) if ligand else 0
+        an = ff.get("atomic_numbers", [])
+        self.atomic_numbers = _i32(an if len(an) == n_atoms else [0] * n_atoms)
+        self.all_bonds = pairs("bond_index")
+
+    def to_c(self, keep):
+        s = abi.ScoreLists()
+
+        def p(name, arr, ctype=C.c_int32):
+            keep.append(arr)
+            setattr(s, name, arr.ctypes.data_as(C.POINTER(ctype)) if arr.size else
+                    C.cast(None, C.POINTER(ctype)))
+
+        for name in ("hydrophobic", "cation", "anion", "ring5", "ring6", "don_charged",
+                     "don_neutral", "acc_charged", "acc_neutral"):
+            arr = getattr(self, name)
+            setattr(s, "n_" + name, len(arr))
+            p(name, arr)
+        s.n_tstrain = len(self.tstrain_coefs)
+        p("tstrain_coefs", self.tstrain_coefs, C.c_double)
+        p("tstrain_offsets", self.tstrain_offsets)
+        p("tstrain_quads", self.tstrain_quads)
+        s.n_rotatable = self.n_rotatable
+        p("atomic_numbers", self.atomic_numbers)
+        s.n_all_bonds = len(self.all_bonds)
+        p("all_bonds", self.all_bonds)
+        return s
+
+
+def _sf_active(x):
+    return x > 1e-5 or x < -1e-5  # CHECK_PARAMETER_NON_ZERO, utility.h:26
+
+
+def scoring_function_params(node):
+    """pxd_sf_params from one section ("pose_selection" / "affinity_ranking") of a
+    scoring-function JSON, as fill(ScoringFunctionParams) and the root_scorer constructor
+    read it (factory.cpp:144-202, scorer.cpp:53-115). The reference registers the
+    rotatable-energy weight under the name "TorsionStrain_Penalty" (scorer.cpp:103-106),
+    so a non-zero rotatable weight replaces the torsion-strain weight and the
+    rotatable term itself is never summed; the effective weights here say exactly that."""
+    p = abi.SfParams()
+    keys = ["interaction_coulomb_energy_coef", "interaction_vdw_energy_coef", "ionic_energy_coef",
+            "pi_cationic_energy_coef", "f2f_pi_stacking_energy_coef",
+            "e2f_pi_stacking_energy_coef", "hbond_energy_coef", "hydrophobic_energy_coef",
+            "torsion_strain_penalty_coef", "rotatable_energy_coef", "gbsa_energy_delta_coef"]
+    raw = [float(node.get(k, 0.0)) for k in keys]
+    eff = list(raw)
+    eff[9] = 0.0
+    if _sf_active(raw[9]):
+        eff[8] = raw[9] if _sf_active(raw[8]) else 0.0
+    for k in range(11):
+        p.coef[k] = eff[k] if _sf_active(raw[k]) or k == 8 else 0.0
+    if _sf_active(raw[1]):
+        v = node["interaction_vdw_energy"]
+        p.vdw_scale = float(v["scale"])
+        p.vdw_cutoff = float(v["cutoff"])
+        for t, ty in enumerate(v["types"][:99]):
+            p.vdw_sigma_scale[t] = float(ty["sigma_scale"])
+            p.vdw_epsilon_scale[t] = float(ty["epsilon_scale"])
+    if _sf_active(raw[2]):
+        v = node["ionic_energy"]
+        p.ionic_coef[0], p.ionic_coef[1] = float(v["lc_coef"]), float(v["pc_coef"])
+        for k, name in enumerate(("lc_inter", "pc_inter")):
+            p.ionic[k][0] = float(v[name]["dist_min"])
+            p.ionic[k][1] = float(v[name]["dist_max"])
+    if _sf_active(raw[3]):
+        v = node["pi_cationic_energy"]
+        for k, name in enumerate(("lc5", "lc6", "pc5", "pc6")):
+            p.picat_coef[k] = float(v[name + "_coef"])
+            p.picat[k][0] = float(v[name + "_inter"]["dist_min"])
+            p.picat[k][1] = float(v[name + "_inter"]["dist_max"])
+    for w, key in ((0, "f2f_pi_stacking_energy"), (1, "e2f_pi_stacking_energy")):
+        if not _sf_active(raw[4 + w]):
+            continue
+        v = node[key]
+        for k, name in enumerate(("l5r5", "l5r6", "l6r5", "l6r6")):
+            p.stack_coef[w][k] = float(v[name + "_coef"])
+            it = v[name + "_inter"]
+            for u, f in enumerate(("dist_min", "dist_max", "angle_min", "angle_max", "sigma_min",
+                                   "sigma_max")):
+                p.stack[w][k][u] = float(it[f])
+    if _sf_active(raw[6]):
+        v = node["hbond_energy"]
+        p.hbond_scale = float(v["scale"])
+        for k, name in enumerate(("hldcc", "hldcn", "hldnc", "hldnn", "hpdcc", "hpdcn", "hpdnc",
+                                  "hpdnn")):
+            p.hbond_coef[k] = float(v[name + "_coef"])
+            it = v[name + "_inter"]
+            for u, f in enumerate(("dist_min", "dist_max", "angle_min", "angle_max", "dist_center",
+                                   "angle_center")):
+                p.hbond[k][u] = float(it[f])
+    if _sf_active(raw[7]):
+        v = node["hydrophobic_energy"]
+        p.hydro_scale = float(v["scale"])
+        p.hydro_dist_min = float(v["dist_min"])
+        p.hydro_dist_max = float(v["dist_max"])
+        p.hydro_scale_factor = float(v["scale_factor"])
+    if not _sf_active(raw[8]):
+        p.coef[8] = 0.0
+    return p
+
+
+def load_scoring_function(path):
+    """(pose_selection, affinity_ranking) pxd_sf_params of a scoring-function file."""
+    with open(path) as f:
+        d = json.load(f)
+    return scoring_function_params(d["pose_selection"]), scoring_function_params(d["affinity_ranking"])

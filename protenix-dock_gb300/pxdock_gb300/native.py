@@ -61,6 +61,11 @@ def load(auto_build=False):
     lib.pxd_ligand_kinematics.argtypes = [vp, C.c_int32, C.c_int32, abi.f64p, abi.f64p, abi.f64p,
                                           abi.f64p, abi.f64p]
     lib.pxd_receptor_kinematics.argtypes = [vp, C.c_int32, abi.f64p, abi.f64p]
+    lib.pxd_set_scoring_function.argtypes = [vp, C.c_int32, C.POINTER(abi.SfParams)]
+    lib.pxd_score_dev.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp]
+    lib.pxd_score.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, abi.f64p, abi.f64p, abi.f64p,
+                              abi.f64p]
+    lib.pxd_score_gbsa.argtypes = [vp, C.c_int32, abi.f64p, abi.f64p, abi.f64p, abi.f64p]
     _lib = lib
     return lib
 
@@ -202,6 +207,32 @@ class Context:
         self._check(self.lib.pxd_ligand_kinematics(self.h, lig, n, _p(_f64(xyz).reshape(-1)),
                                                    _p(centers), _p(rots), _p(tors), _p(out)))
         return out
+
+    def set_scoring_function(self, which, params):
+        self._check(self.lib.pxd_set_scoring_function(self.h, which, C.byref(params)))
+
+    def score(self, which, lig, xyz, tors=None):
+        """Empirical score (0: pose selection, 1: affinity) of poses; returns (score, terms)."""
+        xyz = _f64(xyz)
+        N = self.ligands[lig].n_atoms
+        xyz = xyz.reshape(-1, N, 3)
+        n = xyz.shape[0]
+        tors = _f64(np.zeros((n, self.n_rotors)) if tors is None else tors).reshape(n, self.n_rotors)
+        s = np.zeros(n)
+        terms = np.zeros((n, 11))
+        dummy = np.zeros(1)
+        self._check(self.lib.pxd_score(self.h, which, lig, n, _p(xyz),
+                                       _p(tors if tors.size else dummy), _p(s), _p(terms)))
+        return s, terms
+
+    def gbsa(self, lig, xyz, tors=None):
+        xyz = _f64(xyz).reshape(-1)
+        tors = _f64(np.zeros(self.n_rotors) if tors is None else tors).reshape(-1)
+        d = np.zeros(1)
+        parts = np.zeros(3)
+        self._check(self.lib.pxd_score_gbsa(self.h, lig, _p(xyz), _p(tors if tors.size else np.zeros(1)),
+                                            _p(d), _p(parts)))
+        return d[0], parts
 
     def receptor_kinematics(self, torsions):
         t = _f64(torsions).reshape(-1, self.n_rotors)

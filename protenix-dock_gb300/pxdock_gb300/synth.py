@@ -61,7 +61,7 @@ def _rot(axis, ang):
 
 # --------------------------------------------------------------------- receptor
 def make_receptor(seed=0, n_heavy=1500, cube=26.0, min_dist=1.4, center=(0.0, 0.0, 0.0),
-                  cavity=7.0, n_rotors=0):
+                  cavity=7.0, n_rotors=0, n_rings=(4, 8)):
     rng = np.random.default_rng(seed)
     center = np.asarray(center, float)
     half = cube / 2.0
@@ -136,6 +136,25 @@ def make_receptor(seed=0, n_heavy=1500, cube=26.0, min_dist=1.4, center=(0.0, 0.
     acc_c = list(anions)
     acc_n = [i for i in oxy if i not in anions]
     bond_index = [[parent[h], h] for h in range(n_heavy, n)]
+    # aromatic-ring stand-ins: a carbon near the pocket and its nearest carbons
+    rings5, rings6 = [], []
+    carbons = np.array([i for i in heavy if el[i] == "C"])
+    used = set()
+    if len(carbons) > 12:
+        cx = xyz_a[carbons]
+        order = carbons[np.argsort(np.linalg.norm(cx - center, axis=1))]
+        for size, out, count in ((5, rings5, n_rings[0]), (6, rings6, n_rings[1])):
+            for c0 in order:
+                if len(out) >= count:
+                    break
+                if c0 in used:
+                    continue
+                d = np.linalg.norm(cx - xyz_a[c0], axis=1)
+                near = [int(carbons[k]) for k in np.argsort(d) if int(carbons[k]) not in used][:size]
+                if len(near) < size or c0 not in near:
+                    continue
+                used.update(near)
+                out.append(near)
     ff = {
         "FF_Bonds_atomidx": [], "FF_Bonds_k": [], "FF_Bonds_length": [],
         "FF_Angles_atomidx": [], "FF_Angles_k": [], "FF_Angles_angle": [],
@@ -147,7 +166,7 @@ def make_receptor(seed=0, n_heavy=1500, cube=26.0, min_dist=1.4, center=(0.0, 0.
         "hydrophobic_atomidx": [int(i) for i in hydrophobic],
         "cation_atomidx": [int(i) for i in cations],
         "anion_atomidx": [int(i) for i in anions],
-        "piring5_atomidx": [], "piring6_atomidx": [],
+        "piring5_atomidx": rings5, "piring6_atomidx": rings6,
         "hbonddon_charged_atomidx": [[int(a), int(b)] for a, b in don_c],
         "hbonddon_neut_atomidx": [[int(a), int(b)] for a, b in don_n],
         "hbondacc_charged_atomidx": [int(i) for i in acc_c],
@@ -614,7 +633,9 @@ def _ligand_json(m, rng):
         "FF_ImproperTorsions_phase": [[180.0]] * len(impropers),
         "FF_Nonbonded14_atomidx": [list(p) for p in sorted(nb14)],
         "FF_NonbondedAll_atomidx": [list(p) for p in sorted(allp)],
-        "hydrophobic_atomidx": hydro, "cation_atomidx": [], "anion_atomidx": [],
+        "hydrophobic_atomidx": hydro,
+        "cation_atomidx": [i for i in range(n) if m.ty[i] == T_N3],
+        "anion_atomidx": [i for i in range(n) if m.ty[i] == T_O],
         "piring5_atomidx": ring5, "piring6_atomidx": ring6,
         "tstrain_atomidx_pose_selection": tstrain_idx,
         "tstrain_params_pose_selection": tstrain_par,

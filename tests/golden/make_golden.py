@@ -33,6 +33,31 @@ def write(name, obj):
         f.write("\n")
 
 
+SF_KEYS = ["ligand_ff", "interaction_coulomb_energy_coef", "interaction_vdw_energy_coef",
+           "ionic_energy_coef", "pi_cationic_energy_coef", "f2f_pi_stacking_energy_coef",
+           "e2f_pi_stacking_energy_coef", "hbond_energy_coef", "hydrophobic_energy_coef",
+           "torsion_strain_penalty_coef", "rotatable_energy_coef",
+           "molecular_weight_reward_coef", "gbsa_energy_delta_coef",
+           "interaction_vdw_energy", "ionic_energy", "pi_cationic_energy",
+           "f2f_pi_stacking_energy", "e2f_pi_stacking_energy", "hbond_energy",
+           "hydrophobic_energy"]
+
+
+def scoring_function():
+    """The fields of the default scoring-function file that the engine reads
+    (factory.cpp:144-202): term weights and term parameters."""
+    src = json.load(open("/root/reference/pxdock/data/pscore-v7_and_bscore-fake.json"))
+    out = {}
+    for section in ("pose_selection", "affinity_ranking"):
+        out[section] = {k: v for k, v in src[section].items() if k in SF_KEYS}
+        # terms whose parameter blocks the engine reads but ignores (factory.cpp:136-142)
+        for k in ("interaction_coulomb_energy", "torsion_strain_penalty", "rotatable_energy",
+                  "molecular_weight_reward", "gbsa_energy_delta"):
+            if k in src[section]:
+                out[section][k] = {}
+    write("scoring_function.json", out)
+
+
 def fixtures():
     rec_int = extract("test_interaction.cpp", "receptor_json")[0]
     lig_int = extract("test_interaction.cpp", "ligand_json")[0]
@@ -46,6 +71,7 @@ def fixtures():
     write("utest_optimizer_ligand.json", lig_opt)
     write("utest_conformer_ligand.json", lig_conf)
     write("utest_conformer_receptor.json", rec_conf)
+    scoring_function()
 
 
 if __name__ == "__main__":

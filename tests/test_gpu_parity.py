@@ -55,9 +55,13 @@ def test_maps_match_oracle(complex_small):
         gpu = c["ctx"].read_map(m).astype(np.float64)
         ref = c["port"].grid_map(m, c["box"])
         visited = np.abs(ref[:, 0]) < 1e3  # points a ligand atom can occupy
-        err = np.abs(gpu[visited] - ref[visited])
-        scale = np.maximum(1.0, np.abs(ref[visited]))
-        assert np.max(err / scale) < 2e-5, (m, np.max(err / scale))
+        err = np.max(np.abs(gpu[visited] - ref[visited]), axis=1)
+        # FP32 records: error relative to the record's largest component
+        scale = np.maximum(1.0, np.max(np.abs(ref[visited]), axis=1))
+        assert np.max(err / scale) < 2e-6, (m, np.max(err / scale))
+        # where the physics is mild (|E| < 10), the absolute error is tiny
+        mild = np.abs(ref[:, 0]) < 10.0
+        assert np.max(np.abs(gpu[mild, 0] - ref[mild, 0])) < 1e-4
         # everywhere else the records agree to FP32 relative precision
         hi = ~visited
         if hi.any():

@@ -304,3 +304,82 @@ def test_rng_distributions():
         n = np.linalg.norm(v)
         assert n < 1.0 and n != prev
         prev = n
+
+
+def _lists(**kw):
+    ff = {}
+    ff.update(kw)
+    return model.ScoreLists(ff, kw.pop("_n", 0), ligand=True)
+
+
+def test_torsion_strain_penalty():
+    """test_scorer.cpp:25-94"""
+    xyz = np.array([
+        [-19.492, 19.720, -7.201], [-19.063, 18.558, -7.938], [-18.960, 18.607, -9.386],
+        [-20.077, 17.159, -7.527], [-21.147, 17.375, -6.637], [-21.982, 16.325, -6.257],
+        [-21.750, 15.047, -6.749], [-20.675, 14.819, -7.609], [-19.827, 15.867, -7.998],
+        [-18.539, 15.433, -9.053], [-17.500, 18.112, -7.433], [-16.455, 17.929, -8.463],
+        [-15.587, 19.154, -8.657], [-14.229, 19.120, -8.308], [-13.422, 20.244, -8.487],
+        [-13.959, 21.408, -9.034], [-15.298, 21.443, -9.417], [-16.107, 20.321, -9.239],
+        [-17.198, 18.289, -5.976], [-16.256, 17.156, -5.513], [-15.287, 17.773, -4.563],
+        [-15.163, 19.208, -4.949], [-16.534, 19.601, -5.524], [-17.337, 20.458, -4.579],
+        [-17.723, 20.058, -3.207], [-20.147, 19.632, -3.822], [-17.359, 22.127, -4.945],
+        [-16.891, 22.222, -6.310], [-18.666, 22.636, -4.594], [-16.156, 22.842, -3.870],
+        [-16.567, 23.231, -2.585]])
+    ff = {"tstrain_atomidx_pose_selection": [[[4, 3, 1, 10]], [[30, 29, 26, 23]],
+                                              [[3, 1, 10, 11], [3, 1, 10, 18]],
+                                              [[29, 26, 23, 22], [29, 26, 23, 24]]],
+          "tstrain_params_pose_selection": [[0.1, 0.2, 0.3, 0.4], [0.4, 0.3, 0.2, 0.1],
+                                             [0.2, 0.1, 0.4, 0.3], [0.3, 0.4, 0.1, 0.2]]}
+    lists = model.ScoreLists(ff, len(xyz), ligand=True)
+    keep = []
+    c = lists.to_c(keep)
+    x = np.ascontiguousarray(xyz.reshape(-1))
+    v = O.port_lib().po_torsion_strain(O.C.byref(c), x.ctypes.data_as(abi.f64p))
+    assert abs(v - 5.07775) < 1e-5
+
+
+def test_rotatable_energy_term():
+    """test_scorer.cpp:96-105: -1 / (2.620643 + 3)"""
+    sf = abi.SfParams()
+    sf.coef[abi.TERM_NAMES.index("rotatable_energy")] = 1.0
+    from types import SimpleNamespace as NS
+
+    empty = model.Topology(0, [], [], [])
+    rec = NS(n_atoms=0, ff=empty, lists=model.ScoreLists({}, 0, ligand=False))
+    lig = NS(n_atoms=0, ff=empty, vdw_type=np.zeros(0, np.int32),
+             lists=model.ScoreLists({"rotatable_bond_index": [[0, 1], [1, 2], [2, 3]]}, 0,
+                                    ligand=True))
+    v, terms = O.port_score(sf, rec, lig, np.zeros((0, 3)), np.zeros((0, 3)))
+    assert abs(v - -0.1779) < 1e-4
+
+
+def test_gbsa_ligand_only():
+    """test_scorer.cpp:107-169: ligand-only GB/SA, empty receptor."""
+    xyz = np.array([[7.9080, 27.7630, 9.3690], [8.8900, 26.6620, 8.9590], [8.1900, 25.3030, 9.0050],
+                    [9.4720, 26.9770, 7.5650], [8.8060, 26.2340, 6.3930], [9.7810, 25.6780, 5.4450],
+                    [10.4820, 24.5270, 5.6590], [10.2550, 23.7160, 6.5680], [7.8577, 27.8194, 10.4664],
+                    [8.2507, 28.7281, 8.9676], [6.9102, 27.5324, 8.9676], [9.7322, 26.6217, 9.6655],
+                    [8.0365, 25.0049, 10.0527], [7.2166, 25.3746, 8.4977], [8.8135, 24.5520, 8.4977],
+                    [9.3648, 28.0573, 7.3878], [10.5178, 26.6366, 7.5871], [8.2962, 25.3296, 6.7565],
+                    [9.8020, 26.0140, 4.4710]])
+    q = np.array([-0.0861, -0.0617, -0.0861, -0.0604, 0.0017, -0.5409, 0.6301, -0.6651, 0.0304,
+                  0.0304, 0.0304, 0.0117, 0.0304, 0.0304, 0.0304, 0.0442, 0.0442, 0.0477, 0.3655])
+    ff = {"atomic_numbers": [6, 6, 6, 6, 6, 7, 6, 8, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1],
+          "bond_index": [[0, 1], [1, 2], [1, 3], [3, 4], [4, 5], [5, 6], [6, 7], [0, 8], [0, 9],
+                         [0, 10], [1, 11], [2, 12], [2, 13], [2, 14], [3, 15], [3, 16], [4, 17],
+                         [5, 18]]}
+    ll = model.ScoreLists(ff, 19, ligand=True)
+    rl = model.ScoreLists({}, 0, ligand=False)
+    keep = []
+    lc, rc = ll.to_c(keep), rl.to_c(keep)
+    parts = np.zeros(3)
+    x = np.ascontiguousarray(xyz.reshape(-1))
+    d = O.port_lib().po_gbsa_parts(0, np.zeros(3).ctypes.data_as(abi.f64p),
+                                   np.zeros(1).ctypes.data_as(abi.f64p), O.C.byref(rc), 19,
+                                   x.ctypes.data_as(abi.f64p), q.ctypes.data_as(abi.f64p),
+                                   O.C.byref(lc), parts.ctypes.data_as(abi.f64p))
+    assert abs(parts[1] - -14.4667) < 1e-4  # Gbsa_Lig_Energy
+    assert abs(parts[2]) < 1e-4             # Gbsa_Pro_Energy
+    assert abs(parts[0] - -14.4667) < 1e-4  # Gbsa_Com_Energy
+    assert abs(d) < 1e-4

@@ -147,3 +147,27 @@ def test_rng_streams():
                 b = rl.ref_rng_uniform_real(h, -2.0, 5.0)
             assert a == b, (seed, k, a, b)
         rl.ref_rng_destroy(h)
+
+
+def test_scores_match_reference(system, tmp_path_factory, golden):
+    """pscore and bscore (root_scorer::combine) of the port against the reference."""
+    rec, lig, port, ref = system
+    sf_path = os.path.join(golden, "scoring_function.json")
+    ref.load_sf(sf_path)
+    pose_sf, aff_sf = model.load_scoring_function(sf_path)
+    rng = np.random.default_rng(13)
+    for k in range(4):
+        x = lig.poses[0] + rng.normal(scale=0.5, size=lig.poses[0].shape)
+        t = rng.uniform(-2, 2, size=3)
+        rx = port.receptor_apply(t)
+        for which, sf in ((0, pose_sf), (1, aff_sf)):
+            v_ref, terms_ref = ref.score(which, rx, x)
+            v, terms = port.score(sf, rx, x)
+            assert abs(v - v_ref) <= 1e-10 * max(1.0, abs(v_ref)), (which, v, v_ref)
+            # leaf values that the reference reports under their own names
+            for i in (0, 1, 2, 3, 4, 5, 6, 7, 8, 10):
+                if terms_ref[i] != 0.0:
+                    assert abs(terms[i] - terms_ref[i]) <= 1e-10 * max(1.0, abs(terms_ref[i])), (which, i)
+    # the synthetic system exercises every pose-selection term family
+    _, terms = port.score(pose_sf, port.receptor_apply([0.0, 0.0, 0.0]), lig.poses[0])
+    assert np.count_nonzero(terms[:9]) >= 6
