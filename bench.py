@@ -241,6 +241,7 @@ def _ref_sample(rec, lig, box, poses, threads, target_s):
 
 
 def main():
+    global N_POSES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -250,7 +251,6 @@ def main():
     ap.add_argument("--poses", type=int, default=N_POSES,
                     help="poses per step (smaller only for profiling captures)")
     args = ap.parse_args()
-    global N_POSES
     N_POSES = args.poses
     if args.impl == "reference":
         return run_reference(args)

@@ -89,6 +89,10 @@ def port_lib():
         lib.po_gbsa_parts.restype = C.c_double
         lib.po_gbsa_parts.argtypes = [C.c_int, f64p, f64p, C.POINTER(abi.ScoreLists), C.c_int,
                                       f64p, f64p, C.POINTER(abi.ScoreLists), f64p]
+        lib.po_mc_walker.argtypes = [C.c_void_p, C.POINTER(abi.SfParams), C.POINTER(abi.ScoreLists),
+                                     C.POINTER(abi.ScoreLists), f64p, f64p, C.c_uint32, C.c_int,
+                                     f64p, C.c_int, C.c_int, C.c_int, C.c_double, f64p, f64p, f64p,
+                                     f64p, f64p, C.POINTER(C.c_long)]
         lib.po_rng_uniform_int.restype = C.c_int
         lib.po_rng_uniform_real.restype = C.c_double
         lib.po_rng_uniform_real.argtypes = [C.c_void_p, C.c_double, C.c_double]
@@ -251,6 +255,23 @@ class PortSystem:
     def score(self, sf, rec_xyz, lig_xyz):
         """root_scorer::combine with the scoring function sf; returns (score, terms[11])."""
         return port_score(sf, self.receptor, self.ligand, rec_xyz, lig_xyz)
+
+    def mc_walker(self, sf, lo, hi, seed, walker, start, first_pose, max_nsteps, relax_nsteps,
+                  threshold=-1.0, global_min=None):
+        keep = []
+        rl = self.receptor.lists.to_c(keep)
+        ll = self.ligand.lists.to_c(keep)
+        xyz = np.zeros(self.n_lig * 3)
+        tors = np.zeros(max(self.n_tors, 1))
+        e, ps = np.zeros(1), np.zeros(1)
+        nev = C.c_long(0)
+        gm = np.array([1e8 if global_min is None else global_min])
+        st = self.lib.po_mc_walker(self.h, C.byref(sf), C.byref(rl), C.byref(ll), _p(_d(lo)), _p(_d(hi)),
+                                   seed, walker, _p(_d(start).reshape(-1)), int(first_pose), max_nsteps,
+                                   relax_nsteps, threshold, _p(gm), _p(xyz), _p(tors), _p(e), _p(ps),
+                                   C.byref(nev))
+        return dict(status=st, xyz=xyz.reshape(-1, 3), torsions=tors[: self.n_tors], energy=e[0],
+                    pscore=ps[0], nevals=nev.value, global_min=gm[0])
 
 
 def port_score(sf, receptor, ligand, rec_xyz, lig_xyz):

@@ -1760,3 +1760,213 @@ double po_gbsa_parts(int n_rec, const double* rec_xyz, const double* rec_q, cons
     po_mol L = {n_lig, lig_xyz, lig_q, NULL, NULL, NULL, lig_l};
     return term_gbsa(&R, &L, parts);
 }
+
+/* ======================================= Monte-Carlo walker (searcher.cpp:46-223) */
+static double geometric_center(const double* x, int n, double* c) {
+    c[0] = c[1] = c[2] = 0.0;
+    for (int i = 0; i < n; ++i) v_addi(c, x + 3 * i);
+    v_scalei(c, 1.0 / n);
+    return 0.0;
+}
+
+static int atom_in_box(const double* p, const double* lo, const double* hi) {
+    return p[0] > lo[0] && p[0] < hi[0] && p[1] > lo[1] && p[1] < hi[1] && p[2] > lo[2] && p[2] < hi[2];
+}
+
+static int all_in_box(const double* x, int n, const double* lo, const double* hi) {
+    for (int i = 0; i < n; ++i)
+        if (!atom_in_box(x + 3 * i, lo, hi)) return 0;
+    return 1;
+}
+
+typedef struct {
+    const po_system* s;
+    const pxd_sf_params* sf;
+    const pxd_score_lists* rl;
+    const pxd_score_lists* ll;
+    const double* rec_q;
+    const double* rec_sigma;
+    const double* rec_eps;
+} mc_env;
+
+static double mc_pscore(const mc_env* e, const double* tors, const double* xyz, double* rec_buf) {
+    po_receptor_apply(e->s, tors, rec_buf);
+    return po_score(e->sf, e->s->n_rec, rec_buf, e->s->rec.t.charge, e->s->rec.t.sigma, e->s->rec.t.epsilon,
+                    e->rl, e->s->n_lig, xyz, e->s->lig.t.charge, e->s->lig_type, e->ll, NULL);
+}
+
+/* randomize (searcher.cpp:46-87) */
+static void mc_randomize(const mc_env* e, const double* start, int first_pose, const double* lo,
+                         const double* hi, po_rng* rg, double* out) {
+    const po_system* s = e->s;
+    const int n = s->n_lig, T = s->n_tors;
+    double center[3], q[4], R[9];
+    double* tors = (double*)calloc((size_t)(T + 1), sizeof(double));
+    int num = 0;
+    while (1) {
+        po_rng_in_box(rg, lo, hi, center);
+        po_rng_orientation(rg, q);
+        for (int i = 0; i < T; ++i)
+            if (first_pose) tors[i] = po_rng_torsion(rg);
+        po_rotation_quaternion(q, R);
+        po_ligand_apply(s, start, center, R, tors, out);
+        ++num;
+        if (num < 2000 && !all_in_box(out, n, lo, hi)) continue;
+        double c[3];
+        geometric_center(out, n, c);
+        if (!atom_in_box(c, lo, hi)) continue;
+        if (num > 1999 || po_vdw_check(e->sf, s->n_rec, s->rec_xyz0, e->rec_sigma, e->rec_eps, n, out,
+                                       s->lig_type) < 100.0)
+            break;
+    }
+    free(tors);
+}
+
+/* mutate_inplace (searcher.cpp:189-223); returns 0 when the rotation was skipped */
+static int mc_mutate(const po_system* s, po_rng* rg, double* xyz) {
+    const int n = s->n_lig, T = s->n_tors;
+    const int which = po_rng_uniform_int(rg, 0, T + 1);
+    double center[3], delta[3];
+    geometric_center(xyz, n, center);
+    if (which == 0) {
+        po_rng_in_sphere(rg, delta);
+        v_scalei(delta, 2.0);
+        v_addi(center, delta);
+    }
+    double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (which == 1) {
+        double acc = 0.0;
+        for (int i = 0; i < n; ++i) {
+            double t = 0.0;
+            t += (xyz[3 * i] - center[0]) * (xyz[3 * i] - center[0]);
+            t += (xyz[3 * i + 1] - center[1]) * (xyz[3 * i + 1] - center[1]);
+            t += (xyz[3 * i + 2] - center[2]) * (xyz[3 * i + 2] - center[2]);
+            acc += t;
+        }
+        double gr = n > 0 ? sqrt(acc / n) : 0.0;
+        if (gr < 1e-6) return 0;
+        po_rng_in_sphere(rg, delta);
+        v_scalei(delta, 2.0 / gr);
+        gr = v_norm(delta);
+        v_scalei(delta, 1.0 / gr);
+        rotation_axis_angle(delta, gr, R);
+    }
+    double* tors = (double*)calloc((size_t)(T + 1), sizeof(double));
+    if (which > 1) tors[which - 2] = po_rng_torsion(rg);
+    double* tmp = (double*)malloc((size_t)n * 3 * sizeof(double));
+    po_ligand_apply(s, xyz, center, R, tors, tmp);
+    memcpy(xyz, tmp, (size_t)n * 3 * sizeof(double));
+    free(tmp);
+    free(tors);
+    return 1;
+}
+
+typedef struct {
+    double* xyz;
+    double* tors;
+    double energy, pscore;
+    long nevals;
+} mc_state;
+
+static void mc_copy(mc_state* d, const mc_state* s, int n, int T) {
+    memcpy(d->xyz, s->xyz, (size_t)n * 3 * sizeof(double));
+    memcpy(d->tors, s->tors, (size_t)(T + 1) * sizeof(double));
+    d->energy = s->energy;
+    d->pscore = s->pscore;
+    d->nevals = s->nevals;
+}
+
+/* One walker of monte_carlo_searcher::mutate_and_optimize (searcher.cpp:98-187).
+ * start: the ligand pose the walker starts from; first_pose: 1 when that pose is the
+ * file's first pose (then torsions are randomised as well). walker 0 only relaxes.
+ * global_min: the shared pre-optimisation energy minimum when threshold > 0.
+ * Returns 0 ok, 1 crashed (nevals set to 0), 2 relaxed start left the box. */
+int po_mc_walker(po_system* s, const pxd_sf_params* sf, const pxd_score_lists* rl, const pxd_score_lists* ll,
+                 const double* lo, const double* hi, uint32_t seed, int walker, const double* start,
+                 int first_pose, int max_nsteps, int relax_nsteps, double threshold, double* global_min,
+                 double* out_xyz, double* out_tors, double* out_energy, double* out_pscore, long* out_nevals) {
+    const int n = s->n_lig, R = s->n_rotors;
+    mc_env e = {s, sf, rl, ll, s->rec.t.charge, s->rec.t.sigma, s->rec.t.epsilon};
+    po_rng rg;
+    po_rng_seed(&rg, seed + (uint32_t)walker);
+    double* rec_buf = (double*)malloc((size_t)(s->n_rec + 1) * 3 * sizeof(double));
+    double* mem = (double*)calloc((size_t)3 * (3 * n + R + 1), sizeof(double));
+    mc_state out = {mem, mem + 3 * n, 0, 0, 0};
+    mc_state tmp = {mem + 3 * n + R + 1, mem + 6 * n + R + 1, 0, 0, 0};
+    mc_state cdd = {mem + 6 * n + 2 * R + 2, mem + 9 * n + 2 * R + 2, 0, 0, 0};
+    pxd_lbfgs_params full, fast;
+    full.max_iter = 240; full.max_eval = 0; full.history = 100; full.ls_max = 25; full.lr = 1.0;
+    full.tolerance_grad = 0.5; full.tolerance_change = 1e-4; full.ls_c1 = 1e-4; full.ls_c2 = 0.9;
+    full.ls_tolerance_change = 1e-9; full.ls_gtd_threshold = 1e5; full.reset_threshold = 1e8;
+    fast = full;
+    fast.max_iter = relax_nsteps;
+    po_work w;
+    work_init(s, &w);
+    int32_t nev = 0;
+    if (walker == 0)
+        memcpy(out.xyz, start, (size_t)n * 3 * sizeof(double));
+    else
+        mc_randomize(&e, start, first_pose, lo, hi, &rg, out.xyz);
+    lbfgs_work(s, &w, &full, out.tors, out.xyz, &out.energy, &nev);
+    out.nevals = nev;
+    out.pscore = mc_pscore(&e, out.tors, out.xyz, rec_buf);
+    int status = 0;
+    if (walker != 0) {
+        if (all_in_box(out.xyz, n, lo, hi)) {
+            mc_copy(&tmp, &out, n, R);
+            long total = out.nevals;
+            for (int step = 0; step < max_nsteps; ++step) {
+                mc_copy(&cdd, &tmp, n, R);
+                mc_mutate(s, &rg, cdd.xyz);
+                if (threshold > 0.0 && global_min) {
+                    double tg[PXD_MAX_RECEPTOR_TORSIONS + 1];
+                    double* lg = (double*)malloc((size_t)n * 3 * sizeof(double));
+                    const double pre = score_grad_work(s, &w, cdd.tors, cdd.xyz, tg, lg);
+                    free(lg);
+                    if (pre < *global_min) *global_min = pre;
+                    if (pre > *global_min + threshold) continue;
+                }
+                lbfgs_work(s, &w, &fast, cdd.tors, cdd.xyz, &cdd.energy, &nev);
+                cdd.nevals = nev;
+                total += cdd.nevals;
+                cdd.pscore = mc_pscore(&e, cdd.tors, cdd.xyz, rec_buf);
+                int accept = step == 0;
+                if (!accept) {
+                    if (cdd.pscore < tmp.pscore)
+                        accept = 1;
+                    else
+                        accept = po_rng_uniform_real(&rg, 0.0, 1.0) < exp((tmp.pscore - cdd.pscore) / 1.2);
+                }
+                if (accept && all_in_box(cdd.xyz, n, lo, hi)) {
+                    mc_copy(&tmp, &cdd, n, R);
+                    if (tmp.pscore < out.pscore) {
+                        lbfgs_work(s, &w, &full, tmp.tors, tmp.xyz, &tmp.energy, &nev);
+                        tmp.nevals = nev;
+                        total += tmp.nevals;
+                        tmp.pscore = mc_pscore(&e, tmp.tors, tmp.xyz, rec_buf);
+                        if (tmp.pscore < out.pscore) mc_copy(&out, &tmp, n, R);
+                    }
+                }
+            }
+            out.nevals = total;
+        } else {
+            int big = 0;
+            for (int i = 0; i < 3 * n; ++i) big |= (out.xyz[i] > 1e8 || out.xyz[i] < -1e8);
+            if (big) {
+                out.nevals = 0;
+                status = 1;
+            } else {
+                status = 2;
+            }
+        }
+    }
+    memcpy(out_xyz, out.xyz, (size_t)n * 3 * sizeof(double));
+    memcpy(out_tors, out.tors, (size_t)R * sizeof(double));
+    *out_energy = out.energy;
+    *out_pscore = out.pscore;
+    *out_nevals = out.nevals;
+    work_free(&w);
+    free(mem);
+    free(rec_buf);
+    return status;
+}

@@ -76,6 +76,13 @@ double po_gbsa_parts(int n_rec, const double* rec_xyz, const double* rec_q,
                      const pxd_score_lists* rec_l, int n_lig, const double* lig_xyz,
                      const double* lig_q, const pxd_score_lists* lig_l, double* parts);
 
+/* ---- Monte-Carlo walker (engine/src/core/searcher.cpp:46-223) ---- */
+int po_mc_walker(po_system* s, const pxd_sf_params* sf, const pxd_score_lists* rl,
+                 const pxd_score_lists* ll, const double* lo, const double* hi, uint32_t seed,
+                 int walker, const double* start, int first_pose, int max_nsteps,
+                 int relax_nsteps, double threshold, double* global_min, double* out_xyz,
+                 double* out_tors, double* out_energy, double* out_pscore, long* out_nevals);
+
 /* ---- mt19937 + libstdc++ distributions as random_generator uses them
  *      (engine/include/bytedock/lib/random.h:33-63, engine/src/lib/random.cpp) ---- */
 typedef struct po_rng {

@@ -364,7 +364,8 @@ int upload_explicit(pxd_context* ctx, const std::vector<int>& atoms, const std::
                                  static_cast<float>(ctx->rec_xyz[3 * a + 2]),
                                  static_cast<float>(ctx->rec_charge[a])));
         se.push_back(make_float2(static_cast<float>(ctx->rec_sigma[a]), static_cast<float>(ctx->rec_epsilon[a])));
-        loc.push_back(local_of[a]);
+        // only rotor atoms move; every other atom keeps its stored position
+        loc.push_back(ctx->is_mov[a] ? local_of[a] : -1);
     }
     offs[0] = pk.put(xq);
     offs[1] = pk.put(se);
@@ -983,8 +984,6 @@ int pxd_score_grad_dev(pxd_context* ctx, int32_t n_poses, int32_t max_atoms, con
     if (rc) return rc;
     if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS)
         return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");
-    for (auto& e : ctx->ligands)
-        if (e.n_atoms > max_atoms) return set_error(ctx, PXD_ERR_INVALID, "max_atoms below a ligand's size");
     if (ctx->rec.n_rotors > 0 && (!tors || !tors_grad))
         return set_error(ctx, PXD_ERR_INVALID, "receptor torsion buffers required");
     return launch_score(ctx, n_poses, max_atoms, ids, xyz, tors, energy, lig_grad, tors_grad, pick(ctx, stream));
@@ -999,8 +998,6 @@ int pxd_lbfgs_dev(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses, 
         return set_error(ctx, PXD_ERR_INVALID, "bad L-BFGS parameters");
     if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS)
         return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");
-    for (auto& e : ctx->ligands)
-        if (e.n_atoms > max_atoms) return set_error(ctx, PXD_ERR_INVALID, "max_atoms below a ligand's size");
     if (ctx->rec.n_rotors > 0 && !tors) return set_error(ctx, PXD_ERR_INVALID, "receptor torsion buffer required");
     return launch_lbfgs(ctx, *p, n_poses, max_atoms, ids, xyz, tors, energy, nevals, status, pick(ctx, stream));
 }

@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp)
         pose = __shfl_sync(kFull, pose, 0);
         if (pose >= a.n_poses) break;
         const int lid = a.lig_ids[pose];
-        if (lid < 0 || lid >= a.n_ligands) {
+        if (lid < 0 || lid >= a.n_ligands || a.ligands[lid].n_atoms > a.max_atoms) {
             if (lane == 0) {
                 a.status[pose] = PXD_POSE_BAD_INPUT;
                 a.nevals[pose] = 0;
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp) score_kernel(const Sco
     const int nw = gridDim.x * kWarpsPerBlock;
     for (int pose = blockIdx.x * kWarpsPerBlock + wib; pose < a.n_poses; pose += nw) {
         const int lid = a.lig_ids[pose];
-        if (lid < 0 || lid >= a.n_ligands) {
+        if (lid < 0 || lid >= a.n_ligands || a.ligands[lid].n_atoms > a.max_atoms) {
             if (lane == 0) a.energy[pose] = nan("");
             continue;
         }

@@ -286,7 +286,8 @@ __global__ void __launch_bounds__(kScoreWarps * kWarp) empirical_score_kernel(co
     const int R = a.rec.n_rotors;
     for (int pose = blockIdx.x * kScoreWarps + wib; pose < a.n_poses; pose += gridDim.x * kScoreWarps) {
         const int lid = a.lig_ids[pose];
-        if (lid < 0 || lid >= a.n_ligands || !a.ligands[lid].score.has) {
+        if (lid < 0 || lid >= a.n_ligands || !a.ligands[lid].score.has ||
+            a.ligands[lid].n_atoms > a.max_atoms) {
             if (lane == 0) a.score[pose] = nan("");
             continue;
         }
@@ -455,8 +456,6 @@ int pxd_score_dev(pxd_context* ctx, int32_t which, int32_t n_poses, int32_t max_
         return set_error(ctx, PXD_ERR_INVALID, "bad score batch");
     if (!ctx->has_receptor) return set_error(ctx, PXD_ERR_STATE, "set a receptor first");
     if (!ctx->sf_set[which]) return set_error(ctx, PXD_ERR_STATE, "set the scoring function first");
-    for (auto& e : ctx->ligands)
-        if (e.n_atoms > max_atoms) return set_error(ctx, PXD_ERR_INVALID, "max_atoms below a ligand's size");
     if (ctx->rec.n_rotors > 0 && !tors) return set_error(ctx, PXD_ERR_INVALID, "receptor torsion buffer required");
     cudaSetDevice(ctx->device);
     if (n_poses == 0) return PXD_OK;

@@ -171,3 +171,43 @@ def test_scores_match_reference(system, tmp_path_factory, golden):
     # the synthetic system exercises every pose-selection term family
     _, terms = port.score(pose_sf, port.receptor_apply([0.0, 0.0, 0.0]), lig.poses[0])
     assert np.count_nonzero(terms[:9]) >= 6
+
+
+def test_mc_walkers_match_reference(tmp_path, golden):
+    """monte_carlo_searcher walkers. Walker 0 (relax only) matches to rounding. Random
+    walkers start from clashing poses whose relaxation amplifies last-bit differences
+    (the reference sums rotor-atom pairs and score terms in hash-container order), so
+    they are compared as a population: same outcome classes, similar best scores."""
+    rj = synth.make_receptor(seed=0, n_heavy=500, cube=24.0, cavity=8.0, n_rotors=3)
+    lj = synth.make_ligand(seed=1)
+    rp, lp = str(tmp_path / "r.json"), str(tmp_path / "l.json")
+    json.dump(rj, open(rp, "w"))
+    json.dump(lj, open(lp, "w"))
+    rec, lig = model.Receptor.from_json(rj), model.Ligand.from_json(lj)
+    port, ref = O.PortSystem(rec, lig), O.RefSystem(rp, lp)
+    center, size, spacing = (0.0, 0.0, 0.0), (16.0, 16.0, 16.0), 1.0
+    ref.build_grid(center, size, spacing)
+    box = model.make_box(center, size, spacing)
+    port.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)))
+    ref.set_slope(1e6)
+    port.set_slope(1e6)
+    sf_path = os.path.join(golden, "scoring_function.json")
+    ref.load_sf(sf_path)
+    pose_sf, _ = model.load_scoring_function(sf_path)
+    lo = np.array(box.init_xyz)
+    hi = lo + (np.array(box.npoints) - 1) * box.spacing
+    a = port.mc_walker(pose_sf, lo, hi, 7, 0, lig.poses[0], True, 12, 15)
+    b = ref.mc_walker(7, 0, 12, 15)
+    assert a["nevals"] == b["nevals"]
+    assert rel(a["xyz"], b["xyz"]) < 1e-6
+    assert abs(a["pscore"] - b["pscore"]) <= 1e-6 * max(1.0, abs(b["pscore"]))
+    ps_a, ps_b, same_class = [], [], 0
+    for walker in range(1, 13):
+        a = port.mc_walker(pose_sf, lo, hi, 7, walker, lig.poses[0], True, 4, 15)
+        b = ref.mc_walker(7, walker, 4, 15)
+        same_class += (a["nevals"] == 0) == (b["nevals"] == 0)
+        if a["nevals"] and b["nevals"]:
+            ps_a.append(a["pscore"])
+            ps_b.append(b["pscore"])
+    assert same_class >= 10
+    assert abs(np.median(ps_a) - np.median(ps_b)) < 0.5 + 0.1 * abs(np.median(ps_b))
