@@ -351,6 +351,58 @@ int pxd_score(pxd_context* ctx, int32_t which, int32_t ligand_id, int32_t n_pose
 int pxd_score_gbsa(pxd_context* ctx, int32_t ligand_id, const double* lig_xyz,
                    const double* rec_tors, double* delta, double* parts);
 
+/* ------------------------------------------------------- Monte-Carlo search */
+
+/* Constants of one Monte-Carlo search (monte_carlo_searcher, searcher.h:29-41 and the
+ * search() arguments, entrance.cpp:318-330). pxd_mc_defaults() gives the reference's. */
+typedef struct pxd_mc_params {
+    uint32_t seed;                 /* walker w draws from mt19937(seed + w) */
+    int32_t max_nsteps;            /* 200 */
+    int32_t relax_nsteps;          /* 40: L-BFGS iterations after each move */
+    int32_t full_nsteps;           /* 240: L-BFGS iterations of a full relaxation */
+    double mc_mmenergy_threshold;  /* -1: no pruning on the pre-relaxation energy */
+    double amplitude;              /* 2 A: translation radius and rotation scale */
+    double temperature;            /* 1.2: Metropolis temperature on the pose score */
+    double box_lo[3], box_hi[3];   /* search box (grid box, or the set_box box) */
+    pxd_lbfgs_params lbfgs;        /* optimiser constants (history, tolerances, ...) */
+} pxd_mc_params;
+
+void pxd_mc_defaults(pxd_mc_params* out);
+
+/* Runs n_walkers Monte-Carlo walkers in one persistent launch, one warp per walker:
+ * random start (walker != 0), full relaxation, then max_nsteps moves of translation /
+ * rotation / one torsion, each relaxed, scored by the pose-selection score and accepted
+ * by Metropolis; a new best is fully relaxed again (searcher.cpp:46-223).
+ *   ligand_ids_dev [W] int32, walker_ids_dev [W] int32 (the reference's pose_id: seeds
+ *   the walker's generator; walker 0 only relaxes its start pose),
+ *   first_pose_dev [W] int32 (1: the start is the ligand file's first pose, so torsions
+ *   are randomised too), start_xyz_dev [W][max_atoms][3] float.
+ *   Outputs: best pose xyz [W][max_atoms][3], receptor torsions [W][R], MM energy,
+ *   pose score (double), evaluations and a status (0 ok, 1 crashed: coordinates beyond
+ *   1e8 after the first relaxation, 2 relaxed start outside the box: no moves).
+ *   global_min_dev [n_ligands] double (in/out) holds the pruning minimum per ligand;
+ *   may be NULL when mc_mmenergy_threshold <= 0. */
+int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* params, int32_t n_walkers,
+                      int32_t max_atoms, const int32_t* ligand_ids_dev,
+                      const int32_t* walker_ids_dev, const int32_t* first_pose_dev,
+                      const float* start_xyz_dev, float* out_xyz_dev, float* out_tors_dev,
+                      double* out_energy_dev, double* out_pscore_dev, int32_t* out_nevals_dev,
+                      int32_t* out_status_dev, double* global_min_dev, void* stream);
+
+/* Host-buffer version for the walkers of one ligand (double in / out). */
+int pxd_mc_search(pxd_context* ctx, const pxd_mc_params* params, int32_t ligand_id,
+                  int32_t n_walkers, const int32_t* walker_ids, const int32_t* first_pose,
+                  const double* start_xyz, double* out_xyz, double* out_tors, double* out_energy,
+                  double* out_pscore, int32_t* out_nevals, int32_t* out_status);
+
+/* Draws of the walker generator as the reference's random_generator makes them
+ * (mt19937 + libstdc++ distributions, random.h:33-63), for checking the device stream:
+ * kinds[i] = 0 uniform_int(0, ints[i]), 1 uniform_torsion, 2 uniform_real(0, 1),
+ * 3 random_in_sphere (3 values), 4 random_orientation (4 values). out gets the values
+ * in order. */
+int pxd_rng_draws(pxd_context* ctx, uint32_t seed, int32_t n, const int32_t* kinds,
+                  const int32_t* ints, double* out);
+
 #ifdef __cplusplus
 }
 #endif

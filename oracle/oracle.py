@@ -93,6 +93,8 @@ def port_lib():
                                      C.POINTER(abi.ScoreLists), f64p, f64p, C.c_uint32, C.c_int,
                                      f64p, C.c_int, C.c_int, C.c_int, C.c_double, f64p, f64p, f64p,
                                      f64p, f64p, C.POINTER(C.c_long)]
+        lib.po_mc_randomize.argtypes = [C.c_void_p, C.POINTER(abi.SfParams), f64p, f64p, C.c_uint32,
+                                        C.c_int, f64p, C.c_int, f64p]
         lib.po_rng_uniform_int.restype = C.c_int
         lib.po_rng_uniform_real.restype = C.c_double
         lib.po_rng_uniform_real.argtypes = [C.c_void_p, C.c_double, C.c_double]
@@ -272,6 +274,36 @@ class PortSystem:
                                    C.byref(nev))
         return dict(status=st, xyz=xyz.reshape(-1, 3), torsions=tors[: self.n_tors], energy=e[0],
                     pscore=ps[0], nevals=nev.value, global_min=gm[0])
+
+    def mc_randomize(self, sf, lo, hi, seed, walker, start, first_pose=True):
+        out = np.zeros(self.n_lig * 3)
+        self.lib.po_mc_randomize(self.h, C.byref(sf), _p(_d(lo)), _p(_d(hi)), seed, walker,
+                                 _p(_d(start).reshape(-1)), int(first_pose), _p(out))
+        return out.reshape(-1, 3)
+
+
+def port_rng_draws(seed, kinds, ints):
+    """The draw sequence pxd_rng_draws makes, from the port's generator."""
+    lib = port_lib()
+
+    class Rng(C.Structure):
+        _fields_ = [("mt", C.c_uint32 * 624), ("idx", C.c_int)]
+
+    r = Rng()
+    lib.po_rng_seed(C.byref(r), seed)
+    out = []
+    for k, n in zip(kinds, ints):
+        if k == 0:
+            out.append(lib.po_rng_uniform_int(C.byref(r), 0, int(n)))
+        elif k == 1:
+            out.append(lib.po_rng_torsion(C.byref(r)))
+        elif k == 2:
+            out.append(lib.po_rng_uniform_real(C.byref(r), 0.0, 1.0))
+        else:
+            v = np.zeros(3 if k == 3 else 4)
+            (lib.po_rng_in_sphere if k == 3 else lib.po_rng_orientation)(C.byref(r), _p(v))
+            out.extend(v.tolist())
+    return np.array(out, np.float64)
 
 
 def port_score(sf, receptor, ligand, rec_xyz, lig_xyz):

@@ -1970,3 +1970,13 @@ int po_mc_walker(po_system* s, const pxd_sf_params* sf, const pxd_score_lists* r
     free(rec_buf);
     return status;
 }
+
+/* The random start of walker `walker` alone (searcher.cpp:46-87): the pose randomize()
+ * returns for the generator mt19937(seed + walker). */
+void po_mc_randomize(po_system* s, const pxd_sf_params* sf, const double* lo, const double* hi,
+                     uint32_t seed, int walker, const double* start, int first_pose, double* out) {
+    mc_env e = {s, sf, NULL, NULL, s->rec.t.charge, s->rec.t.sigma, s->rec.t.epsilon};
+    po_rng rg;
+    po_rng_seed(&rg, seed + (uint32_t)walker);
+    mc_randomize(&e, start, first_pose, lo, hi, &rg, out);
+}

@@ -82,6 +82,8 @@ int po_mc_walker(po_system* s, const pxd_sf_params* sf, const pxd_score_lists* r
                  int walker, const double* start, int first_pose, int max_nsteps,
                  int relax_nsteps, double threshold, double* global_min, double* out_xyz,
                  double* out_tors, double* out_energy, double* out_pscore, long* out_nevals);
+void po_mc_randomize(po_system* s, const pxd_sf_params* sf, const double* lo, const double* hi,
+                     uint32_t seed, int walker, const double* start, int first_pose, double* out);
 
 /* ---- mt19937 + libstdc++ distributions as random_generator uses them
  *      (engine/include/bytedock/lib/random.h:33-63, engine/src/lib/random.cpp) ---- */

@@ -36,7 +36,8 @@ int cuda_check(pxd_context* ctx, cudaError_t e, const char* what) {
 int ensure_scratch(pxd_context* ctx, size_t bytes) {
     if (bytes <= ctx->scratch_bytes) return PXD_OK;
     if (ctx->scratch) {
-        cudaStreamSynchronize(ctx->stream);
+        // a launch on any stream may still read the old slab
+        cudaDeviceSynchronize();
         cudaFree(ctx->scratch);
         ctx->scratch = nullptr;
         ctx->scratch_bytes = 0;
@@ -748,24 +749,29 @@ int pxd_grid_build(pxd_context* ctx, const pxd_box* box, const int32_t* types, i
     rc = alloc_maps(ctx, box, tl);
     if (rc) return rc;
     // non-rotor receptor atoms (grid.cpp:119-123, 173)
-    std::vector<float4> xq;
+    std::vector<float4> xq, xl;
     std::vector<float2> se;
     for (int a = 0; a < ctx->n_rec; ++a) {
         if (ctx->is_mov[a]) continue;
-        xq.push_back(make_float4(static_cast<float>(ctx->rec_xyz[3 * a]), static_cast<float>(ctx->rec_xyz[3 * a + 1]),
-                                 static_cast<float>(ctx->rec_xyz[3 * a + 2]), static_cast<float>(ctx->rec_charge[a])));
+        const double* x = &ctx->rec_xyz[3 * a];
+        const float4 hi = make_float4(static_cast<float>(x[0]), static_cast<float>(x[1]), static_cast<float>(x[2]),
+                                      static_cast<float>(ctx->rec_charge[a]));
+        xq.push_back(hi);
+        xl.push_back(make_float4(static_cast<float>(x[0] - hi.x), static_cast<float>(x[1] - hi.y),
+                                 static_cast<float>(x[2] - hi.z), 0.f));
         se.push_back(make_float2(static_cast<float>(ctx->rec_sigma[a]), static_cast<float>(ctx->rec_epsilon[a])));
     }
     std::vector<int> slot_type(ctx->n_slots, -1);
     for (size_t k = 0; k < tl.size(); ++k) slot_type[1 + k] = tl[k];
     Packer pk;
-    const size_t o_xq = pk.put(xq), o_se = pk.put(se), o_st = pk.put(slot_type);
+    const size_t o_xq = pk.put(xq), o_xl = pk.put(xl), o_se = pk.put(se), o_st = pk.put(slot_type);
     void* mem = nullptr;
     rc = cuda_check(ctx, cudaMalloc(&mem, pk.bytes.size()), "grid atom upload");
     if (rc) return rc;
     rc = cuda_check(ctx, cudaMemcpy(mem, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice), "grid atom copy");
     if (!rc)
-        rc = launch_grid_build(ctx, at<float4>(mem, o_xq), at<float2>(mem, o_se), static_cast<int>(xq.size()),
+        rc = launch_grid_build(ctx, at<float4>(mem, o_xq), at<float4>(mem, o_xl), at<float2>(mem, o_se),
+                               static_cast<int>(xq.size()),
                                at<int>(mem, o_st), ctx->n_slots, ctx->maps);
     cudaFree(mem);
     if (rc) {
@@ -917,7 +923,15 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
         for (int k = 0; k < tr.n_torsions; ++k)
             tors.push_back(make_int4(tr.tors_frag[k], tr.tors_parent[k], tr.tors_parent_atom[k], tr.tors_mine_atom[k]));
     }
+    std::vector<int> frag_of(N, 0), frag_mine(tr.n_frags, -1), frag_parent(tr.n_frags, -1);
+    for (int f = 0; f < tr.n_frags; ++f)
+        for (int p = tr.frag_start[f]; p < tr.frag_end[f]; ++p) frag_of[p] = f;
+    for (int k = 0; k < tr.n_torsions; ++k) {
+        frag_mine[tr.tors_frag[k]] = tr.tors_mine_atom[k];
+        frag_parent[tr.tors_frag[k]] = tr.tors_parent[k];
+    }
     const size_t o_perm = pk.put(perm), o_fr = pk.put(frange), o_tors = pk.put(tors), o_root = pk.put(isroot);
+    const size_t o_fof = pk.put(frag_of), o_fmine = pk.put(frag_mine), o_fpar = pk.put(frag_parent);
     LigandEntry e;
     int rc = cuda_check(ctx, cudaMalloc(&e.mem, pk.bytes.size()), "ligand allocation");
     if (rc) return rc;
@@ -942,6 +956,9 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
     d.frag_range = at<int>(e.mem, o_fr);
     d.tors = at<int4>(e.mem, o_tors);
     d.is_root = at<int>(e.mem, o_root);
+    d.frag_of = at<int>(e.mem, o_fof);
+    d.frag_mine = at<int>(e.mem, o_fmine);
+    d.frag_parent = at<int>(e.mem, o_fpar);
     e.charge.assign(lig->ff.charge, lig->ff.charge + N);
     rc = upload_ligand_scoring(ctx, e, lig->lists);
     if (rc) {

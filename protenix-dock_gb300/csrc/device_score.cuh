@@ -94,7 +94,7 @@ __device__ __forceinline__ float signed_dihedral(float3 pi, float3 pj, float3 pk
 // Score of the pose in X (ligand, smem) with receptor rotor atoms in loc_xyz (smem).
 // Returns sum(coef * term) over the active terms except GB/SA; when `terms` is given,
 // lane 0 stores the unweighted values.
-__device__ double score_pose(const ScoreEnv& env, const DevLigand& L, const DevLigScore& ls,
+static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, const DevLigScore& ls,
                              const float4* X, const float4* loc_xyz, int lane, double* terms) {
     const DevRecScore& rs = env.rs;
     const DevSf& sf = *env.sf;

@@ -5,6 +5,9 @@
 // of one map, so all its threads read the same receptor-atom tile from shared memory
 // (broadcast). Pair terms are FP32; each 256-atom tile's partial sums are folded into
 // FP64 accumulators, which keeps the Coulomb sum over ~2k atoms of mixed sign accurate.
+// Atom and point coordinates travel as FP32 hi + lo pairs, so each difference
+// atom - point is formed to FP32 relative precision: a plain FP32 coordinate carries
+// ~1e-6 A of rounding, which the 12th power of the LJ term would amplify 12-fold.
 // The squared distance is floored at 1e-4 A^2 so that a grid point sitting on an atom
 // cannot overflow FP32, and records are clamped to +-1e30 before the FP32 store.
 #include "device_eval.cuh"
@@ -18,7 +21,8 @@ constexpr float kR2Floor = 1e-4f;
 constexpr double kRecordCeil = 1e30;
 
 struct GridArgs {
-    const float4* atoms;   // x, y, z, charge of every non-rotor receptor atom
+    const float4* atoms;   // x, y, z, charge of every non-rotor receptor atom (FP32 hi part)
+    const float4* atoms_lo;// x, y, z residuals: coordinate - hi, in FP32
     const float2* se;      // sigma, epsilon
     int n_atoms;
     int3 npts;
@@ -36,6 +40,7 @@ __device__ __forceinline__ float clampf_rec(double v) {
 
 __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs a) {
     __shared__ float4 s_xyzq[kGridTile];
+    __shared__ float4 s_lo[kGridTile];
     __shared__ float2 s_se[kGridTile];
     const int p = blockIdx.x * kGridThreads + threadIdx.x;
     const int slot = blockIdx.y;
@@ -47,15 +52,17 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
     const int j = (p / nz) % ny;
     const int i = p / (nz * ny);
     // grid.cpp:159-163: point = init + spacing * index, formed in FP64
-    const float3 pt = make_float3(static_cast<float>(a.init.x + a.spacing * i),
-                                  static_cast<float>(a.init.y + a.spacing * j),
-                                  static_cast<float>(a.init.z + a.spacing * k));
+    const double px = a.init.x + a.spacing * i, py = a.init.y + a.spacing * j, pz = a.init.z + a.spacing * k;
+    const float3 pt = make_float3(static_cast<float>(px), static_cast<float>(py), static_cast<float>(pz));
+    const float3 pl = make_float3(static_cast<float>(px - pt.x), static_cast<float>(py - pt.y),
+                                  static_cast<float>(pz - pt.z));
     double E = 0.0, GX = 0.0, GY = 0.0, GZ = 0.0;
     for (int t0 = 0; t0 < a.n_atoms; t0 += kGridTile) {
         const int n = min(kGridTile, a.n_atoms - t0);
         __syncthreads();
         for (int u = threadIdx.x; u < n; u += kGridThreads) {
             s_xyzq[u] = a.atoms[t0 + u];
+            s_lo[u] = a.atoms_lo[t0 + u];
             s_se[u] = a.se[t0 + u];
         }
         __syncthreads();
@@ -63,7 +70,9 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
         if (coul) {
             for (int u = 0; u < n; ++u) {
                 const float4 at = s_xyzq[u];
-                const float vx = at.x - pt.x, vy = at.y - pt.y, vz = at.z - pt.z;
+                const float4 lo = s_lo[u];
+                const float vx = (at.x - pt.x) + (lo.x - pl.x), vy = (at.y - pt.y) + (lo.y - pl.y),
+                            vz = (at.z - pt.z) + (lo.z - pl.z);
                 const float r2 = fmaxf(vx * vx + vy * vy + vz * vz, kR2Floor);
                 const float rinv = rsqrtf(r2);
                 const float qr = at.w * rinv;
@@ -81,8 +90,10 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
         } else {
             for (int u = 0; u < n; ++u) {
                 const float4 at = s_xyzq[u];
+                const float4 lo = s_lo[u];
                 const float2 se = s_se[u];
-                const float vx = at.x - pt.x, vy = at.y - pt.y, vz = at.z - pt.z;
+                const float vx = (at.x - pt.x) + (lo.x - pl.x), vy = (at.y - pt.y) + (lo.y - pl.y),
+                            vz = (at.z - pt.z) + (lo.z - pl.z);
                 const float r2 = fmaxf(vx * vx + vy * vy + vz * vz, kR2Floor);
                 const float rinv2 = 1.f / r2;
                 const float s = (tse.x + se.x) * 0.5f;
@@ -109,10 +120,11 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
     }
 }
 
-int launch_grid_build(pxd_context* ctx, const float4* atoms, const float2* se, int n_atoms,
-                      const int* slot_type, int n_slots, float4* maps) {
+int launch_grid_build(pxd_context* ctx, const float4* atoms, const float4* atoms_lo, const float2* se,
+                      int n_atoms, const int* slot_type, int n_slots, float4* maps) {
     GridArgs a;
     a.atoms = atoms;
+    a.atoms_lo = atoms_lo;
     a.se = se;
     a.n_atoms = n_atoms;
     a.npts = make_int3(ctx->box.npoints[0], ctx->box.npoints[1], ctx->box.npoints[2]);

@@ -1,20 +1,8 @@
-// Persistent batched L-BFGS + strong-Wolfe kernel (one warp per pose) and the
-// score+gradient kernel.
-//
-// Control flow restates lbfgs_step::apply and strong_wolfe (optimizer.cpp:205-560)
-// with the caller's constants; pose vectors live in the warp's shared-memory slice,
-// the m-deep history in a per-warp global scratch slab. All scalars that steer the
-// iteration (f, t, gtd, Wolfe tests, H_diag, ro, alpha) are FP64 and identical on all
-// 32 lanes, so the warp never diverges on control flow. Every loop is bounded by
-// max_iter, max_eval or ls_max.
-#include "device_eval.cuh"
+// Persistent batched L-BFGS kernel (one warp per pose, dynamic pose queue) and the
+// score+gradient kernel, with their launchers.
+#include "device_lbfgs.cuh"
 
 namespace pxd {
-
-struct LbfgsConsts {
-    int max_iter, max_eval, m, ls_max;
-    double lr, tol_grad, tol_change, c1, c2, ls_tol_change, gtd_threshold, reset;
-};
 
 struct LbfgsArgs {
     EvalEnv env;
@@ -35,287 +23,6 @@ struct LbfgsArgs {
     float* hist;       // per warp: S [m][D_pad], Y [m][D_pad]
     size_t hist_stride;
 };
-
-struct Vecs {
-    float *x, *g, *gp, *d, *q, *sv, *gnew, *gprev, *bg0, *bg1;
-    float *S, *Y;
-    double *ro, *al;
-};
-
-struct Closure {
-    const EvalEnv* env;
-    const DevLigand* L;
-    const PoseBufs* b;
-    const float* x0;
-    int lane;
-    int nevals;
-};
-
-__device__ __forceinline__ double closure_eval(Closure& c, double t, const float* d, float* g) {
-    ++c.nevals;
-    return eval_pose(*c.env, *c.L, c.x0, d, static_cast<float>(t), g, *c.b, c.lane);
-}
-
-__device__ __forceinline__ double cubic_interpolate(double x1, double f1, double g1, double x2,
-                                                    double f2, double g2, double lo, double hi) {
-    double d1 = g1 + g2 - 3.0 * (f1 - f2) / (x1 - x2);
-    const double d2sq = d1 * d1 - g1 * g2;
-    if (d2sq >= 0.0) {
-        const double d2 = sqrt(d2sq);
-        if (x1 <= x2)
-            d1 = x2 - (x2 - x1) * ((g2 + d2 - d1) / (g2 - g1 + 2.0 * d2));
-        else
-            d1 = x1 - (x1 - x2) * ((g1 + d2 - d1) / (g1 - g2 + 2.0 * d2));
-        return fmin(fmax(d1, lo), hi);
-    }
-    return (lo + hi) / 2.0;
-}
-
-// strong_wolfe (optimizer.cpp:235-427); g holds the current gradient on entry and the
-// accepted one on exit.
-__device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_io, const float* d,
-                             double& f_io, float* g, double gtd, const Vecs& v, int D,
-                             int lane) {
-    double t = t_io;
-    const double f = f_io;
-    float* g_new = v.gnew;
-    float* g_prev = v.gprev;
-    float* bg[2] = {v.bg0, v.bg1};
-    double br[2] = {0.0, 0.0}, bf[2] = {0.0, 0.0}, bgtd[2] = {0.0, 0.0};
-    double f_new = closure_eval(c, t, d, g_new);
-    if (isnan(f_new)) {
-        f_io = f_new;
-        return;
-    }
-    double gtd_new = vdot(g_new, d, D, lane);
-    if (fabs(gtd_new) > p.gtd_threshold) {
-        f_io = f_new;
-        vcopy(g, g_new, D, lane);
-        return;
-    }
-    double t_prev = 0.0, f_prev = f, gtd_prev = gtd;
-    vcopy(g_prev, g, D, lane);
-    bool done = false;
-    int ls_iter = 0;
-    while (ls_iter < p.ls_max) {
-        if ((f_new > f + p.c1 * t * gtd) || (ls_iter > 1 && f_new >= f_prev)) {
-            br[0] = t_prev; br[1] = t; bf[0] = f_prev; bf[1] = f_new;
-            vcopy(bg[0], g_prev, D, lane);
-            vcopy(bg[1], g_new, D, lane);
-            bgtd[0] = gtd_prev; bgtd[1] = gtd_new;
-            break;
-        }
-        if (fabs(gtd_new) <= -p.c2 * gtd) {
-            br[0] = t; bf[0] = f_new;
-            vcopy(bg[0], g_new, D, lane);
-            done = true;
-            break;
-        }
-        if (gtd_new >= 0.0) {
-            br[0] = t_prev; br[1] = t; bf[0] = f_prev; bf[1] = f_new;
-            vcopy(bg[0], g_prev, D, lane);
-            vcopy(bg[1], g_new, D, lane);
-            bgtd[0] = gtd_prev; bgtd[1] = gtd_new;
-            break;
-        }
-        const double min_step = t + 0.01 * (t - t_prev);
-        const double max_step = t * 10.0;
-        const double tmp = t;
-        t = cubic_interpolate(t_prev, f_prev, gtd_prev, t, f_new, gtd_new, min_step, max_step);
-        t_prev = tmp;
-        f_prev = f_new;
-        vcopy(g_prev, g_new, D, lane);
-        gtd_prev = gtd_new;
-        f_new = closure_eval(c, t, d, g_new);
-        gtd_new = vdot(g_new, d, D, lane);
-        ++ls_iter;
-    }
-    double d_norm = 0.0;
-    if (ls_iter == p.ls_max) {
-        br[0] = 0.0; br[1] = t; bf[0] = f; bf[1] = f_new;
-        vcopy(bg[0], g, D, lane);
-        vcopy(bg[1], g_new, D, lane);
-    } else {
-        d_norm = vabsmax(d, D, lane);
-    }
-    bool insuf = false;
-    int lo = 0, hi = 1;
-    if (!done && bf[0] > bf[1]) {
-        lo = 1;
-        hi = 0;
-    }
-    while (!done && ls_iter < p.ls_max) {
-        double min_step, max_step;
-        if (br[0] > br[1]) {
-            min_step = br[1];
-            max_step = br[0];
-        } else {
-            min_step = br[0];
-            max_step = br[1];
-        }
-        double eps = max_step - min_step;
-        if (eps * d_norm < p.ls_tol_change) break;
-        t = cubic_interpolate(br[0], bf[0], bgtd[0], br[1], bf[1], bgtd[1], min_step, max_step);
-        eps *= 0.1;
-        if (fmin(max_step - t, t - min_step) < eps) {
-            if (insuf || t >= max_step || t <= min_step) {
-                if (fabs(t - max_step) < fabs(t - min_step))
-                    t = max_step - eps;
-                else
-                    t = min_step + eps;
-                insuf = false;
-            } else {
-                insuf = true;
-            }
-        } else {
-            insuf = false;
-        }
-        f_new = closure_eval(c, t, d, g_new);
-        gtd_new = vdot(g_new, d, D, lane);
-        ++ls_iter;
-        if (f_new > (f + p.c1 * t * gtd) || f_new >= bf[lo]) {
-            br[hi] = t;
-            bf[hi] = f_new;
-            vcopy(bg[hi], g_new, D, lane);
-            bgtd[hi] = gtd_new;
-            if (bf[0] > bf[1]) {
-                lo = 1;
-                hi = 0;
-            } else {
-                lo = 0;
-                hi = 1;
-            }
-        } else {
-            if (fabs(gtd_new) <= -p.c2 * gtd) {
-                done = true;
-            } else if (gtd_new * (br[hi] - br[lo]) >= 0.0) {
-                br[hi] = br[lo];
-                bf[hi] = bf[lo];
-                vcopy(bg[hi], bg[lo], D, lane);
-                bgtd[hi] = bgtd[lo];
-            }
-            br[lo] = t;
-            bf[lo] = f_new;
-            vcopy(bg[lo], g_new, D, lane);
-            bgtd[lo] = gtd_new;
-        }
-    }
-    t_io = br[lo];
-    f_io = bf[lo];
-    vcopy(g, bg[lo], D, lane);
-}
-
-// lbfgs_step::apply (optimizer.cpp:429-560) on the pose held in v.x; returns status.
-__device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v, int D,
-                          size_t Dp, int lane, double& energy) {
-    const int m = p.m;
-    const int max_eval = p.max_eval > 0 ? p.max_eval : p.max_iter * 5 / 4;
-    c.x0 = v.x;
-    c.nevals = 0;
-    double loss = closure_eval(c, 0.0, nullptr, v.g);
-    energy = loss;
-    if (vabsmax(v.g, D, lane) < p.tol_grad) return PXD_POSE_CONVERGED;
-    int status = PXD_POSE_NOT_CONVERGED;
-    int head = 0, count = 0;
-    double H_diag = 1.0, t = 0.0, prev_loss;
-    int n_iter = 0;
-    bool updated = false, high = false;
-    while (n_iter < p.max_iter && c.nevals < max_eval) {
-        ++n_iter;
-        if (n_iter > 1) {
-            for (int e = lane; e < D; e += kWarp) v.q[e] = v.g[e] - v.gp[e];  // y
-            __syncwarp();
-            high = vabsmax(v.q, D, lane) > p.reset;
-        }
-        if (n_iter == 1 || high) {
-            for (int e = lane; e < D; e += kWarp) v.d[e] = -v.g[e];
-            __syncwarp();
-            head = count = 0;
-            H_diag = 1.0;
-        } else {
-            const float tf = static_cast<float>(t);
-            for (int e = lane; e < D; e += kWarp) v.sv[e] = v.d[e] * tf;
-            __syncwarp();
-            const double ys = vdot(v.q, v.sv, D, lane);
-            if (ys > 1e-10) {
-                int slot;
-                if (count == m) {
-                    slot = head;
-                    head = (head + 1) % m;
-                } else {
-                    slot = (head + count) % m;
-                    ++count;
-                }
-                H_diag = ys / vdot(v.q, v.q, D, lane);
-                vcopy(v.Y + slot * Dp, v.q, D, lane);
-                vcopy(v.S + slot * Dp, v.sv, D, lane);
-                if (lane == 0) v.ro[slot] = 1.0 / ys;
-                __syncwarp();
-            }
-            for (int e = lane; e < D; e += kWarp) v.q[e] = -v.g[e];
-            __syncwarp();
-            for (int k = count - 1; k > -1; --k) {
-                const int slot = (head + k) % m;
-                const double al = vdot(v.S + slot * Dp, v.q, D, lane) * v.ro[slot];
-                if (lane == 0) v.al[k] = al;
-                const float nal = static_cast<float>(-al);
-                const float* yy = v.Y + slot * Dp;
-                for (int e = lane; e < D; e += kWarp) v.q[e] = fmaf(yy[e], nal, v.q[e]);
-                __syncwarp();
-            }
-            const float hd = static_cast<float>(H_diag);
-            for (int e = lane; e < D; e += kWarp) v.d[e] = v.q[e] * hd;
-            __syncwarp();
-            for (int k = 0; k < count; ++k) {
-                const int slot = (head + k) % m;
-                const double be = vdot(v.Y + slot * Dp, v.d, D, lane) * v.ro[slot];
-                const float w = static_cast<float>(v.al[k] - be);
-                const float* ss = v.S + slot * Dp;
-                for (int e = lane; e < D; e += kWarp) v.d[e] = fmaf(ss[e], w, v.d[e]);
-                __syncwarp();
-            }
-        }
-        vcopy(v.gp, v.g, D, lane);
-        prev_loss = loss;
-        if (n_iter == 1 || high) {
-            const double inv = 1.0 / vabssum(v.g, D, lane);
-            t = fmin(1.0, inv) * p.lr * 0.1;
-        } else {
-            t = p.lr;
-        }
-        const double gtd = vdot(v.g, v.d, D, lane);
-        if (gtd > -p.tol_change) {
-            status = PXD_POSE_CONVERGED;
-            break;
-        }
-        Vecs w = v;
-        strong_wolfe(c, p, t, v.d, loss, v.g, gtd, w, D, lane);
-        if (isnan(loss)) {
-            status = PXD_POSE_NAN;
-            break;
-        }
-        const float tf = static_cast<float>(t);
-        for (int e = lane; e < D; e += kWarp) v.x[e] = fmaf(v.d[e], tf, v.x[e]);
-        __syncwarp();
-        updated = true;
-        if (vabsmax(v.g, D, lane) <= p.tol_grad) {
-            status = PXD_POSE_CONVERGED;
-            break;
-        }
-        float smax = 0.f;
-        for (int e = lane; e < D; e += kWarp) smax = fmaxf(smax, fabsf(v.d[e] * tf));
-        if (warp_max(smax) <= p.tol_change) {
-            status = PXD_POSE_CONVERGED;
-            break;
-        }
-        if (fabs(loss - prev_loss) < p.tol_change) {
-            status = PXD_POSE_CONVERGED;
-            break;
-        }
-    }
-    if (updated) energy = closure_eval(c, 0.0, nullptr, v.gnew);
-    return status;
-}
 
 constexpr int kWarpsPerBlock = 4;
 

@@ -101,6 +101,9 @@ struct DevLigand {
     const int* frag_range;    // [2*F]
     const int4* tors;         // [T] frag, parent frag, parent atom, mine atom (positions)
     const int* is_root;       // [F]
+    const int* frag_of;       // [N] fragment of each permuted position
+    const int* frag_mine;     // [F] bond atom of the fragment (-1 for roots)
+    const int* frag_parent;   // [F] parent fragment (-1 for roots)
 };
 
 struct DevReceptor {
@@ -198,8 +201,9 @@ int sync_ligand_table(pxd_context* ctx);
 int refresh_ligand_slots(pxd_context* ctx);
 
 // kernels (launchers), one per translation unit
-int launch_grid_build(pxd_context* ctx, const float4* atoms_xyzq, const float2* atoms_se,
-                      int n_atoms, const int* slot_types, int n_slots, float4* maps);
+int launch_grid_build(pxd_context* ctx, const float4* atoms_xyzq, const float4* atoms_lo,
+                      const float2* atoms_se, int n_atoms, const int* slot_types, int n_slots,
+                      float4* maps);
 int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_ids,
                  const float* xyz, const float* tors, double* energy, float* lig_grad,
                  float* tors_grad, cudaStream_t s);

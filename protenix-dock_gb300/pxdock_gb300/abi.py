@@ -129,6 +129,23 @@ class LbfgsParams(C.Structure):
     ]
 
 
+class McParams(C.Structure):
+    """pxd_mc_params (monte_carlo_searcher, searcher.h:29-41; search() arguments)."""
+
+    _fields_ = [
+        ("seed", C.c_uint32),
+        ("max_nsteps", C.c_int32),
+        ("relax_nsteps", C.c_int32),
+        ("full_nsteps", C.c_int32),
+        ("mc_mmenergy_threshold", C.c_double),
+        ("amplitude", C.c_double),
+        ("temperature", C.c_double),
+        ("box_lo", C.c_double * 3),
+        ("box_hi", C.c_double * 3),
+        ("lbfgs", LbfgsParams),
+    ]
+
+
 def lbfgs_params(max_iter=240, max_eval=0, history=100, tolerance_grad=0.5,
                  tolerance_change=1e-4, lr=1.0):
     """Reference constants by default (lbfgs_step, optimizer.h:50-67)."""

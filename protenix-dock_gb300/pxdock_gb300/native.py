@@ -66,6 +66,12 @@ def load(auto_build=False):
     lib.pxd_score.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, abi.f64p, abi.f64p, abi.f64p,
                               abi.f64p]
     lib.pxd_score_gbsa.argtypes = [vp, C.c_int32, abi.f64p, abi.f64p, abi.f64p, abi.f64p]
+    lib.pxd_mc_defaults.argtypes = [C.POINTER(abi.McParams)]
+    lib.pxd_mc_search_dev.argtypes = [vp, C.POINTER(abi.McParams), C.c_int32, C.c_int32] + [vp] * 12
+    lib.pxd_mc_search.argtypes = [vp, C.POINTER(abi.McParams), C.c_int32, C.c_int32, abi.i32p,
+                                  abi.i32p, abi.f64p, abi.f64p, abi.f64p, abi.f64p, abi.f64p,
+                                  abi.i32p, abi.i32p]
+    lib.pxd_rng_draws.argtypes = [vp, C.c_uint32, C.c_int32, abi.i32p, abi.i32p, abi.f64p]
     _lib = lib
     return lib
 
@@ -234,6 +240,43 @@ class Context:
                                             _p(d), _p(parts)))
         return d[0], parts
 
+    def mc_search(self, params, lig, starts, walker_ids, first_pose=None):
+        """Monte-Carlo walkers of one ligand: starts [W][N][3] (the pose each walker starts
+        from), walker_ids [W] (seed offsets; walker 0 only relaxes)."""
+        N = self.ligands[lig].n_atoms
+        starts = _f64(starts).reshape(-1, N, 3)
+        W = starts.shape[0]
+        wid = np.ascontiguousarray(np.asarray(walker_ids, np.int32).reshape(W))
+        fp = np.ascontiguousarray(np.ones(W, np.int32) if first_pose is None
+                                  else np.asarray(first_pose, np.int32).reshape(W))
+        out = np.zeros((W, N, 3))
+        tors = np.zeros((W, max(self.n_rotors, 1)))
+        e, ps = np.zeros(W), np.zeros(W)
+        nev, st = np.zeros(W, np.int32), np.zeros(W, np.int32)
+        self._check(self.lib.pxd_mc_search(self.h, C.byref(params), lig, W, _p(wid, C.c_int32),
+                                           _p(fp, C.c_int32), _p(starts), _p(out), _p(tors), _p(e),
+                                           _p(ps), _p(nev, C.c_int32), _p(st, C.c_int32)))
+        return dict(xyz=out, torsions=tors[:, : self.n_rotors], energy=e, pscore=ps, nevals=nev,
+                    status=st)
+
+    def mc_search_dev(self, params, n_walkers, max_atoms, ids_ptr, walker_ptr, first_ptr, start_ptr,
+                      out_xyz_ptr, out_tors_ptr, energy_ptr, pscore_ptr, nevals_ptr, status_ptr,
+                      global_min_ptr=None, stream=None):
+        self._check(self.lib.pxd_mc_search_dev(self.h, C.byref(params), n_walkers, max_atoms, ids_ptr,
+                                               walker_ptr, first_ptr, start_ptr, out_xyz_ptr,
+                                               out_tors_ptr, energy_ptr, pscore_ptr, nevals_ptr,
+                                               status_ptr, global_min_ptr, stream))
+
+    def rng_draws(self, seed, kinds, ints):
+        """Values of the device walker generator (see pxd_rng_draws)."""
+        kinds = np.ascontiguousarray(np.asarray(kinds, np.int32))
+        ints = np.ascontiguousarray(np.asarray(ints, np.int32))
+        width = {3: 3, 4: 4}
+        out = np.zeros(sum(width.get(int(k), 1) for k in kinds) or 1)
+        self._check(self.lib.pxd_rng_draws(self.h, seed, len(kinds), _p(kinds, C.c_int32),
+                                           _p(ints, C.c_int32), _p(out)))
+        return out[: sum(width.get(int(k), 1) for k in kinds)]
+
     def receptor_kinematics(self, torsions):
         t = _f64(torsions).reshape(-1, self.n_rotors)
         n = t.shape[0]
@@ -249,4 +292,21 @@ def lbfgs_params(**kw):
     load().pxd_lbfgs_defaults(C.byref(p))
     for k, v in kw.items():
         setattr(p, k, v)
+    return p
+
+
+def mc_params(box_lo, box_hi, **kw):
+    """pxd_mc_params with the reference defaults (pxd_mc_defaults) and the search box;
+    keyword arguments override fields, lbfgs=dict(...) the optimiser constants."""
+    p = abi.McParams()
+    load().pxd_mc_defaults(C.byref(p))
+    for d in range(3):
+        p.box_lo[d] = float(box_lo[d])
+        p.box_hi[d] = float(box_hi[d])
+    for k, v in kw.items():
+        if k == "lbfgs":
+            for kk, vv in v.items():
+                setattr(p.lbfgs, kk, vv)
+        else:
+            setattr(p, k, v)
     return p
