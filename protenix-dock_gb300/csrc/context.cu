@@ -758,7 +758,7 @@ int pxd_grid_build(pxd_context* ctx, const pxd_box* box, const int32_t* types, i
                                       static_cast<float>(ctx->rec_charge[a]));
         xq.push_back(hi);
         xl.push_back(make_float4(static_cast<float>(x[0] - hi.x), static_cast<float>(x[1] - hi.y),
-                                 static_cast<float>(x[2] - hi.z), 0.f));
+                                 static_cast<float>(x[2] - hi.z), static_cast<float>(ctx->rec_charge[a] - hi.w)));
         se.push_back(make_float2(static_cast<float>(ctx->rec_sigma[a]), static_cast<float>(ctx->rec_epsilon[a])));
     }
     std::vector<int> slot_type(ctx->n_slots, -1);

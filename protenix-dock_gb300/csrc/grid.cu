@@ -8,6 +8,7 @@
 // Atom and point coordinates travel as FP32 hi + lo pairs, so each difference
 // atom - point is formed to FP32 relative precision: a plain FP32 coordinate carries
 // ~1e-6 A of rounding, which the 12th power of the LJ term would amplify 12-fold.
+// The Coulomb map is summed in FP64 (see the loop).
 // The squared distance is floored at 1e-4 A^2 so that a grid point sitting on an atom
 // cannot overflow FP32, and records are clamped to +-1e30 before the FP32 store.
 #include "device_eval.cuh"
@@ -19,10 +20,11 @@ constexpr int kGridThreads = 128;
 constexpr int kGridTile = 256;
 constexpr float kR2Floor = 1e-4f;
 constexpr double kRecordCeil = 1e30;
+constexpr double kCoulombD = 332.0637141491396;  // kCoulombFactor, system.h:83
 
 struct GridArgs {
     const float4* atoms;   // x, y, z, charge of every non-rotor receptor atom (FP32 hi part)
-    const float4* atoms_lo;// x, y, z residuals: coordinate - hi, in FP32
+    const float4* atoms_lo;// x, y, z, charge residuals: value - hi, in FP32
     const float2* se;      // sigma, epsilon
     int n_atoms;
     int3 npts;
@@ -68,25 +70,30 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
         __syncthreads();
         float e = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
         if (coul) {
+            // FP64 per pair: the map is a sum of ~M terms q/r of both signs that cancel
+            // to a small fraction of their magnitudes, so FP32 rounding of each term
+            // (~1e-7 relative) would leave ~1e-3 kcal/mol in the records
+            double ce = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
             for (int u = 0; u < n; ++u) {
                 const float4 at = s_xyzq[u];
                 const float4 lo = s_lo[u];
-                const float vx = (at.x - pt.x) + (lo.x - pl.x), vy = (at.y - pt.y) + (lo.y - pl.y),
-                            vz = (at.z - pt.z) + (lo.z - pl.z);
-                const float r2 = fmaxf(vx * vx + vy * vy + vz * vz, kR2Floor);
-                const float rinv = rsqrtf(r2);
-                const float qr = at.w * rinv;
-                e += qr;
+                const double vx = (static_cast<double>(at.x) - px) + static_cast<double>(lo.x);
+                const double vy = (static_cast<double>(at.y) - py) + static_cast<double>(lo.y);
+                const double vz = (static_cast<double>(at.z) - pz) + static_cast<double>(lo.z);
+                const double r2 = fmax(vx * vx + vy * vy + vz * vz, static_cast<double>(kR2Floor));
+                const double rinv = rsqrt(r2);
+                const double qr = (static_cast<double>(at.w) + static_cast<double>(lo.w)) * rinv;
+                ce += qr;
                 // dE/dpoint = q (atom - point) / r^3 (pair.h:25-40 with grad_i -= ...)
-                const float w = qr * rinv * rinv;
-                gx = fmaf(vx, w, gx);
-                gy = fmaf(vy, w, gy);
-                gz = fmaf(vz, w, gz);
+                const double w = qr * rinv * rinv;
+                cx = fma(vx, w, cx);
+                cy = fma(vy, w, cy);
+                cz = fma(vz, w, cz);
             }
-            E += static_cast<double>(e) * kCoulombF;
-            GX += static_cast<double>(gx) * kCoulombF;
-            GY += static_cast<double>(gy) * kCoulombF;
-            GZ += static_cast<double>(gz) * kCoulombF;
+            E += ce * kCoulombD;
+            GX += cx * kCoulombD;
+            GY += cy * kCoulombD;
+            GZ += cz * kCoulombD;
         } else {
             for (int u = 0; u < n; ++u) {
                 const float4 at = s_xyzq[u];
