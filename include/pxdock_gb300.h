@@ -309,6 +309,20 @@ int pxd_lbfgs_dev(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t n_po
                   float* rec_tors_dev, double* energy_dev, int32_t* nevals_dev,
                   int32_t* status_dev, void* stream);
 
+/* pxd_lbfgs_dev without any device allocation (no counterpart in the reference: it
+ * serves callers that must not allocate, e.g. inside a memory-pool budget). The
+ * L-BFGS history and the pose-queue counter live in a 32 MiB file-scope device array;
+ * the persistent grid shrinks to the warps whose history fits, and a request where not
+ * even one block fits is rejected with PXD_ERR_INVALID. The counter is cleared by a
+ * memset on `stream` at every call. Overlapping calls (other streams or threads) share
+ * the array and race. The first call on a device resolves the array's address: make
+ * it before any stream capture. Ligands added since the last launch must fit the
+ * existing device ligand table (else PXD_ERR_STATE: one pxd_lbfgs_dev call grows it). */
+int pxd_lbfgs_dev_noalloc(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t n_poses,
+                          int32_t max_atoms, const int32_t* ligand_ids_dev, float* xyz_dev,
+                          float* receptor_torsions_dev, double* energy_dev, int32_t* nevals_dev,
+                          int32_t* status_dev, void* stream);
+
 /* Host-buffer version for one ligand: copies in, runs, copies out (double). */
 int pxd_lbfgs(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t ligand_id,
               int32_t n_poses, double* lig_xyz, double* rec_tors, double* energy,

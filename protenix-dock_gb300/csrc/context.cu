@@ -1019,6 +1019,20 @@ int pxd_lbfgs_dev(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses, 
     return launch_lbfgs(ctx, *p, n_poses, max_atoms, ids, xyz, tors, energy, nevals, status, pick(ctx, stream));
 }
 
+int pxd_lbfgs_dev_noalloc(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses, int32_t max_atoms,
+                          const int32_t* ids, float* xyz, float* tors, double* energy, int32_t* nevals,
+                          int32_t* status, void* stream) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!p || p->history < 1 || p->history > PXD_MAX_HISTORY || p->max_iter < 0 || p->ls_max < 1)
+        return set_error(ctx, PXD_ERR_INVALID, "bad L-BFGS parameters");
+    if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS)
+        return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");
+    if (ctx->rec.n_rotors > 0 && !tors) return set_error(ctx, PXD_ERR_INVALID, "receptor torsion buffer required");
+    return launch_lbfgs_noalloc(ctx, *p, n_poses, max_atoms, ids, xyz, tors, energy, nevals, status,
+                                pick(ctx, stream));
+}
+
 int pxd_score_grad(pxd_context* ctx, int32_t lig, int32_t n_poses, const double* xyz, const double* tors,
                    double* energy, double* lig_grad, double* tors_grad) {
     int rc = check_ready(ctx);

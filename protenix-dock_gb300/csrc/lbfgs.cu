@@ -1,5 +1,7 @@
 // Persistent batched L-BFGS kernel (one warp per pose, dynamic pose queue) and the
 // score+gradient kernel, with their launchers.
+#include <mutex>
+
 #include "device_lbfgs.cuh"
 
 namespace pxd {
@@ -242,6 +244,108 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     a.hist = static_cast<float*>(ctx->scratch);
     a.counter = ctx->d_counter;
     rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), s), "counter reset");
+    if (rc) return rc;
+    lbfgs_kernel<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
+    return cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
+}
+
+// ------------------------------------------------------- allocation-free variant
+// The same kernel with its per-warp L-BFGS history and its pose-queue counter in a
+// file-scope device array instead of the context's growable slab, so a launch makes
+// no device allocation. The array holds 32 MiB: 256 bytes for the counter, then the
+// history slabs of as many warps as fit; the persistent grid is trimmed to that many
+// warps (at history 8 and 42 atoms: 4,096 warps, more than one launch's ~1,800).
+// The counter must be zero when the kernel starts: each launch clears it with a
+// memset on the caller's stream. Calls that overlap in time (other streams, other
+// threads) share the array and race; the first call on a device resolves the array's
+// address (cudaGetSymbolAddress), so make it before any stream capture.
+constexpr size_t kStaticScratchBytes = size_t(32) << 20;
+constexpr size_t kStaticCounterBytes = 256;
+constexpr int kStaticMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+static std::mutex g_static_mu;
+static unsigned char* g_static_base[kStaticMaxDevices] = {};
+
+static int static_scratch(pxd_context* ctx, unsigned char** out) {
+    if (ctx->device < 0 || ctx->device >= kStaticMaxDevices)
+        return set_error(ctx, PXD_ERR_INVALID, "device ordinal beyond the static scratch table");
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_base[ctx->device]) {
+        void* p = nullptr;
+        int rc = cuda_check(ctx, cudaGetSymbolAddress(&p, g_static_scratch), "static scratch address");
+        if (rc) return rc;
+        g_static_base[ctx->device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_static_base[ctx->device];
+    return PXD_OK;
+}
+
+int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int max_atoms,
+                         const int* lig_ids, float* xyz, float* tors, double* energy, int* nevals,
+                         int* status, cudaStream_t s) {
+    if (n_poses <= 0) return PXD_OK;
+    if (ctx->ligands_dirty && static_cast<int>(ctx->ligands.size()) > ctx->d_ligands_cap)
+        return set_error(ctx, PXD_ERR_STATE,
+                         "the device ligand table must grow, which allocates: make one "
+                         "pxd_lbfgs_dev or pxd_score_grad_dev call after adding ligands");
+    int rc = sync_ligand_table(ctx);  // a copy into the existing table
+    if (rc) return rc;
+    unsigned char* base = nullptr;
+    rc = static_scratch(ctx, &base);
+    if (rc) return rc;
+    LbfgsArgs a;
+    a.env = make_env(ctx);
+    a.ligands = ctx->d_ligands;
+    a.lig_ids = lig_ids;
+    a.n_ligands = static_cast<int>(ctx->ligands.size());
+    a.xyz = xyz;
+    a.tors = tors;
+    a.max_atoms = max_atoms;
+    a.energy = energy;
+    a.nevals = nevals;
+    a.status = status;
+    a.n_poses = n_poses;
+    a.c.max_iter = p.max_iter;
+    a.c.max_eval = p.max_eval;
+    a.c.m = p.history;
+    a.c.ls_max = p.ls_max;
+    a.c.lr = p.lr;
+    a.c.tol_grad = p.tolerance_grad;
+    a.c.tol_change = p.tolerance_change;
+    a.c.c1 = p.ls_c1;
+    a.c.c2 = p.ls_c2;
+    a.c.ls_tol_change = p.ls_tolerance_change;
+    a.c.gtd_threshold = p.ls_gtd_threshold;
+    a.c.reset = p.reset_threshold;
+    a.n_local = ctx->rec.n_local;
+    a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
+    const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + 10 * a.D_pad + 4 * p.history;
+    const size_t smem = sizeof(float) * kWarpsPerBlock * per_warp;
+    rc = cuda_check(ctx, cudaFuncSetAttribute(lbfgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              static_cast<int>(smem)),
+                    "lbfgs smem attribute");
+    if (rc) return rc;
+    int per_sm = 0;
+    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbfgs_kernel,
+                                                                      kWarpsPerBlock * kWarp, smem),
+                    "lbfgs occupancy");
+    if (rc) return rc;
+    if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
+    a.hist_stride = static_cast<size_t>(2) * p.history * a.D_pad;
+    const size_t block_bytes = sizeof(float) * a.hist_stride * kWarpsPerBlock;
+    const size_t fit = (kStaticScratchBytes - kStaticCounterBytes) / block_bytes;
+    if (fit < 1)
+        return set_error(ctx, PXD_ERR_INVALID,
+                         "one block's L-BFGS history (" + std::to_string(block_bytes) +
+                             " bytes) exceeds the 32 MiB static scratch: lower history or max_atoms");
+    int blocks = per_sm * ctx->n_sm;
+    const int need = (n_poses + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (blocks > need) blocks = need;
+    if (static_cast<size_t>(blocks) > fit) blocks = static_cast<int>(fit);
+    a.counter = reinterpret_cast<int*>(base);
+    a.hist = reinterpret_cast<float*>(base + kStaticCounterBytes);
+    rc = cuda_check(ctx, cudaMemsetAsync(a.counter, 0, sizeof(int), s), "counter reset");
     if (rc) return rc;
     lbfgs_kernel<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
     return cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");

@@ -210,6 +210,9 @@ int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_id
 int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int max_atoms,
                  const int* lig_ids, float* xyz, float* tors, double* energy, int* nevals,
                  int* status, cudaStream_t s);
+int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int max_atoms,
+                         const int* lig_ids, float* xyz, float* tors, double* energy, int* nevals,
+                         int* status, cudaStream_t s);
 int launch_ligand_kinematics(pxd_context* ctx, int lig, int n_poses, const float* xyz_in,
                              const float* centers, const float* rots, const float* tors,
                              float* xyz_out, cudaStream_t s);

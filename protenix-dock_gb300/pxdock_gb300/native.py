@@ -56,6 +56,7 @@ def load(auto_build=False):
                                    abi.f64p, abi.f64p]
     lib.pxd_lbfgs_dev.argtypes = [vp, C.POINTER(abi.LbfgsParams), C.c_int32, C.c_int32, vp, vp, vp,
                                   vp, vp, vp, vp]
+    lib.pxd_lbfgs_dev_noalloc.argtypes = lib.pxd_lbfgs_dev.argtypes
     lib.pxd_lbfgs.argtypes = [vp, C.POINTER(abi.LbfgsParams), C.c_int32, C.c_int32, abi.f64p,
                               abi.f64p, abi.f64p, abi.i32p, abi.i32p]
     lib.pxd_ligand_kinematics.argtypes = [vp, C.c_int32, C.c_int32, abi.f64p, abi.f64p, abi.f64p,
@@ -201,6 +202,13 @@ class Context:
         self._check(self.lib.pxd_lbfgs_dev(self.h, C.byref(params), n_poses, max_atoms, ids_ptr,
                                            xyz_ptr, tors_ptr, energy_ptr, nevals_ptr, status_ptr,
                                            stream))
+
+    def lbfgs_dev_noalloc(self, params, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
+                          nevals_ptr, status_ptr, stream=None):
+        """pxd_lbfgs_dev_noalloc: the batched optimiser without device allocations."""
+        self._check(self.lib.pxd_lbfgs_dev_noalloc(self.h, C.byref(params), n_poses, max_atoms, ids_ptr,
+                                                   xyz_ptr, tors_ptr, energy_ptr, nevals_ptr,
+                                                   status_ptr, stream))
 
     def ligand_kinematics(self, lig, xyz, centers, rots, torsions):
         centers = _f64(centers).reshape(-1, 3)
