@@ -328,6 +328,13 @@ int pxd_lbfgs(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t ligand_i
               int32_t n_poses, double* lig_xyz, double* rec_tors, double* energy,
               int32_t* nevals, int32_t* status);
 
+/* Host-buffer version over poses of several ligands in one launch (the engine's
+ * optimize over a whole ligand index): ligand_ids [n], xyz [n][max_atoms][3] and
+ * torsions [n][R] (in/out, double), energy [n], nevals [n], status [n]. */
+int pxd_lbfgs_multi(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t n_poses,
+                    int32_t max_atoms, const int32_t* ligand_ids, double* xyz, double* torsions,
+                    double* energy, int32_t* nevals, int32_t* status);
+
 /* Forward torsion-tree kinematics of a batch: replaces free_ligand::apply_parameters
  * (data.cpp:592-641). For pose p: centre [3], rotation matrix rot [9] row-major,
  * torsions [n_torsions] (pre-order), applied to the reference pose xyz_in. */
@@ -408,6 +415,16 @@ int pxd_mc_search(pxd_context* ctx, const pxd_mc_params* params, int32_t ligand_
                   int32_t n_walkers, const int32_t* walker_ids, const int32_t* first_pose,
                   const double* start_xyz, double* out_xyz, double* out_tors, double* out_energy,
                   double* out_pscore, int32_t* out_nevals, int32_t* out_status);
+
+/* Host-buffer version over walkers of several ligands in one launch (the engine's
+ * search over a whole ligand index). start / out xyz [n][max_atoms][3]; out_tors
+ * [n][R]; global_min [n_ligands] (in/out, may be NULL: every ligand starts at 1e8,
+ * the reference's minimum_pre_opt_energy). */
+int pxd_mc_search_multi(pxd_context* ctx, const pxd_mc_params* params, int32_t n_walkers,
+                        int32_t max_atoms, const int32_t* ligand_ids, const int32_t* walker_ids,
+                        const int32_t* first_pose, const double* start_xyz, double* out_xyz,
+                        double* out_tors, double* out_energy, double* out_pscore,
+                        int32_t* out_nevals, int32_t* out_status, double* global_min);
 
 /* Draws of the walker generator as the reference's random_generator makes them
  * (mt19937 + libstdc++ distributions, random.h:33-63), for checking the device stream:

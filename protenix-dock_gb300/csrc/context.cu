@@ -9,6 +9,7 @@
 
 #include "../../include/pxdock_gb300_vdw.h"
 #include "pxd_internal.h"
+#include "schedule.h"
 
 namespace pxd {
 
@@ -64,38 +65,6 @@ struct Packer {
 template <class T>
 const T* at(void* base, size_t off) {
     return reinterpret_cast<const T*>(static_cast<const unsigned char*>(base) + off);
-}
-
-// Orders terms into rounds of 32 in which no atom occurs twice (-1 pads a round).
-template <int K>
-std::vector<int> schedule_rounds(const std::vector<std::array<int, K>>& terms, int n_atoms) {
-    std::vector<int> order;
-    std::vector<char> taken(terms.size(), 0);
-    std::vector<int> stamp(static_cast<size_t>(n_atoms) + 1, -1);
-    size_t left = terms.size();
-    int round = 0;
-    size_t first = 0;
-    while (left > 0) {
-        int filled = 0;
-        while (first < terms.size() && taken[first]) ++first;
-        for (size_t t = first; t < terms.size() && filled < kWarp; ++t) {
-            if (taken[t]) continue;
-            bool ok = true;
-            for (int a : terms[t]) ok = ok && stamp[a] != round;
-            if (!ok) continue;
-            for (int a : terms[t]) stamp[a] = round;
-            taken[t] = 1;
-            order.push_back(static_cast<int>(t));
-            ++filled;
-            --left;
-        }
-        while (filled < kWarp) {
-            order.push_back(-1);
-            ++filled;
-        }
-        ++round;
-    }
-    return order;
 }
 
 struct TopoIn {
@@ -182,8 +151,10 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
                 ij.push_back(make_int2(-1, -1));
                 p.push_back(make_float2(0.f, 0.f));
             } else {
-                ij.push_back(make_int2(t.bonds[s][0], t.bonds[s][1]));
-                p.push_back(make_float2(static_cast<float>(t.bond_k[s]), static_cast<float>(t.bond_r0[s])));
+                const auto a = slot_atoms<2>(t.bonds, s);
+                const int b = s & ~kReversed;
+                ij.push_back(make_int2(a[0], a[1]));
+                p.push_back(make_float2(static_cast<float>(t.bond_k[b]), static_cast<float>(t.bond_r0[b])));
             }
         }
         o.n_bond_slots = static_cast<int>(order.size());
@@ -199,8 +170,10 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
                 ijk.push_back(make_int4(-1, -1, -1, -1));
                 p.push_back(make_float2(0.f, 0.f));
             } else {
-                ijk.push_back(make_int4(t.angles[s][0], t.angles[s][1], t.angles[s][2], 0));
-                p.push_back(make_float2(static_cast<float>(t.angle_k[s]), static_cast<float>(t.angle_t0[s])));
+                const auto a = slot_atoms<3>(t.angles, s);
+                const int b = s & ~kReversed;
+                ijk.push_back(make_int4(a[0], a[1], a[2], 0));
+                p.push_back(make_float2(static_cast<float>(t.angle_k[b]), static_cast<float>(t.angle_t0[b])));
             }
         }
         o.n_angle_slots = static_cast<int>(order.size());
@@ -217,9 +190,11 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
                 ijkl.push_back(make_int4(-1, -1, -1, -1));
                 tr.push_back(make_int2(0, 0));
             } else {
-                ijkl.push_back(make_int4(t.dih[s][0], t.dih[s][1], t.dih[s][2], t.dih[s][3]));
-                tr.push_back(make_int2(static_cast<int>(terms.size()), static_cast<int>(t.dih_terms[s].size())));
-                for (auto& u : t.dih_terms[s])
+                const auto a = slot_atoms<4>(t.dih, s);
+                const int b = s & ~kReversed;
+                ijkl.push_back(make_int4(a[0], a[1], a[2], a[3]));
+                tr.push_back(make_int2(static_cast<int>(terms.size()), static_cast<int>(t.dih_terms[b].size())));
+                for (auto& u : t.dih_terms[b])
                     terms.push_back(make_float4(static_cast<float>(u[0]), static_cast<float>(u[1]),
                                                 static_cast<float>(u[2]), 0.f));
             }
@@ -239,10 +214,11 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
                 p.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
                 continue;
             }
-            const int i = t.pairs[s][0], j = t.pairs[s][1];
+            const auto a = slot_atoms<2>(t.pairs, s);
+            const int i = a[0], j = a[1], b = s & ~kReversed;
             // pair.h:25-60: qq = qi qj scale; fused eps = sqrt(ei ej) scale 4; sigma mean
-            const double A = t.q[i] * t.q[j] * t.pair_sc[s] * kCoulomb;
-            const double C = std::sqrt(t.eps[i] * t.eps[j]) * t.pair_sv[s] * 4.0;
+            const double A = t.q[i] * t.q[j] * t.pair_sc[b] * kCoulomb;
+            const double C = std::sqrt(t.eps[i] * t.eps[j]) * t.pair_sv[b] * 4.0;
             const double sm = (t.sigma[i] + t.sigma[j]) * 0.5;
             ij.push_back(make_int2(i, j));
             p.push_back(make_float4(static_cast<float>(A), static_cast<float>(C),
@@ -1103,6 +1079,49 @@ int pxd_lbfgs(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t lig, int32_t 
     if (nt) cudaMemcpyAsync(dt, ht.data(), nt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(di, ids.data(), n_poses * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
     rc = pxd_lbfgs_dev(ctx, p, n_poses, N, di, dx, dt, de, dn, ds, ctx->stream);
+    if (rc) return rc;
+    cudaMemcpyAsync(hx.data(), dx, nx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (nt) cudaMemcpyAsync(ht.data(), dt, nt * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(energy, de, n_poses * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(nevals, dn, n_poses * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(status, ds, n_poses * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "lbfgs");
+    if (rc) return rc;
+    for (size_t i = 0; i < nx; ++i) xyz[i] = hx[i];
+    for (size_t i = 0; i < nt; ++i) tors[i] = ht[i];
+    return PXD_OK;
+}
+
+int pxd_lbfgs_multi(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses, int32_t max_atoms,
+                    const int32_t* ligand_ids, double* xyz, double* tors, double* energy, int32_t* nevals,
+                    int32_t* status) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS || (n_poses > 0 && !ligand_ids))
+        return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");
+    if (n_poses == 0) return PXD_OK;
+    const int R = ctx->rec.n_rotors;
+    const size_t nx = static_cast<size_t>(n_poses) * max_atoms * 3, nt = static_cast<size_t>(n_poses) * R;
+    std::vector<float> hx(nx), ht(nt);
+    for (size_t i = 0; i < nx; ++i) hx[i] = static_cast<float>(xyz[i]);
+    for (size_t i = 0; i < nt; ++i) ht[i] = static_cast<float>(tors[i]);
+    Staging st{ctx, {}};
+    float* dx = st.alloc<float>(nx, &rc);
+    if (rc) return rc;
+    float* dt = st.alloc<float>(nt, &rc);
+    if (rc) return rc;
+    double* de = st.alloc<double>(n_poses, &rc);
+    if (rc) return rc;
+    int* dn = st.alloc<int>(n_poses, &rc);
+    if (rc) return rc;
+    int* ds = st.alloc<int>(n_poses, &rc);
+    if (rc) return rc;
+    int* di = st.alloc<int>(n_poses, &rc);
+    if (rc) return rc;
+    cudaMemcpyAsync(dx, hx.data(), nx * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (nt) cudaMemcpyAsync(dt, ht.data(), nt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(di, ligand_ids, n_poses * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    rc = pxd_lbfgs_dev(ctx, p, n_poses, max_atoms, di, dx, dt, de, dn, ds, ctx->stream);
     if (rc) return rc;
     cudaMemcpyAsync(hx.data(), dx, nx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
     if (nt) cudaMemcpyAsync(ht.data(), dt, nt * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);

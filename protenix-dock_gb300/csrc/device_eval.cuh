@@ -153,10 +153,17 @@ __device__ __forceinline__ void rotation_and_jacobian(float3 k, float theta, Mat
 }
 
 // ------------------------------------------------------------- term kernels
-// Adds the bonded and non-bonded terms of `t` over coordinates `X`; gradients go to
-// `G` (shared memory, atomics). Matches intra_molecular_interactions::put_gradients.
-__device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, float4* G, DS& e,
+// Adds the bonded and non-bonded terms of `t` over coordinates `X`. The gradient of
+// the atom in position k of a term goes to array k: G[k * gs + atom] (shared memory).
+// Within a round the atoms of each position are distinct (host scheduling), so the
+// atomics never collide; the caller sums the arrays. Matches
+// intra_molecular_interactions::put_gradients.
+__device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, float4* G, int gs, DS& e,
                                            int lane) {
+    float4* G0 = G;
+    float4* G1 = G + gs;
+    float4* G2 = G + 2 * gs;
+    float4* G3 = G + 3 * gs;
     // harmonic bonds (interaction.cpp:27-47)
     for (int s = lane; s < t.n_bond_slots; s += kWarp) {
         const int2 ij = __ldg(&t.bond_ij[s]);
@@ -168,8 +175,8 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
         ds_add(e, 0.5f * p.x * (dr * dr));
         const float de_dr = p.x * (1.f - p.y / (r + kEpsF));
         const float3 g = mul3(d, de_dr);
-        atomic_sub3(&G[ij.x], g);
-        atomic_add3(&G[ij.y], g);
+        atomic_sub3(&G0[ij.x], g);
+        atomic_add3(&G1[ij.y], g);
     }
     // harmonic angles (interaction.cpp:49-74, math.cpp:96-110)
     for (int s = lane; s < t.n_angle_slots; s += kWarp) {
@@ -188,9 +195,9 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
         ds_add(e, 0.5f * p.x * (delta * delta));
         const float de = p.x * delta;
         const float3 fi = mul3(gi, de), fk = mul3(gk, de);
-        atomic_add3(&G[ijk.x], fi);
-        atomic_add3(&G[ijk.z], fk);
-        atomic_sub3(&G[ijk.y], add3(fi, fk));
+        atomic_add3(&G0[ijk.x], fi);
+        atomic_sub3(&G1[ijk.y], add3(fi, fk));
+        atomic_add3(&G2[ijk.z], fk);
     }
     // Fourier dihedrals, impropers then propers (interaction.cpp:76-117, math.cpp:130-167)
     for (int s = lane; s < t.n_dih_slots; s += kWarp) {
@@ -214,19 +221,20 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
         const float3 sv = sub3(mul3(gi, pp), mul3(gl, qq));
         const float3 gj = mul3(sub3(gi, sv), -1.f), gk = mul3(add3(gl, sv), -1.f);
         const int2 tr = __ldg(&t.dih_terms[s]);
-        float de = 0.f;
+        float de = 0.f, et = 0.f;
         for (int u = 0; u < tr.y; ++u) {
             const float4 term = __ldg(&t.dih_term[tr.x + u]);
             const float delta = theta * term.y - term.z;
             float sd, cd;
             sincosf(delta, &sd, &cd);
-            ds_add(e, term.x * (1.f + cd));
+            et += term.x * (1.f + cd);
             de += term.x * term.y * sd;
         }
-        atomic_add3(&G[q.x], mul3(gi, -de));
-        atomic_add3(&G[q.y], mul3(gj, -de));
-        atomic_add3(&G[q.z], mul3(gk, -de));
-        atomic_add3(&G[q.w], mul3(gl, -de));
+        ds_add(e, et);
+        atomic_add3(&G0[q.x], mul3(gi, -de));
+        atomic_add3(&G1[q.y], mul3(gj, -de));
+        atomic_add3(&G2[q.z], mul3(gk, -de));
+        atomic_add3(&G3[q.w], mul3(gl, -de));
     }
     // 1-4 and all other pairs: Coulomb + LJ 12-6 (interaction.cpp:127-168, pair.h:25-60)
     for (int s = lane; s < t.n_pair_slots; s += kWarp) {
@@ -241,12 +249,11 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
         const float u6 = x * x * x;
         const float u12 = u6 * u6;
         const float ec = p.x * rinv;
-        ds_add(e, ec);
-        ds_add(e, p.y * (u12 - u6));
+        ds_add(e, fmaf(p.y, u12 - u6, ec));
         const float de_dr_r = (p.y * (6.f * u6 - 12.f * u12) - ec) * rinv2;
         const float3 g = mul3(rij, de_dr_r);
-        atomic_sub3(&G[ij.x], g);
-        atomic_add3(&G[ij.y], g);
+        atomic_sub3(&G0[ij.x], g);
+        atomic_add3(&G1[ij.y], g);
     }
 }
 
@@ -324,10 +331,11 @@ __device__ __forceinline__ float grid_lookup(const DevGrid& g, int slot, float q
 // Per-warp shared-memory slice for one pose evaluation.
 struct PoseBufs {
     float4* lig_xyz;   // [N]
-    float4* lig_grad;  // [N]
+    float4* lig_grad;  // [4][N]: one array per term position (topo_terms)
     float4* loc_xyz;   // [n_local]
-    float4* loc_grad;  // [n_local]
+    float4* loc_grad;  // [4][n_local]
     float4* mov_jac;   // [n_mov]
+    int lig_gs, loc_gs;  // array strides
 };
 
 struct EvalEnv {
@@ -351,7 +359,8 @@ static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const
             pz = fmaf(d[3 * a + 2], t, pz);
         }
         b.lig_xyz[a] = make_float4(px, py, pz, 0.f);
-        b.lig_grad[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) b.lig_grad[k * b.lig_gs + a] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     // receptor rotors (receptor_torsion2xyz, interaction.cpp:316-336)
     for (int l = lane; l < R.n_local; l += kWarp) {
@@ -370,12 +379,13 @@ static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const
         } else {
             b.loc_xyz[l] = v;
         }
-        b.loc_grad[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) b.loc_grad[k * b.loc_gs + l] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
     DS e{0.f, 0.f};
-    topo_terms(L.topo, b.lig_xyz, b.lig_grad, e, lane);
-    if (R.n_local > 0) topo_terms(R.intra, b.loc_xyz, b.loc_grad, e, lane);
+    topo_terms(L.topo, b.lig_xyz, b.lig_grad, b.lig_gs, e, lane);
+    if (R.n_local > 0) topo_terms(R.intra, b.loc_xyz, b.loc_grad, b.loc_gs, e, lane);
     // grid lookups (inter_molecular_interactions, cached branch)
     if (env.grid.has_grid) {
         for (int a = lane; a < N; a += kWarp) {
@@ -451,15 +461,22 @@ static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const
     __syncwarp();
     // flat gradient and the receptor-torsion chain rule (interaction.cpp:338-350)
     for (int a = lane; a < N; a += kWarp) {
-        const float4 g = b.lig_grad[a];
-        gout[3 * a] = g.x;
-        gout[3 * a + 1] = g.y;
-        gout[3 * a + 2] = g.z;
+        const float4 g0 = b.lig_grad[a], g1 = b.lig_grad[b.lig_gs + a];
+        const float4 g2 = b.lig_grad[2 * b.lig_gs + a], g3 = b.lig_grad[3 * b.lig_gs + a];
+        gout[3 * a] = (g0.x + g1.x) + (g2.x + g3.x);
+        gout[3 * a + 1] = (g0.y + g1.y) + (g2.y + g3.y);
+        gout[3 * a + 2] = (g0.z + g1.z) + (g2.z + g3.z);
     }
     for (int r = lane; r < R.n_rotors; r += kWarp) {
         float acc = 0.f;
         const int l0 = __ldg(&R.rotor_mov[r]), l1 = __ldg(&R.rotor_mov[r + 1]);
-        for (int l = l0; l < l1; ++l) acc += dot3(xyz(b.mov_jac[l]), xyz(b.loc_grad[l]));
+        for (int l = l0; l < l1; ++l) {
+            const float4 g0 = b.loc_grad[l], g1 = b.loc_grad[b.loc_gs + l];
+            const float4 g2 = b.loc_grad[2 * b.loc_gs + l], g3 = b.loc_grad[3 * b.loc_gs + l];
+            const float3 g = make_float3((g0.x + g1.x) + (g2.x + g3.x), (g0.y + g1.y) + (g2.y + g3.y),
+                                         (g0.z + g1.z) + (g2.z + g3.z));
+            acc += dot3(xyz(b.mov_jac[l]), g);
+        }
         gout[n3 + r] = acc;
     }
     __syncwarp();
@@ -468,16 +485,18 @@ static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const
 
 // Shared-memory floats needed by PoseBufs for a ligand of up to n_atoms atoms.
 __host__ __device__ inline int pose_bufs_floats(int n_atoms, int n_local) {
-    return 8 * n_atoms + 12 * n_local;
+    return 20 * n_atoms + 24 * n_local;
 }
 
 __device__ inline PoseBufs carve_pose_bufs(float* base, int n_atoms, int n_local) {
     PoseBufs b;
     b.lig_xyz = reinterpret_cast<float4*>(base);
     b.lig_grad = b.lig_xyz + n_atoms;
-    b.loc_xyz = b.lig_grad + n_atoms;
+    b.loc_xyz = b.lig_grad + 4 * n_atoms;
     b.loc_grad = b.loc_xyz + n_local;
-    b.mov_jac = b.loc_grad + n_local;
+    b.mov_jac = b.loc_grad + 4 * n_local;
+    b.lig_gs = n_atoms;
+    b.loc_gs = n_local;
     return b;
 }
 

@@ -1,5 +1,6 @@
 // Persistent batched L-BFGS kernel (one warp per pose, dynamic pose queue) and the
 // score+gradient kernel, with their launchers.
+#include <cstdlib>
 #include <mutex>
 
 #include "device_lbfgs.cuh"
@@ -27,8 +28,12 @@ struct LbfgsArgs {
 };
 
 constexpr int kWarpsPerBlock = 4;
+constexpr int kDefaultMinBlocks = 0;
 
-__global__ void __launch_bounds__(kWarpsPerBlock * kWarp)
+// kMinBlocks > 0 asks the compiler to fit that many blocks per SM (register cap);
+// variants are chosen per launch (lbfgs_variant).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinBlocks : 1)
     lbfgs_kernel(const LbfgsArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
@@ -153,6 +158,23 @@ static EvalEnv make_env(pxd_context* ctx) {
 
 static int padded(int D) { return (D + kWarp - 1) / kWarp * kWarp; }
 
+using LbfgsKernelFn = void (*)(LbfgsArgs);
+
+// Register / occupancy variant of lbfgs_kernel: 0 = unconstrained registers, else the
+// minimum resident blocks per SM. PXD_LBFGS_MIN_BLOCKS overrides the default.
+static LbfgsKernelFn lbfgs_variant() {
+    static int choice = [] {
+        const char* v = std::getenv("PXD_LBFGS_MIN_BLOCKS");
+        return v ? std::atoi(v) : kDefaultMinBlocks;
+    }();
+    switch (choice) {
+        case 4: return lbfgs_kernel<4>;
+        case 5: return lbfgs_kernel<5>;
+        case 6: return lbfgs_kernel<6>;
+        default: return lbfgs_kernel<0>;
+    }
+}
+
 int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_ids,
                  const float* xyz, const float* tors, double* energy, float* lig_grad,
                  float* tors_grad, cudaStream_t s) {
@@ -224,14 +246,14 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
     const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + 10 * a.D_pad + 4 * p.history;
     const size_t smem = sizeof(float) * kWarpsPerBlock * per_warp;
-    rc = cuda_check(ctx, cudaFuncSetAttribute(lbfgs_kernel,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const LbfgsKernelFn kern = lbfgs_variant();
+    rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(smem)),
                     "lbfgs smem attribute");
     if (rc) return rc;
     int per_sm = 0;
     rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                             &per_sm, lbfgs_kernel, kWarpsPerBlock * kWarp, smem),
+                             &per_sm, kern, kWarpsPerBlock * kWarp, smem),
                     "lbfgs occupancy");
     if (rc) return rc;
     if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
@@ -245,7 +267,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     a.counter = ctx->d_counter;
     rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), s), "counter reset");
     if (rc) return rc;
-    lbfgs_kernel<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
+    kern<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
     return cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
 }
 
@@ -322,12 +344,13 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
     const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + 10 * a.D_pad + 4 * p.history;
     const size_t smem = sizeof(float) * kWarpsPerBlock * per_warp;
-    rc = cuda_check(ctx, cudaFuncSetAttribute(lbfgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const LbfgsKernelFn kern = lbfgs_variant();
+    rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(smem)),
                     "lbfgs smem attribute");
     if (rc) return rc;
     int per_sm = 0;
-    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lbfgs_kernel,
+    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern,
                                                                       kWarpsPerBlock * kWarp, smem),
                     "lbfgs occupancy");
     if (rc) return rc;
@@ -347,7 +370,7 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.hist = reinterpret_cast<float*>(base + kStaticCounterBytes);
     rc = cuda_check(ctx, cudaMemsetAsync(a.counter, 0, sizeof(int), s), "counter reset");
     if (rc) return rc;
-    lbfgs_kernel<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
+    kern<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
     return cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
 }
 

@@ -654,6 +654,71 @@ int pxd_mc_search(pxd_context* ctx, const pxd_mc_params* p, int32_t lig, int32_t
     return PXD_OK;
 }
 
+int pxd_mc_search_multi(pxd_context* ctx, const pxd_mc_params* p, int32_t n, int32_t max_atoms,
+                        const int32_t* ligand_ids, const int32_t* walker_ids, const int32_t* first_pose,
+                        const double* start, double* out_xyz, double* out_tors, double* out_e, double* out_ps,
+                        int32_t* out_nev, int32_t* out_st, double* global_min) {
+    if (!ctx) return PXD_ERR_INVALID;
+    if (n < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS ||
+        (n > 0 && (!ligand_ids || !walker_ids || !first_pose || !start)))
+        return set_error(ctx, PXD_ERR_INVALID, "bad walker batch");
+    if (n == 0) return PXD_OK;
+    cudaSetDevice(ctx->device);
+    const int R = ctx->rec.n_rotors;
+    const size_t nl = ctx->ligands.size();
+    const size_t nx = static_cast<size_t>(n) * max_atoms * 3, nt = static_cast<size_t>(n) * R;
+    std::vector<float> hx(nx);
+    for (size_t i = 0; i < nx; ++i) hx[i] = static_cast<float>(start[i]);
+    std::vector<double> gm(nl ? nl : 1, 1e8);
+    if (global_min)
+        for (size_t i = 0; i < nl; ++i) gm[i] = global_min[i];
+    const size_t bytes =
+        8 * (2 * static_cast<size_t>(n) + gm.size()) + 4 * (2 * nx + nt + 5 * static_cast<size_t>(n)) + 256;
+    void* mem = nullptr;
+    int rc = cuda_check(ctx, cudaMallocAsync(&mem, bytes, ctx->stream), "search staging");
+    if (rc) return rc;
+    double* d_e = static_cast<double*>(mem);
+    double* d_ps = d_e + n;
+    double* d_gm = d_ps + n;
+    float* d_start = reinterpret_cast<float*>(d_gm + gm.size());
+    float* d_out = d_start + nx;
+    float* d_tors = d_out + nx;
+    int* d_ids = reinterpret_cast<int*>(d_tors + nt);
+    int* d_w = d_ids + n;
+    int* d_first = d_w + n;
+    int* d_nev = d_first + n;
+    int* d_st = d_nev + n;
+    cudaMemcpyAsync(d_start, hx.data(), 4 * nx, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_ids, ligand_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_w, walker_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_first, first_pose, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_gm, gm.data(), 8 * gm.size(), cudaMemcpyHostToDevice, ctx->stream);
+    rc = pxd_mc_search_dev(ctx, p, n, max_atoms, d_ids, d_w, d_first, d_start, d_out, d_tors, d_e, d_ps, d_nev,
+                           d_st, d_gm, ctx->stream);
+    std::vector<float> ho(nx), ht(nt);
+    if (!rc) {
+        cudaMemcpyAsync(ho.data(), d_out, 4 * nx, cudaMemcpyDeviceToHost, ctx->stream);
+        if (nt) cudaMemcpyAsync(ht.data(), d_tors, 4 * nt, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(out_e, d_e, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(out_ps, d_ps, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(out_nev, d_nev, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(out_st, d_st, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(gm.data(), d_gm, 8 * gm.size(), cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    cudaFreeAsync(mem, ctx->stream);
+    if (rc) return rc;
+    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "search");
+    if (rc) return rc;
+    int err = 0;
+    cudaMemcpy(&err, ctx->d_counter + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    for (size_t i = 0; i < nx; ++i) out_xyz[i] = ho[i];
+    for (size_t i = 0; i < nt; ++i) out_tors[i] = ht[i];
+    if (global_min)
+        for (size_t i = 0; i < nl; ++i) global_min[i] = gm[i];
+    if (err) return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a random start found no pose inside the box");
+    return PXD_OK;
+}
+
 int pxd_rng_draws(pxd_context* ctx, uint32_t seed, int32_t n, const int32_t* kinds, const int32_t* ints, double* out) {
     if (!ctx || n < 0 || (n > 0 && (!kinds || !ints || !out))) return PXD_ERR_INVALID;
     cudaSetDevice(ctx->device);

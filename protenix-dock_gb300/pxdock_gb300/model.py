@@ -199,7 +199,7 @@ class Receptor:
         if int(geo["num_atoms"]) != n:
             raise ValueError("Atom count mismatches! Wanted [%s] vs. Parsed [%d]"
                              % (geo["num_atoms"], n))
-        axes, groups = [], []
+        axes, groups, order = [], [], []
         for batch in geo.get("data", {}).values():  # data.cpp:314-336, JSON key order
             a0 = batch["rot_bond_1"]
             a1 = batch["rot_bond_2"]
@@ -207,11 +207,17 @@ class Receptor:
                 axes.append((int(a0[i]), int(a1[i])))
             for frag in batch["fragments"]:
                 groups.append([int(a) for a in frag])
+            order.extend(int(v) for v in batch.get("rot_bond_order", []))
         sigma = _per_atom([float(v) for v in ff["FF_vdW_sigma"]], n)
         eps = _per_atom([float(v) for v in ff["FF_vdW_epsilon"]], n)
         top = Topology.from_ffdata(ff, n, sigma, eps)
         r = cls(xyz, top, axes, groups, raw=d)
         r.lists = ScoreLists(ff, n, ligand=False)
+        # leaf -> position among the rotatable bonds (data.cpp:337-348), used to write
+        # receptor torsions in bond order (restore_bond_orders, data.h:53-61)
+        r.bond_mappings = order if len(order) == len(axes) else list(range(len(axes)))
+        r.num_rotatable_bonds = max([int(geo.get("num_rotatable_bonds", 0))] +
+                                    [m + 1 for m in r.bond_mappings])
         return r
 
     @classmethod

@@ -72,6 +72,11 @@ def load(auto_build=False):
     lib.pxd_mc_search.argtypes = [vp, C.POINTER(abi.McParams), C.c_int32, C.c_int32, abi.i32p,
                                   abi.i32p, abi.f64p, abi.f64p, abi.f64p, abi.f64p, abi.f64p,
                                   abi.i32p, abi.i32p]
+    lib.pxd_lbfgs_multi.argtypes = [vp, C.POINTER(abi.LbfgsParams), C.c_int32, C.c_int32, abi.i32p,
+                                    abi.f64p, abi.f64p, abi.f64p, abi.i32p, abi.i32p]
+    lib.pxd_mc_search_multi.argtypes = [vp, C.POINTER(abi.McParams), C.c_int32, C.c_int32, abi.i32p,
+                                        abi.i32p, abi.i32p, abi.f64p, abi.f64p, abi.f64p, abi.f64p,
+                                        abi.f64p, abi.i32p, abi.i32p, abi.f64p]
     lib.pxd_rng_draws.argtypes = [vp, C.c_uint32, C.c_int32, abi.i32p, abi.i32p, abi.f64p]
     _lib = lib
     return lib
@@ -266,6 +271,41 @@ class Context:
                                            _p(ps), _p(nev, C.c_int32), _p(st, C.c_int32)))
         return dict(xyz=out, torsions=tors[:, : self.n_rotors], energy=e, pscore=ps, nevals=nev,
                     status=st)
+
+    def lbfgs_multi(self, params, lig_ids, xyz, tors=None):
+        """Poses of several ligands in one launch: lig_ids [n], xyz [n][max_atoms][3]
+        (each pose padded to max_atoms), tors [n][R]."""
+        xyz = _f64(xyz).copy()
+        n, max_atoms = xyz.shape[0], xyz.shape[1]
+        ids = np.ascontiguousarray(np.asarray(lig_ids, np.int32).reshape(n))
+        R = self.n_rotors
+        tors = _f64(np.zeros((n, R)) if tors is None else tors).reshape(n, R).copy()
+        e = np.zeros(n)
+        nev = np.zeros(n, np.int32)
+        st = np.zeros(n, np.int32)
+        dummy = np.zeros(1)
+        self._check(self.lib.pxd_lbfgs_multi(self.h, C.byref(params), n, max_atoms, _p(ids, C.c_int32), _p(xyz),
+                                             _p(tors if tors.size else dummy), _p(e), _p(nev, C.c_int32),
+                                             _p(st, C.c_int32)))
+        return dict(xyz=xyz, torsions=tors, energy=e, nevals=nev, status=st)
+
+    def mc_search_multi(self, params, lig_ids, starts, walker_ids, first_pose, global_min=None):
+        """Walkers of several ligands in one launch; starts [n][max_atoms][3]."""
+        starts = _f64(starts)
+        n, max_atoms = starts.shape[0], starts.shape[1]
+        i32 = lambda a: np.ascontiguousarray(np.asarray(a, np.int32).reshape(n))
+        ids, wid, fp = i32(lig_ids), i32(walker_ids), i32(first_pose)
+        out = np.zeros_like(starts)
+        tors = np.zeros((n, max(self.n_rotors, 1)))
+        e, ps = np.zeros(n), np.zeros(n)
+        nev, st = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        gm = None if global_min is None else np.ascontiguousarray(global_min, np.float64)
+        self._check(self.lib.pxd_mc_search_multi(self.h, C.byref(params), n, max_atoms, _p(ids, C.c_int32),
+                                                 _p(wid, C.c_int32), _p(fp, C.c_int32), _p(starts), _p(out),
+                                                 _p(tors), _p(e), _p(ps), _p(nev, C.c_int32), _p(st, C.c_int32),
+                                                 None if gm is None else _p(gm)))
+        return dict(xyz=out, torsions=tors[:, : self.n_rotors], energy=e, pscore=ps, nevals=nev,
+                    status=st, global_min=gm)
 
     def mc_search_dev(self, params, n_walkers, max_atoms, ids_ptr, walker_ptr, first_ptr, start_ptr,
                       out_xyz_ptr, out_tors_ptr, energy_ptr, pscore_ptr, nevals_ptr, status_ptr,

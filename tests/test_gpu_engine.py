@@ -1,0 +1,137 @@
+"""The GB300 `_protenix_dock.ReusableEngine` on the reference engine's own inputs and
+outputs (tests/golden/engine, written by oracle/_ref).
+
+- evaluate: every pose's pscore / bscore within 1e-3 + 1e-5 |s| of the reference's;
+- optimize: the reference's schema and pose order; every energy and score is the FP64
+  value at the returned pose (|dE| <= 1e-3); the final energies of the 30-iteration
+  runs from the same starts agree with the reference's to the optimiser's FP32 bound;
+- search: schema, at most num_modes poses sorted by pose score, poses inside the box,
+  every energy / score the FP64 value at the pose; best scores comparable;
+- dump_maps / load_maps round trip; the reference's precondition errors.
+"""
+import csv
+import json
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+import oracle as O
+from pxdock_gb300 import abi, model
+
+import _protenix_dock as E
+
+pytestmark = pytest.mark.gpu
+
+ENG = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "engine")
+SF = os.path.join(ENG, "scoring_function.json")
+
+
+@pytest.fixture(scope="module")
+def setup(tmp_path_factory):
+    d = tmp_path_factory.mktemp("engine")
+    for f in ("receptor.json", "ligand.json"):
+        shutil.copy(os.path.join(ENG, f), d / f)
+    (d / "index.txt").write_text(str(d / "ligand.json") + "\n")
+    calls = json.load(open(os.path.join(ENG, "calls.json")))
+    rec = model.Receptor.from_file(os.path.join(ENG, "receptor.json"))
+    lig = model.Ligand.from_file(os.path.join(ENG, "ligand.json"))
+    pose_sf, aff_sf = model.load_scoring_function(SF)
+    port = O.PortSystem(rec, lig)
+    box = model.make_box(calls["box"][:3], calls["box"][3:], calls["spacing"])
+    port.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)), nthreads=os.cpu_count() or 1)
+    port.set_slope(1e6)
+    eng = E.ReusableEngine(str(d / "receptor.json"), SF)
+    eng.set_box(*calls["box"])
+    return dict(dir=d, calls=calls, rec=rec, lig=lig, port=port, sf=(pose_sf, aff_sf), eng=eng, box=box)
+
+
+def consistent(s, p):
+    t = np.asarray([p["receptor"]["torsions"][m] for m in s["rec"].bond_mappings])
+    x = np.asarray(p["ligand"]["xyz"])
+    e, _, _ = s["port"].score_grad(t, x)
+    assert abs(p["energy"] - e) <= 1e-3 + 1e-5 * abs(e), (p["energy"], e)
+    ps, _ = s["port"].score(s["sf"][0], s["port"].receptor_apply(t), x)
+    assert abs(p["pscore"] - ps) <= 1e-3 + 1e-5 * abs(ps) + 5e-6 * abs(p["pscore"])
+    return t, x
+
+
+def test_evaluate_matches_reference(setup):
+    s = setup
+    out = str(s["dir"] / "eval.csv")
+    s["eng"].evaluate(str(s["dir"] / "index.txt"), out)
+    ours = list(csv.reader(open(out)))
+    ref = list(csv.reader(open(os.path.join(ENG, "ref_evaluate.csv"))))
+    assert ours[0] == ref[0] and len(ours) == len(ref)
+    for a, b in zip(ours[1:], ref[1:]):
+        assert a[:2] == b[:2]
+        for k in (2, 3):
+            assert abs(float(a[k]) - float(b[k])) <= 1e-3 + 1e-5 * abs(float(b[k])), (a, b)
+
+
+def test_optimize_matches_reference(setup):
+    s = setup
+    s["eng"].generate_maps(s["calls"]["spacing"])
+    out = s["dir"] / "opt"
+    s["eng"].optimize(str(s["dir"] / "index.txt"), str(out), **s["calls"]["optimize"])
+    ours = json.load(open(out / "ligand_out.json"))
+    ref = json.load(open(os.path.join(ENG, "ref_optimize", "ligand_out.json")))
+    assert list(ours) == list(ref)
+    assert [p["offset"] for p in ours["poses"]] == [p["offset"] for p in ref["poses"]]
+    for a, b in zip(ours["poses"], ref["poses"]):
+        assert list(a) == list(b)
+        consistent(s, a)
+        assert a["nevals"] > 0
+        assert abs(a["energy"] - b["energy"]) <= 0.5 + 0.02 * abs(b["energy"]), (a["energy"], b["energy"])
+    best = ours["poses"][ours["best_pose"]["index"]]
+    assert best["pscore"] == min(p["pscore"] for p in ours["poses"])
+
+
+def test_search_outputs(setup):
+    s = setup
+    out = s["dir"] / "search"
+    args = s["calls"]["search"]
+    s["eng"].search(str(s["dir"] / "index.txt"), str(out), **args)
+    ours = json.load(open(out / "ligand_out.json"))
+    ref = json.load(open(os.path.join(ENG, "ref_search", "ligand_out.json")))
+    assert list(ours) == list(ref)
+    assert 1 <= len(ours["poses"]) <= args["num_modes"]
+    ps = [p["pscore"] for p in ours["poses"]]
+    assert ps == sorted(ps) and ours["best_pose"]["index"] == 0
+    lo = np.array(s["box"].init_xyz)
+    hi = lo + (np.array(s["box"].npoints) - 1) * s["box"].spacing
+    for p in ours["poses"]:
+        t, x = consistent(s, p)
+        assert np.all(x > lo) and np.all(x < hi)
+    t, x = consistent(s, ours["poses"][0])
+    bs, _ = s["port"].score(s["sf"][1], s["port"].receptor_apply(t), x)
+    assert abs(ours["best_pose"]["bscore"] - bs) <= 1e-3 + 1e-5 * abs(bs)
+    assert abs(ps[0] - ref["poses"][0]["pscore"]) <= 3.0 + 0.2 * abs(ref["poses"][0]["pscore"])
+
+
+def test_maps_round_trip(setup):
+    s = setup
+    cache = s["dir"] / "maps"
+    s["eng"].dump_maps(str(cache))
+    a = s["dir"] / "opt_a"
+    s["eng"].optimize(str(s["dir"] / "index.txt"), str(a), max_niters=10)
+    other = E.ReusableEngine(str(s["dir"] / "receptor.json"), SF)
+    other.load_maps(str(cache))
+    b = s["dir"] / "opt_b"
+    other.optimize(str(s["dir"] / "index.txt"), str(b), max_niters=10)
+    assert (a / "ligand_out.json").read_text() == (b / "ligand_out.json").read_text()
+
+
+def test_precondition_errors(setup):
+    s = setup
+    eng = E.ReusableEngine(str(s["dir"] / "receptor.json"), SF)
+    with pytest.raises(RuntimeError, match="set_box"):
+        eng.generate_maps(0.5)
+    with pytest.raises(RuntimeError, match="set_box"):
+        eng.search(str(s["dir"] / "index.txt"), str(s["dir"] / "x"))
+    with pytest.raises(RuntimeError):
+        eng.dump_maps(str(s["dir"] / "y"))
+    with pytest.raises(RuntimeError):
+        E.ReusableEngine(str(s["dir"] / "missing.json"), SF)
+    assert E.version()

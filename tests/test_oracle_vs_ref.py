@@ -152,7 +152,17 @@ def test_rng_streams():
 def test_scores_match_reference(system, tmp_path_factory, golden):
     """pscore and bscore (root_scorer::combine) of the port against the reference."""
     rec, lig, port, ref = system
-    sf_path = os.path.join(golden, "scoring_function.json")
+    # The shipped affinity function lists vdW scales for 38 ligand types only; the
+    # reference indexes that list with types up to 98 (an out-of-range read whose
+    # value is whatever memory follows). Pad the list with the neutral scale 1 so that
+    # both sides read defined parameters.
+    sf = json.load(open(os.path.join(golden, "scoring_function.json")))
+    for sec in sf.values():
+        types = sec.get("interaction_vdw_energy", {}).get("types")
+        if types is not None:
+            types.extend({"sigma_scale": 1.0, "epsilon_scale": 1.0} for _ in range(99 - len(types)))
+    sf_path = str(tmp_path_factory.mktemp("sf") / "sf.json")
+    json.dump(sf, open(sf_path, "w"))
     ref.load_sf(sf_path)
     pose_sf, aff_sf = model.load_scoring_function(sf_path)
     rng = np.random.default_rng(13)
