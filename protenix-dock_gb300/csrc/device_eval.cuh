@@ -153,10 +153,29 @@ __device__ __forceinline__ void rotation_and_jacobian(float3 k, float theta, Mat
 }
 
 // ------------------------------------------------------------- term kernels
+// Adds `g` to the gradient record p (shared memory): one 16-byte load and store.
+__device__ __forceinline__ void add_rec(float4* p, float3 g) {
+    float4 v = *p;
+    v.x += g.x;
+    v.y += g.y;
+    v.z += g.z;
+    *p = v;
+}
+__device__ __forceinline__ void sub_rec(float4* p, float3 g) {
+    float4 v = *p;
+    v.x -= g.x;
+    v.y -= g.y;
+    v.z -= g.z;
+    *p = v;
+}
+
 // Adds the bonded and non-bonded terms of `t` over coordinates `X`. The gradient of
 // the atom in position k of a term goes to array k: G[k * gs + atom] (shared memory).
 // Within a round the atoms of each position are distinct (host scheduling), so the
-// atomics never collide; the caller sums the arrays. Matches
+// lanes of a round update distinct records with plain loads and stores; a warp
+// barrier between rounds orders a record's updates from different rounds. Padded
+// slots (-1) compute nothing. Every loop runs a multiple of 32 slots, so all lanes
+// meet every barrier. The caller sums the arrays. Matches
 // intra_molecular_interactions::put_gradients.
 __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, float4* G, int gs, DS& e,
                                            int lane) {
@@ -164,96 +183,105 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
     float4* G1 = G + gs;
     float4* G2 = G + 2 * gs;
     float4* G3 = G + 3 * gs;
+    __syncwarp();
     // harmonic bonds (interaction.cpp:27-47)
     for (int s = lane; s < t.n_bond_slots; s += kWarp) {
         const int2 ij = __ldg(&t.bond_ij[s]);
-        if (ij.x < 0) continue;
-        const float2 p = __ldg(&t.bond_p[s]);
-        const float3 d = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
-        const float r = sqrtf(dot3(d, d));
-        const float dr = r - p.y;
-        ds_add(e, 0.5f * p.x * (dr * dr));
-        const float de_dr = p.x * (1.f - p.y / (r + kEpsF));
-        const float3 g = mul3(d, de_dr);
-        atomic_sub3(&G0[ij.x], g);
-        atomic_add3(&G1[ij.y], g);
+        if (ij.x >= 0) {
+            const float2 p = __ldg(&t.bond_p[s]);
+            const float3 d = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
+            const float r = sqrtf(dot3(d, d));
+            const float dr = r - p.y;
+            ds_add(e, 0.5f * p.x * (dr * dr));
+            const float de_dr = p.x * (1.f - p.y / (r + kEpsF));
+            const float3 g = mul3(d, de_dr);
+            sub_rec(&G0[ij.x], g);
+            add_rec(&G1[ij.y], g);
+        }
+        __syncwarp();
     }
     // harmonic angles (interaction.cpp:49-74, math.cpp:96-110)
     for (int s = lane; s < t.n_angle_slots; s += kWarp) {
         const int4 ijk = __ldg(&t.angle_ijk[s]);
-        if (ijk.x < 0) continue;
-        const float2 p = __ldg(&t.angle_p[s]);
-        const float3 xi = xyz(X[ijk.x]), xj = xyz(X[ijk.y]), xk = xyz(X[ijk.z]);
-        const float3 v0 = sub3(xj, xi), v1 = sub3(xj, xk);
-        const float3 c = cross3(v0, v1);
-        const float rp = sqrtf(dot3(c, c));
-        float3 gi = cross3(v0, c), gk = cross3(c, v1);
-        gi = mul3(gi, -1.f / (dot3(v0, v0) * rp + kEpsF));
-        gk = mul3(gk, -1.f / (dot3(v1, v1) * rp + kEpsF));
-        const float theta = atan2f(rp, dot3(v0, v1) + kEpsF);
-        const float delta = theta - p.y;
-        ds_add(e, 0.5f * p.x * (delta * delta));
-        const float de = p.x * delta;
-        const float3 fi = mul3(gi, de), fk = mul3(gk, de);
-        atomic_add3(&G0[ijk.x], fi);
-        atomic_sub3(&G1[ijk.y], add3(fi, fk));
-        atomic_add3(&G2[ijk.z], fk);
+        if (ijk.x >= 0) {
+            const float2 p = __ldg(&t.angle_p[s]);
+            const float3 xi = xyz(X[ijk.x]), xj = xyz(X[ijk.y]), xk = xyz(X[ijk.z]);
+            const float3 v0 = sub3(xj, xi), v1 = sub3(xj, xk);
+            const float3 c = cross3(v0, v1);
+            const float rp = sqrtf(dot3(c, c));
+            float3 gi = cross3(v0, c), gk = cross3(c, v1);
+            gi = mul3(gi, -1.f / (dot3(v0, v0) * rp + kEpsF));
+            gk = mul3(gk, -1.f / (dot3(v1, v1) * rp + kEpsF));
+            const float theta = atan2f(rp, dot3(v0, v1) + kEpsF);
+            const float delta = theta - p.y;
+            ds_add(e, 0.5f * p.x * (delta * delta));
+            const float de = p.x * delta;
+            const float3 fi = mul3(gi, de), fk = mul3(gk, de);
+            add_rec(&G0[ijk.x], fi);
+            sub_rec(&G1[ijk.y], add3(fi, fk));
+            add_rec(&G2[ijk.z], fk);
+        }
+        __syncwarp();
     }
     // Fourier dihedrals, impropers then propers (interaction.cpp:76-117, math.cpp:130-167)
     for (int s = lane; s < t.n_dih_slots; s += kWarp) {
         const int4 q = __ldg(&t.dih_ijkl[s]);
-        if (q.x < 0) continue;
-        const float3 pi = xyz(X[q.x]), pj = xyz(X[q.y]), pk = xyz(X[q.z]), pl = xyz(X[q.w]);
-        const float3 rij = sub3(pj, pi), rkj = sub3(pj, pk), rkl = sub3(pl, pk);
-        const float3 m = cross3(rij, rkj), n = cross3(rkj, rkl);
-        const float3 w = cross3(m, n);
-        const float wlen = sqrtf(dot3(w, w));
-        const float phi = atan2f(wlen, dot3(m, n) + kEpsF);
-        const float theta = dot3(rij, n) < 0.f ? phi : -phi;
-        const float nrkj2 = dot3(rkj, rkj);
-        const float nrkj_1 = 1.f / (sqrtf(nrkj2) + kEpsF);
-        const float nrkj_2 = nrkj_1 * nrkj_1;
-        const float nrkj = nrkj2 * nrkj_1;
-        const float a = -nrkj / dot3(m, m);
-        const float b = nrkj / dot3(n, n);
-        const float3 gi = mul3(m, -a), gl = mul3(n, -b);
-        const float pp = dot3(rij, rkj) * nrkj_2, qq = dot3(rkj, rkl) * nrkj_2;
-        const float3 sv = sub3(mul3(gi, pp), mul3(gl, qq));
-        const float3 gj = mul3(sub3(gi, sv), -1.f), gk = mul3(add3(gl, sv), -1.f);
-        const int2 tr = __ldg(&t.dih_terms[s]);
-        float de = 0.f, et = 0.f;
-        for (int u = 0; u < tr.y; ++u) {
-            const float4 term = __ldg(&t.dih_term[tr.x + u]);
-            const float delta = theta * term.y - term.z;
-            float sd, cd;
-            sincosf(delta, &sd, &cd);
-            et += term.x * (1.f + cd);
-            de += term.x * term.y * sd;
+        if (q.x >= 0) {
+            const float3 pi = xyz(X[q.x]), pj = xyz(X[q.y]), pk = xyz(X[q.z]), pl = xyz(X[q.w]);
+            const float3 rij = sub3(pj, pi), rkj = sub3(pj, pk), rkl = sub3(pl, pk);
+            const float3 m = cross3(rij, rkj), n = cross3(rkj, rkl);
+            const float3 w = cross3(m, n);
+            const float wlen = sqrtf(dot3(w, w));
+            const float phi = atan2f(wlen, dot3(m, n) + kEpsF);
+            const float theta = dot3(rij, n) < 0.f ? phi : -phi;
+            const float nrkj2 = dot3(rkj, rkj);
+            const float nrkj_1 = 1.f / (sqrtf(nrkj2) + kEpsF);
+            const float nrkj_2 = nrkj_1 * nrkj_1;
+            const float nrkj = nrkj2 * nrkj_1;
+            const float a = -nrkj / dot3(m, m);
+            const float b = nrkj / dot3(n, n);
+            const float3 gi = mul3(m, -a), gl = mul3(n, -b);
+            const float pp = dot3(rij, rkj) * nrkj_2, qq = dot3(rkj, rkl) * nrkj_2;
+            const float3 sv = sub3(mul3(gi, pp), mul3(gl, qq));
+            const float3 gj = mul3(sub3(gi, sv), -1.f), gk = mul3(add3(gl, sv), -1.f);
+            const int2 tr = __ldg(&t.dih_terms[s]);
+            float de = 0.f, et = 0.f;
+            for (int u = 0; u < tr.y; ++u) {
+                const float4 term = __ldg(&t.dih_term[tr.x + u]);
+                const float delta = theta * term.y - term.z;
+                float sd, cd;
+                sincosf(delta, &sd, &cd);
+                et += term.x * (1.f + cd);
+                de += term.x * term.y * sd;
+            }
+            ds_add(e, et);
+            add_rec(&G0[q.x], mul3(gi, -de));
+            add_rec(&G1[q.y], mul3(gj, -de));
+            add_rec(&G2[q.z], mul3(gk, -de));
+            add_rec(&G3[q.w], mul3(gl, -de));
         }
-        ds_add(e, et);
-        atomic_add3(&G0[q.x], mul3(gi, -de));
-        atomic_add3(&G1[q.y], mul3(gj, -de));
-        atomic_add3(&G2[q.z], mul3(gk, -de));
-        atomic_add3(&G3[q.w], mul3(gl, -de));
+        __syncwarp();
     }
     // 1-4 and all other pairs: Coulomb + LJ 12-6 (interaction.cpp:127-168, pair.h:25-60)
     for (int s = lane; s < t.n_pair_slots; s += kWarp) {
         const int2 ij = __ldg(&t.pair_ij[s]);
-        if (ij.x < 0) continue;
-        const float4 p = __ldg(&t.pair_p[s]);
-        const float3 rij = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
-        const float r2 = dot3(rij, rij);
-        const float rinv = rsqrtf(r2);
-        const float rinv2 = rinv * rinv;
-        const float x = p.z * rinv2;
-        const float u6 = x * x * x;
-        const float u12 = u6 * u6;
-        const float ec = p.x * rinv;
-        ds_add(e, fmaf(p.y, u12 - u6, ec));
-        const float de_dr_r = (p.y * (6.f * u6 - 12.f * u12) - ec) * rinv2;
-        const float3 g = mul3(rij, de_dr_r);
-        atomic_sub3(&G0[ij.x], g);
-        atomic_add3(&G1[ij.y], g);
+        if (ij.x >= 0) {
+            const float4 p = __ldg(&t.pair_p[s]);
+            const float3 rij = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
+            const float r2 = dot3(rij, rij);
+            const float rinv = rsqrtf(r2);
+            const float rinv2 = rinv * rinv;
+            const float x = p.z * rinv2;
+            const float u6 = x * x * x;
+            const float u12 = u6 * u6;
+            const float ec = p.x * rinv;
+            ds_add(e, fmaf(p.y, u12 - u6, ec));
+            const float de_dr_r = (p.y * (6.f * u6 - 12.f * u12) - ec) * rinv2;
+            const float3 g = mul3(rij, de_dr_r);
+            sub_rec(&G0[ij.x], g);
+            add_rec(&G1[ij.y], g);
+        }
+        __syncwarp();
     }
 }
 
@@ -393,8 +421,9 @@ static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const
             const float ea = grid_lookup(env.grid, __ldg(&L.map_slot[a]), __ldg(&L.charge[a]),
                                          xyz(b.lig_xyz[a]), g);
             ds_add(e, ea);
-            atomic_add3(&b.lig_grad[a], g);
+            add_rec(&b.lig_grad[a], g);  // one lane per atom; topo_terms ended on a barrier
         }
+        __syncwarp();  // the explicit pairs below add to the same records atomically
     }
     // explicit inter pairs (rotor atoms with maps, every receptor atom without)
     const int M = R.n_explicit;

@@ -500,6 +500,11 @@ def scoring_function_params(node):
         v = node["interaction_vdw_energy"]
         p.vdw_scale = float(v["scale"])
         p.vdw_cutoff = float(v["cutoff"])
+        # types beyond the file's list keep the neutral scale 1 (the reference reads
+        # past its list there: scorer.cpp indexes the scales by ligand type)
+        for t in range(99):
+            p.vdw_sigma_scale[t] = 1.0
+            p.vdw_epsilon_scale[t] = 1.0
         for t, ty in enumerate(v["types"][:99]):
             p.vdw_sigma_scale[t] = float(ty["sigma_scale"])
             p.vdw_epsilon_scale[t] = float(ty["epsilon_scale"])
