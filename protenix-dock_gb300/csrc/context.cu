@@ -194,9 +194,11 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
                 const int b = s & ~kReversed;
                 ijkl.push_back(make_int4(a[0], a[1], a[2], a[3]));
                 tr.push_back(make_int2(static_cast<int>(terms.size()), static_cast<int>(t.dih_terms[b].size())));
+                // k, periodicity, cos(phase), sin(phase)
                 for (auto& u : t.dih_terms[b])
                     terms.push_back(make_float4(static_cast<float>(u[0]), static_cast<float>(u[1]),
-                                                static_cast<float>(u[2]), 0.f));
+                                                static_cast<float>(std::cos(u[2])),
+                                                static_cast<float>(std::sin(u[2]))));
             }
         }
         o.n_dih_slots = static_cast<int>(order.size());

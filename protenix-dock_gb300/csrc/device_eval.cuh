@@ -73,7 +73,8 @@ __device__ __forceinline__ float warp_sum_f(float v) {
 
 // Dot product of two D-vectors with exact FP32 products (fma) accumulated as a
 // compensated pair: ~44 significant bits, on the FP32 pipe.
-__device__ __forceinline__ double vdot(const float* a, const float* b, int D, int lane) {
+// Out of line for the same reason as eval_pose: the optimiser takes ~20 of these.
+static __device__ __noinline__ double vdot(const float* a, const float* b, int D, int lane) {
     DS acc{0.f, 0.f};
     for (int e = lane; e < D; e += kWarp) {
         const float x = a[e], y = b[e];
@@ -231,9 +232,14 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const float3 rij = sub3(pj, pi), rkj = sub3(pj, pk), rkl = sub3(pl, pk);
             const float3 m = cross3(rij, rkj), n = cross3(rkj, rkl);
             const float3 w = cross3(m, n);
-            const float wlen = sqrtf(dot3(w, w));
-            const float phi = atan2f(wlen, dot3(m, n) + kEpsF);
-            const float theta = dot3(rij, n) < 0.f ? phi : -phi;
+            // cos / sin of the dihedral from the geometry: phi = atan2(|m x n|, m.n), and
+            // theta = -phi unless rij.n < 0 (math.cpp:130-167); a degenerate (collinear)
+            // dihedral takes phi = 0 as atan2(0, +eps) does
+            const float mn2 = dot3(m, m) * dot3(n, n);
+            const float inv = mn2 > 0.f ? rsqrtf(mn2) : 0.f;
+            const float c1 = mn2 > 0.f ? dot3(m, n) * inv : 1.f;
+            const float s_phi = sqrtf(dot3(w, w)) * inv;
+            const float s1 = dot3(rij, n) < 0.f ? s_phi : -s_phi;
             const float nrkj2 = dot3(rkj, rkj);
             const float nrkj_1 = 1.f / (sqrtf(nrkj2) + kEpsF);
             const float nrkj_2 = nrkj_1 * nrkj_1;
@@ -247,10 +253,19 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const int2 tr = __ldg(&t.dih_terms[s]);
             float de = 0.f, et = 0.f;
             for (int u = 0; u < tr.y; ++u) {
+                // term: k, periodicity, cos(phase), sin(phase); cos / sin(n theta) by
+                // the angle-addition recurrence
                 const float4 term = __ldg(&t.dih_term[tr.x + u]);
-                const float delta = theta * term.y - term.z;
-                float sd, cd;
-                sincosf(delta, &sd, &cd);
+                const int per = __float2int_rn(term.y);
+                float cn = 1.f, sn = 0.f;
+                for (int k = 0; k < abs(per); ++k) {
+                    const float c = fmaf(cn, c1, -sn * s1);
+                    sn = fmaf(sn, c1, cn * s1);
+                    cn = c;
+                }
+                if (per < 0) sn = -sn;
+                const float cd = fmaf(cn, term.z, sn * term.w);   // cos(n theta - phase)
+                const float sd = fmaf(sn, term.z, -cn * term.w);  // sin(n theta - phase)
                 et += term.x * (1.f + cd);
                 de += term.x * term.y * sd;
             }
@@ -374,8 +389,9 @@ struct EvalEnv {
 // Energy and flat gradient [dE/dxyz (3N) | dE/dtorsion (R)] at x0 + t * d (d may be
 // null: evaluate at x0). Replaces binding_system_interactions::put_gradients as the
 // optimiser's closure calls it (optimizer.cpp:155-167).
-static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const float* x0,
-                            const float* d, float t, float* gout, const PoseBufs& b, int lane) {
+__device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLigand& L, const float* x0,
+                                                const float* d, float t, float* gout, const PoseBufs& b,
+                                                int lane) {
     const int N = L.n_atoms;
     const int n3 = 3 * N;
     const DevReceptor& R = env.rec;
@@ -510,6 +526,14 @@ static __device__ double eval_pose(const EvalEnv& env, const DevLigand& L, const
     }
     __syncwarp();
     return ds_warp_sum(e) + R.e_const;
+}
+
+// Kept out of line: the optimiser calls it from five places, and inlined copies of this
+// much code overflow the instruction cache (the top stall of the batched kernel).
+static __device__ __noinline__ double eval_pose(const EvalEnv& env, const DevLigand& L, const float* x0,
+                                                const float* d, float t, float* gout, const PoseBufs& b,
+                                                int lane) {
+    return eval_pose_body(env, L, x0, d, t, gout, b, lane);
 }
 
 // Shared-memory floats needed by PoseBufs for a ligand of up to n_atoms atoms.

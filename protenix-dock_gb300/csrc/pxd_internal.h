@@ -33,7 +33,7 @@ struct DevTopo {
     const float2* angle_p;    // k, theta0
     const int4* dih_ijkl;
     const int2* dih_terms;    // first term, number of terms
-    const float4* dih_term;   // k, periodicity, phase, -
+    const float4* dih_term;   // k, periodicity, cos(phase), sin(phase)
     const int2* pair_ij;
     const float4* pair_p;     // A = 332.06 qi qj s_c, C = 4 sqrt(ei ej) s_v, S2 = ((si+sj)/2)^2
 };

@@ -112,9 +112,9 @@ def test_walker_population_matches_port(mc):
         ref = c["port"].mc_walker(c["sf"], c["lo"], c["hi"], 7, int(ids[w]), starts[w], True, 6, 15)
         same_class += (out["status"][w] == 0) == (ref["status"] == 0)
         if out["status"][w] == 0:
+            # no box check: a new best is fully relaxed after its in-box test and may
+            # leave the box, as in the reference (searcher.cpp:168-172)
             consistent(c, out, w)
-            x = out["xyz"][w]
-            assert np.all(x > c["lo"]) and np.all(x < c["hi"])
             ps_gpu.append(out["pscore"][w])
         if ref["status"] == 0:
             ps_port.append(ref["pscore"])
