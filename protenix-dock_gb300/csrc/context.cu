@@ -194,11 +194,9 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
                 const int b = s & ~kReversed;
                 ijkl.push_back(make_int4(a[0], a[1], a[2], a[3]));
                 tr.push_back(make_int2(static_cast<int>(terms.size()), static_cast<int>(t.dih_terms[b].size())));
-                // k, periodicity, cos(phase), sin(phase)
                 for (auto& u : t.dih_terms[b])
                     terms.push_back(make_float4(static_cast<float>(u[0]), static_cast<float>(u[1]),
-                                                static_cast<float>(std::cos(u[2])),
-                                                static_cast<float>(std::sin(u[2]))));
+                                                static_cast<float>(u[2]), 0.f));
             }
         }
         o.n_dih_slots = static_cast<int>(order.size());
@@ -692,6 +690,18 @@ static int alloc_maps(pxd_context* ctx, const pxd_box* box, const std::vector<in
     g.init = make_float3(static_cast<float>(box->init_xyz[0]), static_cast<float>(box->init_xyz[1]),
                          static_cast<float>(box->init_xyz[2]));
     g.npts = make_int3(box->npoints[0], box->npoints[1], box->npoints[2]);
+    float fl[3][4];
+    for (int d = 0; d < 3; ++d) {
+        const double lo = box->init_xyz[d], hi = box->init_xyz[d] + (box->npoints[d] - 1) * box->spacing;
+        fl[d][0] = static_cast<float>(lo);
+        fl[d][1] = static_cast<float>(lo - fl[d][0]);
+        fl[d][2] = static_cast<float>(hi);
+        fl[d][3] = static_cast<float>(hi - fl[d][2]);
+    }
+    g.lo_h = make_float3(fl[0][0], fl[1][0], fl[2][0]);
+    g.lo_l = make_float3(fl[0][1], fl[1][1], fl[2][1]);
+    g.hi_h = make_float3(fl[0][2], fl[1][2], fl[2][2]);
+    g.hi_l = make_float3(fl[0][3], fl[1][3], fl[2][3]);
     g.spacing = static_cast<float>(box->spacing);
     g.spacing_inv = static_cast<float>(1.0 / box->spacing);
     g.slope = static_cast<float>(ctx->slope);

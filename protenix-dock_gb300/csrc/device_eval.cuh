@@ -170,6 +170,22 @@ __device__ __forceinline__ void sub_rec(float4* p, float3 g) {
     *p = v;
 }
 
+// One pre-combined pair (p = A, C, S2): energy into `en`, returns dE/dr_ij * r_ij / r
+// (the gradient of atom j; atom i takes its negative).
+__device__ __forceinline__ float3 pair_grad(float4 p, float4 xi, float4 xj, float& en) {
+    const float3 rij = sub3(xyz(xj), xyz(xi));
+    const float r2 = dot3(rij, rij);
+    const float rinv = rsqrtf(r2);
+    const float rinv2 = rinv * rinv;
+    const float x = p.z * rinv2;
+    const float u6 = x * x * x;
+    const float u12 = u6 * u6;
+    const float ec = p.x * rinv;
+    en = fmaf(p.y, u12 - u6, ec);
+    const float de_dr_r = (p.y * (6.f * u6 - 12.f * u12) - ec) * rinv2;
+    return mul3(rij, de_dr_r);
+}
+
 // Adds the bonded and non-bonded terms of `t` over coordinates `X`. The gradient of
 // the atom in position k of a term goes to array k: G[k * gs + atom] (shared memory).
 // Within a round the atoms of each position are distinct (host scheduling), so the
@@ -232,14 +248,9 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const float3 rij = sub3(pj, pi), rkj = sub3(pj, pk), rkl = sub3(pl, pk);
             const float3 m = cross3(rij, rkj), n = cross3(rkj, rkl);
             const float3 w = cross3(m, n);
-            // cos / sin of the dihedral from the geometry: phi = atan2(|m x n|, m.n), and
-            // theta = -phi unless rij.n < 0 (math.cpp:130-167); a degenerate (collinear)
-            // dihedral takes phi = 0 as atan2(0, +eps) does
-            const float mn2 = dot3(m, m) * dot3(n, n);
-            const float inv = mn2 > 0.f ? rsqrtf(mn2) : 0.f;
-            const float c1 = mn2 > 0.f ? dot3(m, n) * inv : 1.f;
-            const float s_phi = sqrtf(dot3(w, w)) * inv;
-            const float s1 = dot3(rij, n) < 0.f ? s_phi : -s_phi;
+            const float wlen = sqrtf(dot3(w, w));
+            const float phi = atan2f(wlen, dot3(m, n) + kEpsF);
+            const float theta = dot3(rij, n) < 0.f ? phi : -phi;
             const float nrkj2 = dot3(rkj, rkj);
             const float nrkj_1 = 1.f / (sqrtf(nrkj2) + kEpsF);
             const float nrkj_2 = nrkj_1 * nrkj_1;
@@ -253,19 +264,10 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const int2 tr = __ldg(&t.dih_terms[s]);
             float de = 0.f, et = 0.f;
             for (int u = 0; u < tr.y; ++u) {
-                // term: k, periodicity, cos(phase), sin(phase); cos / sin(n theta) by
-                // the angle-addition recurrence
-                const float4 term = __ldg(&t.dih_term[tr.x + u]);
-                const int per = __float2int_rn(term.y);
-                float cn = 1.f, sn = 0.f;
-                for (int k = 0; k < abs(per); ++k) {
-                    const float c = fmaf(cn, c1, -sn * s1);
-                    sn = fmaf(sn, c1, cn * s1);
-                    cn = c;
-                }
-                if (per < 0) sn = -sn;
-                const float cd = fmaf(cn, term.z, sn * term.w);   // cos(n theta - phase)
-                const float sd = fmaf(sn, term.z, -cn * term.w);  // sin(n theta - phase)
+                const float4 term = __ldg(&t.dih_term[tr.x + u]);  // k, periodicity, phase
+                const float delta = theta * term.y - term.z;
+                float sd, cd;
+                sincosf(delta, &sd, &cd);
                 et += term.x * (1.f + cd);
                 de += term.x * term.y * sd;
             }
@@ -281,18 +283,9 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
     for (int s = lane; s < t.n_pair_slots; s += kWarp) {
         const int2 ij = __ldg(&t.pair_ij[s]);
         if (ij.x >= 0) {
-            const float4 p = __ldg(&t.pair_p[s]);
-            const float3 rij = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
-            const float r2 = dot3(rij, rij);
-            const float rinv = rsqrtf(r2);
-            const float rinv2 = rinv * rinv;
-            const float x = p.z * rinv2;
-            const float u6 = x * x * x;
-            const float u12 = u6 * u6;
-            const float ec = p.x * rinv;
-            ds_add(e, fmaf(p.y, u12 - u6, ec));
-            const float de_dr_r = (p.y * (6.f * u6 - 12.f * u12) - ec) * rinv2;
-            const float3 g = mul3(rij, de_dr_r);
+            float en;
+            const float3 g = pair_grad(__ldg(&t.pair_p[s]), X[ij.x], X[ij.y], en);
+            ds_add(e, en);
             sub_rec(&G0[ij.x], g);
             add_rec(&G1[ij.y], g);
         }
@@ -320,24 +313,29 @@ __device__ __forceinline__ float grid_lookup(const DevGrid& g, int slot, float q
                                              float3& grad) {
     float f[3] = {(p.x - g.init.x) * g.spacing_inv, (p.y - g.init.y) * g.spacing_inv,
                   (p.z - g.init.z) * g.spacing_inv};
+    // distance beyond the low / high face in A, exact near the face (Sterbenz): with
+    // slope 1e6 a rounded grid coordinate would misplace the penalty by ~1 kcal/mol
+    const float below[3] = {(g.lo_h.x - p.x) + g.lo_l.x, (g.lo_h.y - p.y) + g.lo_l.y, (g.lo_h.z - p.z) + g.lo_l.z};
+    const float above[3] = {(p.x - g.hi_h.x) - g.hi_l.x, (p.y - g.hi_h.y) - g.hi_l.y, (p.z - g.hi_h.z) - g.hi_l.z};
     const int npm1[3] = {g.npts.x - 1, g.npts.y - 1, g.npts.z - 1};
     int lo[3];
     float gs[3];
-    float penalty = 0.f;
+    float penalty = 0.f;  // A beyond the box, summed over axes
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        if (f[d] < 0.f) {
+        if (below[d] > 0.f) {
             lo[d] = 0;
             gs[d] = -1.f;
-            penalty -= f[d];
+            penalty += below[d];
             f[d] = 0.f;
-        } else if (f[d] < static_cast<float>(npm1[d])) {
-            lo[d] = static_cast<int>(f[d]);
+        } else if (above[d] < 0.f) {
+            f[d] = fminf(fmaxf(f[d], 0.f), static_cast<float>(npm1[d]));
+            lo[d] = min(static_cast<int>(f[d]), npm1[d] - 1);
             gs[d] = 0.f;
         } else {
             lo[d] = npm1[d] - 1;
             gs[d] = 1.f;
-            penalty += f[d] - static_cast<float>(npm1[d]);
+            penalty += above[d];
             f[d] = static_cast<float>(npm1[d]);
         }
     }
@@ -352,7 +350,7 @@ __device__ __forceinline__ float grid_lookup(const DevGrid& g, int slot, float q
     float e = 0.f;
     bool hit = true;
     if (penalty > 0.f) {
-        e += penalty * g.spacing * g.slope;
+        e += penalty * g.slope;  // (grid units x spacing) x slope, grid.cpp:211-236
         grad.x += gs[0] * g.slope;
         grad.y += gs[1] * g.slope;
         grad.z += gs[2] * g.slope;

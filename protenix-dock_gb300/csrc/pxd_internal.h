@@ -33,7 +33,7 @@ struct DevTopo {
     const float2* angle_p;    // k, theta0
     const int4* dih_ijkl;
     const int2* dih_terms;    // first term, number of terms
-    const float4* dih_term;   // k, periodicity, cos(phase), sin(phase)
+    const float4* dih_term;   // k, periodicity, phase, -
     const int2* pair_ij;
     const float4* pair_p;     // A = 332.06 qi qj s_c, C = 4 sqrt(ei ej) s_v, S2 = ((si+sj)/2)^2
 };
@@ -123,6 +123,9 @@ struct DevReceptor {
 struct DevGrid {
     int has_grid;
     float3 init;
+    // box faces as FP32 hi + lo pairs (init and init + (npoints - 1) * spacing), so
+    // that the distance of an atom beyond a face is formed exactly near the face
+    float3 lo_h, lo_l, hi_h, hi_l;
     int3 npts;                // points per axis
     float spacing, spacing_inv;
     float slope;
