@@ -210,7 +210,7 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const float r = sqrtf(dot3(d, d));
             const float dr = r - p.y;
             ds_add(e, 0.5f * p.x * (dr * dr));
-            const float de_dr = p.x * (1.f - p.y / (r + kEpsF));
+            const float de_dr = p.x * (1.f - __fdividef(p.y, r + kEpsF));
             const float3 g = mul3(d, de_dr);
             sub_rec(&G0[ij.x], g);
             add_rec(&G1[ij.y], g);
@@ -227,8 +227,8 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const float3 c = cross3(v0, v1);
             const float rp = sqrtf(dot3(c, c));
             float3 gi = cross3(v0, c), gk = cross3(c, v1);
-            gi = mul3(gi, -1.f / (dot3(v0, v0) * rp + kEpsF));
-            gk = mul3(gk, -1.f / (dot3(v1, v1) * rp + kEpsF));
+            gi = mul3(gi, -__fdividef(1.f, dot3(v0, v0) * rp + kEpsF));
+            gk = mul3(gk, -__fdividef(1.f, dot3(v1, v1) * rp + kEpsF));
             const float theta = atan2f(rp, dot3(v0, v1) + kEpsF);
             const float delta = theta - p.y;
             ds_add(e, 0.5f * p.x * (delta * delta));
@@ -252,11 +252,11 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const float phi = atan2f(wlen, dot3(m, n) + kEpsF);
             const float theta = dot3(rij, n) < 0.f ? phi : -phi;
             const float nrkj2 = dot3(rkj, rkj);
-            const float nrkj_1 = 1.f / (sqrtf(nrkj2) + kEpsF);
+            const float nrkj_1 = __fdividef(1.f, sqrtf(nrkj2) + kEpsF);
             const float nrkj_2 = nrkj_1 * nrkj_1;
             const float nrkj = nrkj2 * nrkj_1;
-            const float a = -nrkj / dot3(m, m);
-            const float b = nrkj / dot3(n, n);
+            const float a = -__fdividef(nrkj, dot3(m, m));
+            const float b = __fdividef(nrkj, dot3(n, n));
             const float3 gi = mul3(m, -a), gl = mul3(n, -b);
             const float pp = dot3(rij, rkj) * nrkj_2, qq = dot3(rkj, rkl) * nrkj_2;
             const float3 sv = sub3(mul3(gi, pp), mul3(gl, qq));
@@ -267,7 +267,7 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
                 const float4 term = __ldg(&t.dih_term[tr.x + u]);  // k, periodicity, phase
                 const float delta = theta * term.y - term.z;
                 float sd, cd;
-                sincosf(delta, &sd, &cd);
+                __sincosf(delta, &sd, &cd);  // |delta| <= 7 pi: fast path within FP32 parity
                 et += term.x * (1.f + cd);
                 de += term.x * term.y * sd;
             }
