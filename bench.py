@@ -206,6 +206,101 @@ def run_reference(args):
     return 0
 
 
+def screening_ligands(n, seed=3):
+    """Seeded ligands of uneven size: heavy atoms U{10..60}, rotatable bonds U{0..15},
+    C 70 % / N 12 % / O 15 % / Cl 3 % (a draw the generator cannot embed is redrawn)."""
+    from pxdock_gb300 import model, synth
+
+    rng = np.random.default_rng(seed)
+    out, k = [], 0
+    while len(out) < n and k < 20 * n:
+        h, r = int(rng.integers(10, 61)), int(rng.integers(0, 16))
+        k += 1
+        try:
+            lj = synth.make_ligand(seed=1000 + k, n_heavy=h, n_rot=min(r, h // 3), n_n=max(1, round(0.12 * h)),
+                                   n_o=max(1, round(0.15 * h)), n_other=round(0.03 * h))
+        except RuntimeError:
+            continue
+        lig = model.Ligand.from_json(lj)
+        if lig.n_atoms <= 256 and lig.n_torsions <= 32 and lig.tree.n_frags <= 64:
+            out.append(lig)
+    return out
+
+
+def run_screening(args):
+    """Batched L-BFGS over many ligands of uneven size and their poses in ONE persistent
+    launch (the batching of the screening configuration; L-BFGS steps only)."""
+    import torch
+
+    from pxdock_gb300 import model, native, synth
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    native.load(auto_build=True)
+    rec = model.Receptor.from_json(synth.make_receptor(seed=0))
+    box = model.make_box((0.0, 0.0, 0.0), (BOX_SIZE,) * 3, SPACING)
+    ligs = screening_ligands(args.ligands)
+    ctx = native.Context(local)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, sorted(set(int(t) for l in ligs for t in l.vdw_type)))
+    ctx.set_slope(SLOPE)
+    ids = [ctx.add_ligand(l) for l in ligs]
+    lo = np.array(box.init_xyz)
+    hi = lo + (np.array(box.npoints) - 1) * box.spacing
+    P = args.poses_per_ligand
+    max_atoms = max(l.n_atoms for l in ligs)
+    n = P * len(ligs)
+    xyz = np.zeros((n, max_atoms, 3), np.float32)
+    lig_ids = np.zeros(n, np.int32)
+    for k, (l, lid) in enumerate(zip(ligs, ids)):
+        xyz[k * P:(k + 1) * P, : l.n_atoms] = synth.random_poses(l, lo, hi, P, seed=10 + k)
+        lig_ids[k * P:(k + 1) * P] = lid
+    # interleave ligands so that every stretch of the queue mixes sizes
+    order = np.random.default_rng(0).permutation(n)
+    xyz, lig_ids = xyz[order], lig_ids[order]
+    dev = torch.device("cuda", local)
+    start = torch.from_numpy(xyz).to(dev)
+    x = start.clone()
+    d_ids = torch.from_numpy(lig_ids).to(dev)
+    tors = torch.zeros(1, device=dev)
+    energy = torch.zeros(n, dtype=torch.float64, device=dev)
+    nevals = torch.zeros(n, dtype=torch.int32, device=dev)
+    status = torch.zeros(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    p = lbfgs_params()
+    stream = torch.cuda.Stream(dev)
+    events = []
+    for k in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            x.copy_(start)
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.lbfgs_dev(p, n, max_atoms, d_ids.data_ptr(), x.data_ptr(), tors.data_ptr(), energy.data_ptr(),
+                          nevals.data_ptr(), status.data_ptr(), stream.cuda_stream)
+            b.record(stream)
+        if k >= args.warmup:
+            events.append((a, b))
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in events]))
+    ev = int(nevals.sum().item())
+    sizes = [l.n_atoms for l in ligs]
+    line = {"metric": "L-BFGS-optimised poses/s, uneven ligands batched in one launch", "value": n / ms * 1e3,
+            "unit": "poses/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "gpu_launches": args.steps,
+            "config": {"workload": "screening: %d ligands (%d-%d atoms, 0-%d torsions) x %d poses, one launch, "
+                                   "81^3 maps, m=%d, max_iter=%d, tol_grad=%g"
+                                   % (len(ligs), min(sizes), max(sizes), max(l.n_torsions for l in ligs), P,
+                                      HISTORY, MAX_ITER, TOL_GRAD),
+                       "l2": "flushed between steps (256 MiB write)"},
+            "evals_per_s": ev / ms * 1e3, "evals_per_pose": ev / n,
+            "status_counts": {str(k): int((status == k).sum().item()) for k in range(4)}}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main():
     global N_POSES
     ap = argparse.ArgumentParser()
@@ -214,12 +309,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="optimize", choices=["optimize", "screening"],
+                    help="optimize: the headline (one ligand, 65,536 poses); screening: uneven "
+                         "ligands batched in one launch")
+    ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
+    ap.add_argument("--poses-per-ligand", type=int, default=256, help="screening: poses per ligand")
     ap.add_argument("--poses", type=int, default=N_POSES,
                     help="poses per step (smaller only for profiling captures)")
     args = ap.parse_args()
     N_POSES = args.poses
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "screening":
+        return run_screening(args)
 
     import torch
 
