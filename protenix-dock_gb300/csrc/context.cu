@@ -469,6 +469,13 @@ void pxd_context_destroy(pxd_context* ctx) {
         if (ctx->d_sf[k]) cudaFree(ctx->d_sf[k]);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
+    for (auto& cs : ctx->class_streams)
+        if (cs) {
+            cudaStreamSynchronize(cs);
+            cudaStreamDestroy(cs);
+        }
+    for (auto& ev : ctx->class_events)
+        if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

@@ -1,5 +1,6 @@
 // Persistent batched L-BFGS kernel (one warp per pose, dynamic pose queue) and the
 // score+gradient kernel, with their launchers.
+#include <algorithm>
 #include <cstdlib>
 #include <mutex>
 
@@ -12,9 +13,12 @@ struct LbfgsArgs {
     const DevLigand* ligands;
     const int* lig_ids;
     int n_ligands;
-    float* xyz;        // [P][max_atoms][3]
+    float* xyz;        // [P][stride_atoms][3]
     float* tors;       // [P][R]
-    int max_atoms;
+    int max_atoms;     // shared-memory capacity of a warp (atoms)
+    int stride_atoms;  // pose stride of xyz
+    const int* order;     // optional: queue position -> pose (a size class)
+    const int* count_dev; // optional: number of queue positions, on the device
     double* energy;
     int* nevals;
     int* status;
@@ -64,11 +68,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
     c.env = &a.env;
     c.b = &b;
     c.lane = lane;
+    const int n_queue = a.count_dev ? *a.count_dev : a.n_poses;
     while (true) {
-        int pose = 0;
-        if (lane == 0) pose = atomicAdd(a.counter, 1);
-        pose = __shfl_sync(kFull, pose, 0);
-        if (pose >= a.n_poses) break;
+        int k = 0;
+        if (lane == 0) k = atomicAdd(a.counter, 1);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= n_queue) break;
+        const int pose = a.order ? a.order[k] : k;
         const int lid = a.lig_ids[pose];
         if (lid < 0 || lid >= a.n_ligands || a.ligands[lid].n_atoms > a.max_atoms) {
             if (lane == 0) {
@@ -81,14 +87,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
         const DevLigand L = a.ligands[lid];
         const int N = L.n_atoms;
         const int D = 3 * N + R;
-        const float* px = a.xyz + static_cast<size_t>(pose) * a.max_atoms * 3;
+        const float* px = a.xyz + static_cast<size_t>(pose) * a.stride_atoms * 3;
         for (int e = lane; e < 3 * N; e += kWarp) v.x[e] = px[e];
         for (int r = lane; r < R; r += kWarp) v.x[3 * N + r] = a.tors[static_cast<size_t>(pose) * R + r];
         __syncwarp();
         c.L = &L;
         double energy = 0.0;
         const int st = lbfgs_pose(c, a.c, v, D, Dp, lane, energy);
-        float* ox = a.xyz + static_cast<size_t>(pose) * a.max_atoms * 3;
+        float* ox = a.xyz + static_cast<size_t>(pose) * a.stride_atoms * 3;
         for (int e = lane; e < 3 * N; e += kWarp) ox[e] = v.x[e];
         for (int r = lane; r < R; r += kWarp) a.tors[static_cast<size_t>(pose) * R + r] = v.x[3 * N + r];
         if (lane == 0) {
@@ -212,24 +218,41 @@ int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_id
     return cuda_check(ctx, cudaGetLastError(), "score_kernel launch");
 }
 
-int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int max_atoms,
-                 const int* lig_ids, float* xyz, float* tors, double* energy, int* nevals,
-                 int* status, cudaStream_t s) {
-    if (n_poses <= 0) return PXD_OK;
-    int rc = sync_ligand_table(ctx);
-    if (rc) return rc;
-    LbfgsArgs a;
-    a.env = make_env(ctx);
-    a.ligands = ctx->d_ligands;
-    a.lig_ids = lig_ids;
-    a.n_ligands = static_cast<int>(ctx->ligands.size());
-    a.xyz = xyz;
-    a.tors = tors;
-    a.max_atoms = max_atoms;
-    a.energy = energy;
-    a.nevals = nevals;
-    a.status = status;
-    a.n_poses = n_poses;
+// Size classes of the batched launch: poses are grouped by their ligand's atom count so
+// that each persistent launch sizes its per-warp shared memory (and so its residency)
+// for its own class instead of the largest ligand of the batch.
+constexpr int kSizeClasses = 8;
+constexpr int kClassBound[kSizeClasses] = {32, 64, 96, 128, 160, 192, 224, 256};
+
+struct ClassArgs {
+    const int* lig_ids;
+    const DevLigand* ligands;
+    int n_ligands, n_poses, n_classes;
+    int bound[kSizeClasses];  // atom capacity of each class, ascending
+    int* counts;              // [n_classes]
+    int* lists;               // [n_classes][n_poses]
+};
+
+// One thread per pose: appends the pose to the first class that holds its ligand (an
+// invalid ligand id or an oversize ligand goes to the last class, whose launch flags it).
+__global__ void size_class_kernel(const ClassArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n_poses) return;
+    const int lid = a.lig_ids[i];
+    int c = a.n_classes - 1;
+    if (lid >= 0 && lid < a.n_ligands) {
+        const int n = a.ligands[lid].n_atoms;
+        for (int k = 0; k < a.n_classes; ++k)
+            if (n <= a.bound[k]) {
+                c = k;
+                break;
+            }
+    }
+    const int pos = atomicAdd(&a.counts[c], 1);
+    a.lists[static_cast<size_t>(c) * a.n_poses + pos] = i;
+}
+
+static void fill_consts(LbfgsArgs& a, const pxd_lbfgs_params& p) {
     a.c.max_iter = p.max_iter;
     a.c.max_eval = p.max_eval;
     a.c.m = p.history;
@@ -242,33 +265,145 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     a.c.ls_tol_change = p.ls_tolerance_change;
     a.c.gtd_threshold = p.ls_gtd_threshold;
     a.c.reset = p.reset_threshold;
-    a.n_local = ctx->rec.n_local;
-    a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
-    const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + 10 * a.D_pad + 4 * p.history;
-    const size_t smem = sizeof(float) * kWarpsPerBlock * per_warp;
+}
+
+int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int max_atoms,
+                 const int* lig_ids, float* xyz, float* tors, double* energy, int* nevals,
+                 int* status, cudaStream_t s) {
+    if (n_poses <= 0) return PXD_OK;
+    int rc = sync_ligand_table(ctx);
+    if (rc) return rc;
+    LbfgsArgs base;
+    base.env = make_env(ctx);
+    base.ligands = ctx->d_ligands;
+    base.lig_ids = lig_ids;
+    base.n_ligands = static_cast<int>(ctx->ligands.size());
+    base.xyz = xyz;
+    base.tors = tors;
+    base.stride_atoms = max_atoms;
+    base.energy = energy;
+    base.nevals = nevals;
+    base.status = status;
+    base.n_poses = n_poses;
+    base.order = nullptr;
+    base.count_dev = nullptr;
+    fill_consts(base, p);
+    base.n_local = ctx->rec.n_local;
+    // the classes that registered ligands fall in (capped at the caller's max_atoms)
+    std::vector<int> caps;
+    for (int k = 0; k < kSizeClasses; ++k) {
+        const int cap = std::min(kClassBound[k], max_atoms);
+        bool used = false;
+        for (auto& e : ctx->ligands) used = used || (e.n_atoms <= cap && (k == 0 || e.n_atoms > kClassBound[k - 1]));
+        if (used && (caps.empty() || caps.back() != cap)) caps.push_back(cap);
+        if (cap == max_atoms) break;
+    }
+    if (caps.empty() || caps.back() != max_atoms) caps.push_back(max_atoms);  // oversize / invalid ids
+    const bool classes = caps.size() > 1 && n_poses >= 1024;
+    if (!classes) caps.assign(1, max_atoms);
     const LbfgsKernelFn kern = lbfgs_variant();
-    rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(smem)),
-                    "lbfgs smem attribute");
+    struct Plan {
+        int cap, dp, blocks;
+        size_t smem, stride;
+    };
+    std::vector<Plan> plan;
+    size_t hist_floats = 0;
+    for (int cap : caps) {
+        Plan q;
+        q.cap = cap;
+        q.dp = padded(3 * cap + ctx->rec.n_rotors);
+        const int per_warp = pose_bufs_floats(cap, base.n_local) + 10 * q.dp + 4 * p.history;
+        q.smem = sizeof(float) * kWarpsPerBlock * per_warp;
+        rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  static_cast<int>(q.smem)),
+                        "lbfgs smem attribute");
+        if (rc) return rc;
+        int per_sm = 0;
+        rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpsPerBlock * kWarp,
+                                                                          q.smem),
+                        "lbfgs occupancy");
+        if (rc) return rc;
+        if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
+        q.blocks = per_sm * ctx->n_sm;
+        const int need = (n_poses + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        if (q.blocks > need) q.blocks = need;
+        q.stride = static_cast<size_t>(2) * p.history * q.dp;
+        plan.push_back(q);
+    }
+    // the class launches run concurrently, each on its own history slab
+    std::vector<size_t> hist_off(plan.size());
+    for (size_t k = 0; k < plan.size(); ++k) {
+        hist_off[k] = hist_floats;
+        hist_floats += (plan[k].stride * plan[k].blocks * kWarpsPerBlock + 63) / 64 * 64;
+    }
+    const size_t hist_bytes = (sizeof(float) * hist_floats + 255) / 256 * 256;
+    const size_t n_cls = plan.size();
+    const size_t class_bytes = classes ? sizeof(int) * (2 * n_cls + n_cls * static_cast<size_t>(n_poses)) : 0;
+    rc = ensure_scratch(ctx, hist_bytes + class_bytes);
     if (rc) return rc;
-    int per_sm = 0;
-    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                             &per_sm, kern, kWarpsPerBlock * kWarp, smem),
-                    "lbfgs occupancy");
-    if (rc) return rc;
-    if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
-    int blocks = per_sm * ctx->n_sm;
-    const int need = (n_poses + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    if (blocks > need) blocks = need;
-    a.hist_stride = static_cast<size_t>(2) * p.history * a.D_pad;
-    rc = ensure_scratch(ctx, sizeof(float) * a.hist_stride * blocks * kWarpsPerBlock);
-    if (rc) return rc;
-    a.hist = static_cast<float*>(ctx->scratch);
-    a.counter = ctx->d_counter;
-    rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), s), "counter reset");
-    if (rc) return rc;
-    kern<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
-    return cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
+    float* hist = static_cast<float*>(ctx->scratch);
+    int* counters = classes ? reinterpret_cast<int*>(static_cast<char*>(ctx->scratch) + hist_bytes) : ctx->d_counter;
+    if (classes) {
+        ClassArgs ca;
+        ca.lig_ids = lig_ids;
+        ca.ligands = ctx->d_ligands;
+        ca.n_ligands = base.n_ligands;
+        ca.n_poses = n_poses;
+        ca.n_classes = static_cast<int>(n_cls);
+        for (size_t k = 0; k < n_cls; ++k) ca.bound[k] = plan[k].cap;
+        ca.counts = counters + n_cls;
+        ca.lists = counters + 2 * n_cls;
+        rc = cuda_check(ctx, cudaMemsetAsync(counters, 0, sizeof(int) * 2 * n_cls, s), "class counters");
+        if (rc) return rc;
+        size_class_kernel<<<(n_poses + 255) / 256, 256, 0, s>>>(ca);
+        rc = cuda_check(ctx, cudaGetLastError(), "size_class_kernel launch");
+        if (rc) return rc;
+    } else {
+        rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), s), "counter reset");
+        if (rc) return rc;
+    }
+    // fork: class k runs on side stream k after the classification; join back on s
+    if (classes) {
+        for (size_t k = 0; k <= n_cls; ++k) {
+            if (k < n_cls && !ctx->class_streams[k]) {
+                rc = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->class_streams[k], cudaStreamNonBlocking),
+                                "class stream");
+                if (rc) return rc;
+            }
+            if (!ctx->class_events[k]) {
+                rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->class_events[k], cudaEventDisableTiming),
+                                "class event");
+                if (rc) return rc;
+            }
+        }
+        rc = cuda_check(ctx, cudaEventRecord(ctx->class_events[n_cls], s), "fork");
+        if (rc) return rc;
+    }
+    for (size_t k = 0; k < n_cls; ++k) {
+        LbfgsArgs a = base;
+        a.max_atoms = plan[k].cap;
+        a.D_pad = plan[k].dp;
+        a.hist = hist + hist_off[k];
+        a.hist_stride = plan[k].stride;
+        a.counter = counters + k;
+        cudaStream_t ks = s;
+        if (classes) {
+            a.count_dev = counters + n_cls + k;
+            a.order = counters + 2 * n_cls + k * static_cast<size_t>(n_poses);
+            ks = ctx->class_streams[k];
+            rc = cuda_check(ctx, cudaStreamWaitEvent(ks, ctx->class_events[n_cls], 0), "fork wait");
+            if (rc) return rc;
+        }
+        kern<<<plan[k].blocks, kWarpsPerBlock * kWarp, plan[k].smem, ks>>>(a);
+        rc = cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
+        if (rc) return rc;
+        if (classes) {
+            rc = cuda_check(ctx, cudaEventRecord(ctx->class_events[k], ks), "join record");
+            if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(s, ctx->class_events[k], 0), "join wait");
+            if (rc) return rc;
+        }
+    }
+    return PXD_OK;
 }
 
 // ------------------------------------------------------- allocation-free variant
@@ -328,6 +463,9 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.nevals = nevals;
     a.status = status;
     a.n_poses = n_poses;
+    a.stride_atoms = max_atoms;
+    a.order = nullptr;
+    a.count_dev = nullptr;
     a.c.max_iter = p.max_iter;
     a.c.max_eval = p.max_eval;
     a.c.m = p.history;

@@ -152,6 +152,10 @@ struct LigandEntry {
 struct pxd_context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // side streams and events for the concurrent size-class launches of the batched
+    // optimiser (created on first use)
+    cudaStream_t class_streams[8] = {};
+    cudaEvent_t class_events[9] = {};
     std::string error;
     int n_sm = 0;
     // receptor
