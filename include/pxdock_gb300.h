@@ -342,6 +342,19 @@ int pxd_ligand_kinematics(pxd_context* ctx, int32_t ligand_id, int32_t n_poses,
                           const double* xyz_in, const double* centers, const double* rots,
                           const double* torsions, double* xyz_out);
 
+/* Backward torsion-tree kinematics (no reference counterpart: the reference optimises
+ * ligand atoms in Cartesian space and only runs the tree forward). For poses produced by
+ * pxd_ligand_kinematics with centre c, and dE/dx of some E at those coordinates:
+ *   center_grad [P][3] = sum_i dE/dx_i,
+ *   torque      [P][3] = sum_i (x_i - c) x dE/dx_i   (rotation applied left of the root
+ *                        orientation, rotation-vector coordinates at zero),
+ *   torsion_grad [P][T] = dE/dtheta_k: u_k . sum over the torsion's subtree of
+ *                        (x_i - x_bond) x dE/dx_i, u_k the unit parent->bond-atom axis.
+ * xyz and atom_grad are [P][N][3] in the ligand's atom order. */
+int pxd_ligand_backward(pxd_context* ctx, int32_t ligand_id, int32_t n_poses, const double* xyz,
+                        const double* centers, const double* atom_grad, double* center_grad,
+                        double* torque, double* torsion_grad);
+
 /* Receptor rotor kinematics: replaces torsional_receptor::apply_parameters
  * (data.cpp:366-385). out: [n_poses][n_atoms][3]. */
 int pxd_receptor_kinematics(pxd_context* ctx, int32_t n_poses, const double* torsions,

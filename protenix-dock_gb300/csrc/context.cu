@@ -1194,6 +1194,56 @@ int pxd_ligand_kinematics(pxd_context* ctx, int32_t lig, int32_t n_poses, const 
     return PXD_OK;
 }
 
+int pxd_ligand_backward(pxd_context* ctx, int32_t lig, int32_t n_poses, const double* xyz, const double* centers,
+                        const double* atom_grad, double* center_grad, double* torque, double* torsion_grad) {
+    if (!ctx) return PXD_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (lig < 0 || lig >= static_cast<int>(ctx->ligands.size()) || n_poses < 0)
+        return set_error(ctx, PXD_ERR_INVALID, "ligand id");
+    const LigandEntry& e = ctx->ligands[lig];
+    if (e.dev.n_frags == 0) return set_error(ctx, PXD_ERR_STATE, "ligand has no torsion tree");
+    if (n_poses == 0) return PXD_OK;
+    const int N = e.n_atoms, T = e.n_tors;
+    const size_t nx = static_cast<size_t>(n_poses) * N * 3;
+    std::vector<float> hx(nx), hg(nx), hc(3 * static_cast<size_t>(n_poses));
+    for (size_t i = 0; i < nx; ++i) {
+        hx[i] = static_cast<float>(xyz[i]);
+        hg[i] = static_cast<float>(atom_grad[i]);
+    }
+    for (size_t i = 0; i < hc.size(); ++i) hc[i] = static_cast<float>(centers[i]);
+    int rc;
+    Staging st{ctx, {}};
+    float* dx = st.alloc<float>(nx, &rc);
+    if (rc) return rc;
+    float* dg = st.alloc<float>(nx, &rc);
+    if (rc) return rc;
+    float* dc = st.alloc<float>(hc.size(), &rc);
+    if (rc) return rc;
+    float* doc = st.alloc<float>(hc.size(), &rc);
+    if (rc) return rc;
+    float* dot = st.alloc<float>(hc.size(), &rc);
+    if (rc) return rc;
+    float* dtt = st.alloc<float>(static_cast<size_t>(n_poses) * T, &rc);
+    if (rc) return rc;
+    cudaMemcpyAsync(dx, hx.data(), nx * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dg, hg.data(), nx * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dc, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    rc = launch_ligand_backward(ctx, lig, n_poses, dx, dc, dg, doc, dot, dtt, ctx->stream);
+    if (rc) return rc;
+    std::vector<float> oc(hc.size()), oq(hc.size()), ot(static_cast<size_t>(n_poses) * T);
+    cudaMemcpyAsync(oc.data(), doc, oc.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(oq.data(), dot, oq.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (!ot.empty()) cudaMemcpyAsync(ot.data(), dtt, ot.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ligand backward");
+    if (rc) return rc;
+    for (size_t i = 0; i < oc.size(); ++i) {
+        center_grad[i] = oc[i];
+        torque[i] = oq[i];
+    }
+    for (size_t i = 0; i < ot.size(); ++i) torsion_grad[i] = ot[i];
+    return PXD_OK;
+}
+
 int pxd_receptor_kinematics(pxd_context* ctx, int32_t n_poses, const double* torsions, double* xyz_out) {
     int rc = check_ready(ctx);
     if (rc) return rc;

@@ -142,4 +142,97 @@ int launch_receptor_kinematics(pxd_context* ctx, int n_poses, const float* tors,
     return rc;
 }
 
+// Backward kinematics: gradients of a function of the ligand's atom coordinates with
+// respect to the pose parameters of the forward map above, one warp per pose.
+//   dE/dcentre = sum_i g_i,   dE/domega = sum_i (x_i - centre) x g_i  (a rotation applied
+//   on the left of the root orientation), and for torsion k, which turns the subtree of
+//   its fragment about the unit axis u_k (parent atom -> bond atom) through the bond atom:
+//   dE/dtheta_k = u_k . sum_{i in subtree} (x_i - x_bond) x g_i.
+// Torques are summed about the centre; subtree sums are folded in reverse pre-order.
+struct LigBackArgs {
+    DevLigand L;
+    int n_poses;
+    const float* xyz;      // [P][N][3] current coordinates (atom order)
+    const float* centers;  // [P][3]
+    const float* grad;     // [P][N][3] dE/dx
+    float* out_center;     // [P][3]
+    float* out_torque;     // [P][3]
+    float* out_tors;       // [P][T]
+};
+
+__global__ void __launch_bounds__(kKinWarps * kWarp) ligand_backward_kernel(const LigBackArgs a) {
+    __shared__ float3 s_f[kKinWarps][kMaxFrags];
+    __shared__ float3 s_t[kKinWarps][kMaxFrags];
+    const DevLigand& L = a.L;
+    const int N = L.n_atoms;
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int w = threadIdx.x / kWarp;
+    for (int pose = blockIdx.x * kKinWarps + w; pose < a.n_poses; pose += gridDim.x * kKinWarps) {
+        const float* x = a.xyz + static_cast<size_t>(pose) * N * 3;
+        const float* g = a.grad + static_cast<size_t>(pose) * N * 3;
+        const float3 c = make_float3(a.centers[3 * pose], a.centers[3 * pose + 1], a.centers[3 * pose + 2]);
+        for (int f = lane; f < L.n_frags; f += kWarp) {
+            s_f[w][f] = make_float3(0.f, 0.f, 0.f);
+            s_t[w][f] = make_float3(0.f, 0.f, 0.f);
+        }
+        __syncwarp();
+        float3 ftot = make_float3(0.f, 0.f, 0.f), ttot = ftot;
+        for (int p = lane; p < N; p += kWarp) {
+            const int atom = __ldg(&L.perm[p]);
+            const float3 xi = make_float3(x[3 * atom], x[3 * atom + 1], x[3 * atom + 2]);
+            const float3 gi = make_float3(g[3 * atom], g[3 * atom + 1], g[3 * atom + 2]);
+            const float3 ti = cross3(sub3(xi, c), gi);
+            const int f = __ldg(&L.frag_of[p]);
+            atomicAdd(&s_f[w][f].x, gi.x);
+            atomicAdd(&s_f[w][f].y, gi.y);
+            atomicAdd(&s_f[w][f].z, gi.z);
+            atomicAdd(&s_t[w][f].x, ti.x);
+            atomicAdd(&s_t[w][f].y, ti.y);
+            atomicAdd(&s_t[w][f].z, ti.z);
+            ftot = add3(ftot, gi);
+            ttot = add3(ttot, ti);
+        }
+        ftot = make_float3(warp_sum_f(ftot.x), warp_sum_f(ftot.y), warp_sum_f(ftot.z));
+        ttot = make_float3(warp_sum_f(ttot.x), warp_sum_f(ttot.y), warp_sum_f(ttot.z));
+        __syncwarp();
+        if (lane == 0) {
+            float* ot = a.out_tors + static_cast<size_t>(pose) * L.n_tors;
+            for (int k = L.n_tors - 1; k >= 0; --k) {
+                const int4 q = __ldg(&L.tors[k]);  // fragment, parent fragment, parent atom, bond atom
+                const int ap = __ldg(&L.perm[q.z]), am = __ldg(&L.perm[q.w]);
+                const float3 xp = make_float3(x[3 * ap], x[3 * ap + 1], x[3 * ap + 2]);
+                const float3 xm = make_float3(x[3 * am], x[3 * am + 1], x[3 * am + 2]);
+                float3 u = sub3(xm, xp);
+                u = mul3(u, rsqrtf(dot3(u, u)));
+                const float3 sf = s_f[w][q.x], st = s_t[w][q.x];
+                ot[k] = dot3(u, sub3(st, cross3(sub3(xm, c), sf)));
+                s_f[w][q.y] = add3(s_f[w][q.y], sf);
+                s_t[w][q.y] = add3(s_t[w][q.y], st);
+            }
+            float* oc = a.out_center + 3 * static_cast<size_t>(pose);
+            float* oq = a.out_torque + 3 * static_cast<size_t>(pose);
+            oc[0] = ftot.x;
+            oc[1] = ftot.y;
+            oc[2] = ftot.z;
+            oq[0] = ttot.x;
+            oq[1] = ttot.y;
+            oq[2] = ttot.z;
+        }
+        __syncwarp();
+    }
+}
+
+int launch_ligand_backward(pxd_context* ctx, int lig, int n_poses, const float* xyz, const float* centers,
+                           const float* grad, float* out_center, float* out_torque, float* out_tors,
+                           cudaStream_t s) {
+    const DevLigand& L = ctx->ligands[lig].dev;
+    if (L.n_frags > kMaxFrags) return set_error(ctx, PXD_ERR_INVALID, "too many fragments");
+    LigBackArgs a{L, n_poses, xyz, centers, grad, out_center, out_torque, out_tors};
+    int blocks = (n_poses + kKinWarps - 1) / kKinWarps;
+    if (blocks > ctx->n_sm * 8) blocks = ctx->n_sm * 8;
+    if (blocks < 1) blocks = 1;
+    ligand_backward_kernel<<<blocks, kKinWarps * kWarp, 0, s>>>(a);
+    return cuda_check(ctx, cudaGetLastError(), "ligand_backward_kernel launch");
+}
+
 }  // namespace pxd

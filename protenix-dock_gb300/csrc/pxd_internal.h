@@ -223,6 +223,9 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
 int launch_ligand_kinematics(pxd_context* ctx, int lig, int n_poses, const float* xyz_in,
                              const float* centers, const float* rots, const float* tors,
                              float* xyz_out, cudaStream_t s);
+int launch_ligand_backward(pxd_context* ctx, int lig, int n_poses, const float* xyz, const float* centers,
+                           const float* grad, float* out_center, float* out_torque, float* out_tors,
+                           cudaStream_t s);
 int launch_receptor_kinematics(pxd_context* ctx, int n_poses, const float* tors, float* out,
                                cudaStream_t s);
 int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l);

@@ -61,6 +61,7 @@ def load(auto_build=False):
                               abi.f64p, abi.f64p, abi.i32p, abi.i32p]
     lib.pxd_ligand_kinematics.argtypes = [vp, C.c_int32, C.c_int32, abi.f64p, abi.f64p, abi.f64p,
                                           abi.f64p, abi.f64p]
+    lib.pxd_ligand_backward.argtypes = [vp, C.c_int32, C.c_int32] + [abi.f64p] * 6
     lib.pxd_receptor_kinematics.argtypes = [vp, C.c_int32, abi.f64p, abi.f64p]
     lib.pxd_set_scoring_function.argtypes = [vp, C.c_int32, C.POINTER(abi.SfParams)]
     lib.pxd_score_dev.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp]
@@ -226,6 +227,19 @@ class Context:
         self._check(self.lib.pxd_ligand_kinematics(self.h, lig, n, _p(_f64(xyz).reshape(-1)),
                                                    _p(centers), _p(rots), _p(tors), _p(out)))
         return out
+
+    def ligand_backward(self, lig, xyz, centers, atom_grad):
+        """(dE/dcentre [P][3], torque [P][3], dE/dtorsion [P][T]) from dE/dx at poses xyz."""
+        N = self.ligands[lig].n_atoms
+        T = self.ligands[lig].n_torsions
+        xyz = _f64(xyz).reshape(-1, N, 3)
+        n = xyz.shape[0]
+        g = _f64(atom_grad).reshape(n, N, 3)
+        c = _f64(centers).reshape(n, 3)
+        oc, oq = np.zeros((n, 3)), np.zeros((n, 3))
+        ot = np.zeros((n, max(T, 1)))
+        self._check(self.lib.pxd_ligand_backward(self.h, lig, n, _p(xyz), _p(c), _p(g), _p(oc), _p(oq), _p(ot)))
+        return oc, oq, ot[:, :T]
 
     def set_scoring_function(self, which, params):
         self._check(self.lib.pxd_set_scoring_function(self.h, which, C.byref(params)))
