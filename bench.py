@@ -301,6 +301,78 @@ def run_screening(args):
     return 0
 
 
+def run_docking(args):
+    """Plain docking of one complex (the reference engine's search): --walkers Monte-Carlo
+    walkers of the bench ligand in a 20 A box (55^3 maps), --mc-steps steps each relaxed
+    by up to --relax-steps L-BFGS iterations, all walkers in one persistent launch. The CPU
+    line runs the FP64 port of the same walkers (seeds, moves, relaxations) on all host
+    threads over a bounded sample of walkers, scaled to the same count."""
+    import concurrent.futures
+
+    import torch
+
+    import oracle
+    from pxdock_gb300 import model, native, synth
+
+    torch.cuda.set_device(0)
+    native.load(auto_build=True)
+    rec = model.Receptor.from_json(synth.make_receptor(seed=0))
+    lig = model.Ligand.from_json(synth.make_ligand(seed=1))
+    pose_sf, _ = model.load_scoring_function(os.path.join(REPO, "protenix-dock_gb300", "pxdock_gb300", "data",
+                                                          "scoring_function.json"))
+    box = model.make_box((0.0, 0.0, 0.0), (20.0,) * 3, SPACING)
+    lo = np.array(box.init_xyz)
+    hi = lo + (np.array(box.npoints) - 1) * box.spacing
+    types = sorted(set(int(t) for t in lig.vdw_type))
+    ctx = native.Context(0)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, types)
+    ctx.set_slope(SLOPE)
+    ctx.set_scoring_function(0, pose_sf)
+    lid = ctx.add_ligand(lig)
+    W = args.walkers
+    p = native.mc_params(lo, hi, seed=0, max_nsteps=args.mc_steps, relax_nsteps=args.relax_steps)
+    starts = np.repeat(lig.poses[0][None], W, axis=0)
+    ids = np.arange(W)
+    times = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = ctx.mc_search(p, lid, starts, ids)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    gpu_s = float(np.mean(times))
+    # CPU: the FP64 port walkers on the host threads, a bounded sample
+    threads = cpu_threads()
+    port = oracle.PortSystem(rec, lig)
+    port.build_grid(box, types, nthreads=threads)
+    port.set_slope(SLOPE)
+    n_cpu = min(W, threads)
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda w: port.mc_walker(pose_sf, lo, hi, 0, w, lig.poses[0], True, args.mc_steps,
+                                             args.relax_steps), range(1, n_cpu + 1)))
+    cpu_dt = time.perf_counter() - t0
+    cpu_s = cpu_dt * W / n_cpu  # walkers are independent: the full search is W / n_cpu rounds
+    best = float(np.min(out["pscore"][out["status"] == 0])) if np.any(out["status"] == 0) else None
+    line = {"metric": "docking searches/s (one complex, %d walkers)" % W, "value": 1.0 / gpu_s,
+            "unit": "searches/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * gpu_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)", "gpu_launches": args.steps,
+            "config": {"workload": "docking: bench ligand, %d walkers x %d MC steps, relax <= %d L-BFGS "
+                                   "iterations, 55^3 maps (20 A box @ 0.375 A)" % (W, args.mc_steps, args.relax_steps)},
+            "e2e": {"value": 1.0 / gpu_s, "unit": "searches/s", "h2d_bytes_per_step": int(starts.nbytes),
+                    "d2h_bytes_per_step": int(out["xyz"].nbytes + 24 * W)},
+            "best_pscore": best, "status_counts": {str(k): int((out["status"] == k).sum()) for k in range(3)},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "searches/s", "cores": threads, "kind": "port",
+                             "sample": "%d of %d walkers on %d threads in %.1f s, scaled to %d walkers"
+                                       % (n_cpu, W, threads, cpu_dt, W)}}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main():
     global N_POSES
     ap = argparse.ArgumentParser()
@@ -309,10 +381,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="optimize", choices=["optimize", "screening"],
+    ap.add_argument("--workload", default="optimize", choices=["optimize", "screening", "docking"],
                     help="optimize: the headline (one ligand, 65,536 poses); screening: uneven "
                          "ligands batched in one launch")
     ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
+    ap.add_argument("--walkers", type=int, default=64, help="docking: Monte-Carlo walkers (exhaustiveness)")
+    ap.add_argument("--mc-steps", type=int, default=2000, help="docking: Monte-Carlo steps per walker")
+    ap.add_argument("--relax-steps", type=int, default=300, help="docking: L-BFGS iterations per step")
     ap.add_argument("--poses-per-ligand", type=int, default=256, help="screening: poses per ligand")
     ap.add_argument("--poses", type=int, default=N_POSES,
                     help="poses per step (smaller only for profiling captures)")
@@ -322,6 +397,8 @@ def main():
         return run_reference(args)
     if args.workload == "screening":
         return run_screening(args)
+    if args.workload == "docking":
+        return run_docking(args)
 
     import torch
 
