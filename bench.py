@@ -373,6 +373,54 @@ def run_docking(args):
     return 0
 
 
+def run_evaluate(args):
+    """Score+gradient evaluations/s of the bench workload's poses (one evaluation per pose
+    per launch, pxd_score_grad_dev), inputs resident in HBM, L2 flushed between launches."""
+    import torch
+
+    from pxdock_gb300 import native
+
+    torch.cuda.set_device(0)
+    native.load(auto_build=True)
+    rec, lig, box, poses = workload(n_poses=args.poses)
+    ctx = native.Context(0)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)))
+    ctx.set_slope(SLOPE)
+    lid = ctx.add_ligand(lig)
+    n, N = args.poses, lig.n_atoms
+    dev = torch.device("cuda", 0)
+    x = torch.from_numpy(poses.astype(np.float32)).to(dev)
+    ids = torch.full((n,), lid, dtype=torch.int32, device=dev)
+    tors = torch.zeros(1, device=dev)
+    e = torch.zeros(n, dtype=torch.float64, device=dev)
+    g = torch.zeros_like(x)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    ms = []
+    for k in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.score_grad_dev(n, N, ids.data_ptr(), x.data_ptr(), tors.data_ptr(), e.data_ptr(), g.data_ptr(),
+                               tors.data_ptr(), stream.cuda_stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            ms.append(a.elapsed_time(b))
+    t = float(np.mean(ms))
+    line = {"metric": "score+gradient evaluations/s", "value": n / t * 1e3, "unit": "evals/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "gpu_launches": args.steps,
+            "config": {"workload": "one evaluation of each of %d poses of the bench ligand (%d atoms), 81^3 maps"
+                                   % (n, N), "l2": "flushed between launches (256 MiB write)"}}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main():
     global N_POSES
     ap = argparse.ArgumentParser()
@@ -381,7 +429,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="optimize", choices=["optimize", "screening", "docking"],
+    ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "docking"],
                     help="optimize: the headline (one ligand, 65,536 poses); screening: uneven "
                          "ligands batched in one launch")
     ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
@@ -399,6 +447,8 @@ def main():
         return run_screening(args)
     if args.workload == "docking":
         return run_docking(args)
+    if args.workload == "evaluate":
+        return run_evaluate(args)
 
     import torch
 

@@ -447,6 +447,53 @@ int pxd_mc_search_multi(pxd_context* ctx, const pxd_mc_params* params, int32_t n
 int pxd_rng_draws(pxd_context* ctx, uint32_t seed, int32_t n, const int32_t* kinds,
                   const int32_t* ints, double* out);
 
+/* ------------------------------------------------------------ engine facade */
+
+/* bytedock::ReusableEngine (engine/include/bytedock/core/entrance.h:30-74) over this
+ * library: the same methods, argument meanings and defaults, files in and files out
+ * in the reference's formats (engine/src/core/writer.cpp:40-230). Every call returns
+ * PXD_OK or an error whose message pxd_engine_last_error gives (the reference's
+ * exception texts: "Please call `set_box(...)` first!", ...). pxd_engine_create's own
+ * failure is reported by pxd_engine_last_error(NULL). An empty sf_file selects the
+ * default scoring function shipped beside the library (data/scoring_function.json). */
+typedef struct pxd_engine pxd_engine;
+
+int pxd_engine_create(const char* receptor_file, const char* sf_file, int32_t cpu_nthreads,
+                      int32_t device, pxd_engine** out);
+void pxd_engine_destroy(pxd_engine* engine);
+const char* pxd_engine_last_error(const pxd_engine* engine);
+int pxd_engine_set_box(pxd_engine* engine, double center_x, double center_y, double center_z,
+                       double size_x, double size_y, double size_z);
+int pxd_engine_generate_maps(pxd_engine* engine, double grid_spacing, double max_size);
+/* map cache in this library's format: grid.json + one FP32 record file per map */
+int pxd_engine_dump_maps(pxd_engine* engine, const char* cache_dir);
+int pxd_engine_load_maps(pxd_engine* engine, const char* cache_dir);
+int pxd_engine_drop_maps(pxd_engine* engine);
+/* evaluate: pscore / bscore of every pose of every ligand in the index -> CSV file */
+int pxd_engine_evaluate(pxd_engine* engine, const char* ligand_index_file, const char* output_file);
+/* optimize: L-BFGS of every pose (max_niters, slope), pose_ranker output per ligand */
+int pxd_engine_optimize(pxd_engine* engine, const char* ligand_index_file, const char* output_dir,
+                        int32_t max_niters, double slope);
+/* search: exhaustiveness Monte-Carlo walkers per ligand, pose_cluster output per ligand */
+int pxd_engine_search(pxd_engine* engine, const char* ligand_index_file, const char* output_dir,
+                      int32_t seed, int32_t exhaustiveness, int32_t max_nsteps, int32_t relax_nsteps,
+                      int32_t num_modes, double min_rmsd, double mc_mmenergy_threshold, double slope);
+/* setup_global_logging (entrance.cpp:51-54): "-" = standard error; verbosity 0..2 */
+int pxd_engine_log2file(const char* log_file, int32_t verbosity);
+
+/* The engine's writer and clustering alone (host only, no device needed):
+ * pose_writer::consume for n_poses poses (torsions [n][n_rotors] in receptor-leaf order,
+ * written in rotatable-bond order through bond_mappings), and pose_cluster::preprocess
+ * (kept receives the indices of the kept poses, best first). */
+int pxd_write_poses(const char* path, const char* smiles, int32_t best_id, double bscore,
+                    int32_t n_poses, int32_t n_atoms, const int32_t* offsets, const double* energy,
+                    const double* pscore, const int64_t* nevals, int32_t n_rotors,
+                    const double* torsions, const double* xyz, const int32_t* bond_mappings,
+                    int32_t num_rotatable_bonds);
+int pxd_cluster_poses(int32_t n_poses, int32_t n_atoms, const double* xyz, const double* pscore,
+                      const int64_t* nevals, int32_t num_modes, double min_rmsd, int32_t* kept,
+                      int32_t* n_kept);
+
 #ifdef __cplusplus
 }
 #endif

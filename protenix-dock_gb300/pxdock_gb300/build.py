@@ -1,6 +1,7 @@
 """Build recipe of the native library (libpxdock_gb300.so), in-tree.
 
-nvcc compiles every csrc/*.cu for sm_103a in parallel and links one shared library
+nvcc compiles every csrc/*.cu (and the host-only csrc/*.cpp) for sm_103a in parallel and
+links one shared library
 with the C ABI of include/pxdock_gb300.h. A content hash of sources and flags makes a
 rebuild a no-op when nothing changed.
 """
@@ -29,7 +30,7 @@ def nvcc():
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _digest(files, flags):
@@ -62,7 +63,7 @@ def build(verbose=False, jobs=None):
     logs = {}
 
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(OUT_DIR, os.path.splitext(os.path.basename(src))[0] + ".o")
         cmd = [cc] + NVCC_FLAGS + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -77,7 +78,7 @@ def build(verbose=False, jobs=None):
         for name in sorted(logs):
             f.write("== %s\n%s\n" % (name, logs[name]))
     tmp = out + ".tmp"
-    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

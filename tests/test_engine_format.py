@@ -1,6 +1,6 @@
-"""The engine facade's host logic against the reference engine's own output files
-(tests/golden/engine, written by oracle/_ref through ReusableEngine; see
-tests/golden/make_ref_golden.py).
+"""The C++ engine's host logic (csrc/engine.cpp: writer and clustering, callable
+without a GPU) against the reference engine's own output files (tests/golden/engine,
+written by oracle/_ref through ReusableEngine; see tests/golden/make_ref_golden.py).
 
 - The writer reproduces the reference's output text byte for byte from the values
   (pose_writer::consume, writer.cpp:40-81; report_writer, writer.cpp:210-230).
@@ -36,7 +36,8 @@ def test_writer_reproduces_reference_text(tmp_path, which):
                   torsions=leaf_order(p["receptor"]["torsions"], rec), xyz=np.array(p["ligand"]["xyz"]))
              for p in d["poses"]]
     out = E._write_poses(str(tmp_path / "ligand_out.json"), d.get("mapped_smiles", ""),
-                         d["best_pose"]["index"], d["best_pose"]["bscore"], poses, rec)
+                         d["best_pose"]["index"], d["best_pose"]["bscore"], poses, rec.bond_mappings,
+                         rec.num_rotatable_bonds)
     assert open(out).read() == open(src).read()
 
 
@@ -49,14 +50,26 @@ def test_evaluate_csv_text():
     assert text == open(src).read()
 
 
-def test_format_rows_edge_cases():
-    assert E._format_rows([], "", 10) == ""
-    assert E._format_rows([1.0, 2.5], "  ", 10) == "    1, 2.5\n"
-    ten = E._format_rows([float(i) for i in range(10)], "", 10)
-    assert ten == "  0, 1, 2, 3, 4, 5, 6, 7, 8, 9\n"
-    eleven = E._format_rows([float(i) for i in range(11)], "", 10)
-    assert eleven == "  0, 1, 2, 3, 4, 5, 6, 7, 8, 9, \n  10\n"
-    assert E._g(-0.0) == "-0" and E._g(1e-5) == "1e-05" and E._g(123456789.0) == "1.23457e+08"
+@pytest.mark.parametrize("n_rot", [0, 2, 10, 11])
+def test_torsion_rows_and_numbers(tmp_path, n_rot):
+    """Receptor torsions in rows of ten, every row but the last ending in ", " (printer.h);
+    numbers as std::ostream prints doubles by default."""
+    vals = [float(k) + 0.5 for k in range(n_rot)]
+    vals[:1] = [-0.0] if n_rot else []
+    pose = dict(offset=3, energy=1e-5, pscore=123456789.0, nevals=7, torsions=vals,
+                xyz=np.array([[1.0, 2.25, -3.0]]))
+    path = E._write_poses(str(tmp_path / "o.json"), "C\\C", 0, -2.5, [pose], list(range(n_rot)), n_rot)
+    text = open(path).read()
+    assert '"mapped_smiles": "C\\\\C"' in text
+    assert '"energy": 1e-05,' in text and '"pscore": 1.23457e+08,' in text
+    fmt = ["%g" % v for v in vals]
+    rows = [fmt[i:i + 10] for i in range(0, len(fmt), 10)]
+    expect = "".join("            " + ", ".join(r) + (",\n" if k < len(rows) - 1 else "\n")
+                     for k, r in enumerate(rows))
+    # the full rows end with ", " before the newline
+    expect = expect.replace(",\n", ", \n")
+    assert '"torsions": [\n' + expect + "        ]" in text
+    assert '"xyz": [\n          [1, 2.25, -3]\n        ]' in text
 
 
 def cand(ps, x, nevals=1, off=0):
@@ -87,5 +100,5 @@ def test_port_reproduces_reference_optimize():
     p = abi.lbfgs_params(max_iter=calls["optimize"]["max_niters"])
     for pose in ref["poses"]:
         r = port.lbfgs(p, np.zeros(rec.n_rotors), lig.poses[pose["offset"]])
-        assert E._g(r["energy"]) == E._g(pose["energy"])
+        assert "%g" % r["energy"] == "%g" % pose["energy"]
         assert r["nevals"] == pose["nevals"]
