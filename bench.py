@@ -373,6 +373,152 @@ def run_docking(args):
     return 0
 
 
+DIFF_COMPLEXES = 64
+DIFF_POSES = 256
+DIFF_BOX = 20.0
+
+
+def diff_complexes(n_complexes, seed0=100):
+    """Seeded complexes of the differentiation configuration: receptor seed 100+c (1,500
+    heavy atoms + polar H, 26 A cube), a ligand of U{20..40} heavy atoms and U{2..8}
+    rotatable bonds, a 20 A box at 0.375 A (55^3 points)."""
+    from pxdock_gb300 import model, synth
+
+    rng = np.random.default_rng(seed0)
+    out = []
+    k = 0
+    while len(out) < n_complexes:
+        c = len(out)
+        h, r = int(rng.integers(20, 41)), int(rng.integers(2, 9))
+        k += 1
+        try:
+            lj = synth.make_ligand(seed=5000 + k, n_heavy=h, n_rot=min(r, h // 3), n_n=max(1, round(0.12 * h)),
+                                   n_o=max(1, round(0.15 * h)), n_other=round(0.03 * h))
+        except RuntimeError:
+            continue
+        rec = model.Receptor.from_json(synth.make_receptor(seed=seed0 + c))
+        out.append((rec, model.Ligand.from_json(lj)))
+    return out
+
+
+def run_differentiate(args):
+    """Differentiation through fixed poses: for every pose of every complex, the summed
+    score (empirical terms with 36 weights + 32 x 256 pair tables, plus the grid-map
+    docking energy) and its gradients with respect to the pose DOFs (centre, quaternion,
+    torsions), the atom coordinates, the weights and the tables, through the
+    torch.autograd Functions of pxdock_gb300.autograd. A step is one forward + backward
+    over all poses."""
+    import torch
+
+    from pxdock_gb300 import abi, model, native
+    from pxdock_gb300 import autograd as AG
+
+    torch.cuda.set_device(0)
+    native.load(auto_build=True)
+    dev = torch.device("cuda", 0)
+    pose_sf, _ = model.load_scoring_function(os.path.join(REPO, "protenix-dock_gb300", "pxdock_gb300", "data",
+                                                          "scoring_function.json"))
+    cplx = diff_complexes(args.complexes)
+    P = args.poses_per_ligand
+    box = model.make_box((0.0, 0.0, 0.0), (DIFF_BOX,) * 3, SPACING)
+    ctxs, lids, refs, dofs = [], [], [], []
+    rng = np.random.default_rng(7)
+    for c, (rec, lig) in enumerate(cplx):
+        ctx = native.Context(0)
+        ctx.set_receptor(rec)
+        ctx.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)))
+        ctx.set_slope(SLOPE)
+        ctx.set_scoring_function(0, pose_sf)
+        lid = ctx.add_ligand(lig)
+        ctxs.append(ctx)
+        lids.append(lid)
+        x0 = lig.poses[0] - lig.poses[0].mean(axis=0)
+        refs.append(torch.tensor(x0, dtype=torch.float32, device=dev))
+        q = rng.normal(size=(P, 4))
+        dofs.append((rng.uniform(-4.0, 4.0, size=(P, 3)), q / np.linalg.norm(q, axis=1, keepdims=True),
+                     rng.uniform(-np.pi, np.pi, size=(P, lig.n_torsions))))
+    A = max(l.n_atoms for _, l in cplx)
+    n = P * len(cplx)
+    ctx_ids = torch.tensor(np.repeat(np.arange(len(cplx)), P).astype(np.int32), device=dev)
+    lig_ids = torch.tensor(np.repeat(np.array(lids), P).astype(np.int32), device=dev)
+    per_ids = [torch.full((P,), lid, dtype=torch.int32, device=dev) for lid in lids]
+    w0 = abi.sf_weights(pose_sf)
+    t0 = abi.smooth_pair_tables(1)
+    # pinned host inputs (the e2e leg copies them in and the gradients out every step)
+    h_dofs = [tuple(torch.from_numpy(a.astype(np.float32)).pin_memory() for a in d) for d in dofs]
+    h_w = torch.from_numpy(w0).pin_memory()
+    h_t = torch.from_numpy(t0.astype(np.float32)).pin_memory()
+    d_dofs = [tuple(a.to(dev) for a in d) for d in h_dofs]
+    d_w = h_w.to(dev)
+    d_t = h_t.to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(dev)
+
+    def step(dofs_dev, w_dev, t_dev):
+        leaves = [tuple(a.detach().requires_grad_(True) for a in d) for d in dofs_dev]
+        w = w_dev.detach().requires_grad_(True)
+        t = t_dev.detach().requires_grad_(True)
+        xs = [AG.ligand_pose(ctxs[c], lids[c], refs[c], *leaves[c]) for c in range(len(ctxs))]
+        xyz = torch.cat([torch.nn.functional.pad(x, (0, 0, 0, A - x.shape[1])) for x in xs])
+        s = AG.empirical_score(ctxs, lig_ids, xyz, w, t, ctx_ids=ctx_ids)
+        e = torch.cat([AG.docking_energy(ctxs[c], per_ids[c], xs[c]) for c in range(len(ctxs))])
+        total = (s + e).sum()
+        total.backward()
+        return total, leaves, w, t
+
+    ms, e2e_ms = [], []
+    launches = 3 * len(ctxs) + 3 + 1
+    for k in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            total, leaves, w, t = step(d_dofs, d_w, d_t)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            ms.append(a.elapsed_time(b))
+    # end to end: pinned host DOFs and parameters in, every gradient back to pinned host memory
+    h_out = [tuple(torch.empty(a.shape, dtype=torch.float32).pin_memory() for a in d) for d in h_dofs]
+    h_gw = torch.empty(abi.NUM_SF_WEIGHTS, dtype=torch.float64).pin_memory()
+    h_gt = torch.empty(t0.shape, dtype=torch.float32).pin_memory()
+    for k in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            dd = [tuple(x.to(dev, non_blocking=True) for x in d) for d in h_dofs]
+            total, leaves, w, t = step(dd, h_w.to(dev, non_blocking=True), h_t.to(dev, non_blocking=True))
+            for lv, ho in zip(leaves, h_out):
+                for x, y in zip(lv, ho):
+                    y.copy_(x.grad, non_blocking=True)
+            h_gw.copy_(w.grad, non_blocking=True)
+            h_gt.copy_(t.grad, non_blocking=True)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            e2e_ms.append(a.elapsed_time(b))
+    t_ms, e_ms = float(np.mean(ms)), float(np.mean(e2e_ms))
+    h2d = sum(x.numel() * 4 for d in h_dofs for x in d) + h_w.numel() * 8 + h_t.numel() * 4
+    d2h = sum(x.numel() * 4 for d in h_out for x in d) + h_gw.numel() * 8 + h_gt.numel() * 4
+    sizes = [l.n_atoms for _, l in cplx]
+    line = {"metric": "differentiated poses/s (score + gradients in coordinates, DOFs, 36 weights, 32x256 "
+                      "pair tables)", "value": n / t_ms * 1e3, "unit": "poses/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "gpu_launches": launches * args.steps,
+            "e2e": {"value": n / e_ms * 1e3, "unit": "poses/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "config": {"workload": "differentiation through fixed poses: %d complexes x %d poses, 55^3 maps each, "
+                                   "ligands %d-%d atoms, forward + backward through torch.autograd"
+                                   % (len(cplx), P, min(sizes), max(sizes)),
+                       "l2": "flushed between steps (256 MiB write); 64 map sets exceed L2"},
+            "total_score": float(total.item())}
+    print(json.dumps(line))
+    for c in ctxs:
+        c.close()
+    return 0
+
+
 def run_evaluate(args):
     """Score+gradient evaluations/s of the bench workload's poses (one evaluation per pose
     per launch, pxd_score_grad_dev), inputs resident in HBM, L2 flushed between launches."""
@@ -429,10 +575,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "docking"],
+    ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "docking", "differentiate"],
                     help="optimize: the headline (one ligand, 65,536 poses); screening: uneven "
                          "ligands batched in one launch")
     ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
+    ap.add_argument("--complexes", type=int, default=DIFF_COMPLEXES, help="differentiate: number of complexes")
     ap.add_argument("--walkers", type=int, default=64, help="docking: Monte-Carlo walkers (exhaustiveness)")
     ap.add_argument("--mc-steps", type=int, default=2000, help="docking: Monte-Carlo steps per walker")
     ap.add_argument("--relax-steps", type=int, default=300, help="docking: L-BFGS iterations per step")
@@ -447,6 +594,8 @@ def main():
         return run_screening(args)
     if args.workload == "docking":
         return run_docking(args)
+    if args.workload == "differentiate":
+        return run_differentiate(args)
     if args.workload == "evaluate":
         return run_evaluate(args)
 

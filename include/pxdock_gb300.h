@@ -385,6 +385,96 @@ int pxd_score(pxd_context* ctx, int32_t which, int32_t ligand_id, int32_t n_pose
 int pxd_score_gbsa(pxd_context* ctx, int32_t ligand_id, const double* lig_xyz,
                    const double* rec_tors, double* delta, double* parts);
 
+/* ------------------------------------------- differentiable empirical score */
+/* No reference counterpart: the reference's scorers return values only
+ * (root_scorer::combine, scorer.cpp:53-126). Here the empirical score is a function
+ *   S(x; w, T) = sum over the terms of scorer.cpp:207-613 with the 36 weights w in place
+ *                of the scoring function's coefficients and term scales (GB/SA
+ *                excluded; every term is evaluated whatever its weight)
+ *              + sum over ligand x receptor heavy-atom pairs closer than
+ *                (PXD_PAIR_BINS - 1) * PXD_PAIR_BIN_WIDTH of T[type][r / width],
+ *                linearly interpolated between bins,
+ * and the adjoint returns dS/dx (ligand atoms), dS/dw and dS/dT. The ramps, cut-offs
+ * and sigma / epsilon scales stay those of the installed scoring function. */
+#define PXD_NUM_SF_WEIGHTS 36
+enum pxd_sf_weight {
+    PXD_W_COEF = 0,          /* coef[PXD_TERM_*], 11 entries */
+    PXD_W_VDW_SCALE = 11,
+    PXD_W_HYDRO_SCALE = 12,
+    PXD_W_HBOND_SCALE = 13,
+    PXD_W_IONIC = 14,        /* ionic_coef[2] */
+    PXD_W_PICAT = 16,        /* picat_coef[4] */
+    PXD_W_STACK = 20,        /* stack_coef[2][4] */
+    PXD_W_HBOND = 28         /* hbond_coef[8] */
+};
+/* Unweighted sums the score is linear in, per pose (features[PXD_NUM_SCORE_FEATURES]):
+ * 0 Coulomb, 1 clamped LJ, 2-3 ionic (ligand cation, receptor cation), 4-7 cation-pi
+ * (l-cation x r-ring5, x r-ring6, l-ring5 x r-cation, l-ring6 x r-cation), 8-15
+ * pi stacking [f2f, e2f][l5r5, l5r6, l6r5, l6r6], 16-23 hydrogen-bond classes, 24
+ * hydrophobic, 25 torsion strain, 26 rotatable, 27 pair table. */
+#define PXD_NUM_SCORE_FEATURES 28
+/* Pair-table typing: ligand heavy atoms C N O S P F Cl other (8 classes) x receptor
+ * heavy atoms C N O other (4 classes); hydrogens take no table term. Needs
+ * atomic_numbers in both molecules' pxd_score_lists. */
+#define PXD_PAIR_TYPES 32
+#define PXD_PAIR_BINS 256
+#define PXD_PAIR_BIN_WIDTH 0.03125
+
+/* The 36 weights of a scoring function, in pxd_sf_weight order. */
+void pxd_sf_weights(const pxd_sf_params* params, double* weights);
+
+/* Score and adjoint of a batch, one warp per pose (device buffers, stream-ordered).
+ * weights [36] (double) and tables [PXD_PAIR_TYPES][PXD_PAIR_BINS] (float, NULL: no
+ * table term). grad_out [n_poses] is dL/dS per pose; NULL computes scores and features
+ * only. Outputs (each may be NULL): score [n_poses], features [n_poses][28],
+ * dxyz [n_poses][max_atoms][3] = grad_out * dS/dx (overwritten, padding rows zero),
+ * dweights [36] and dtables [32][256] (double) ACCUMULATE sum_p grad_out_p * dS_p/d...
+ * (callers zero them first, as the reference's gradient callers do). Receptor atoms are
+ * fixed (rotor atoms placed by rec_tors). */
+int pxd_score_adjoint_dev(pxd_context* ctx, int32_t which, int32_t n_poses, int32_t max_atoms,
+                          const int32_t* ligand_ids_dev, const float* lig_xyz_dev,
+                          const float* rec_tors_dev, const double* weights_dev,
+                          const float* tables_dev, const double* grad_out_dev, double* score_dev,
+                          double* features_dev, float* dxyz_dev, double* dweights_dev,
+                          double* dtables_dev, void* stream);
+
+/* pxd_score_adjoint_dev over poses of several contexts (one receptor and its grid each,
+ * all on one device) in one launch: contexts [n_contexts] is a host array,
+ * context_ids_dev [n_poses] picks each pose's context and ligand_ids_dev the ligand in it;
+ * rec_tors_dev rows have the largest receptor-torsion count of the contexts. Every
+ * context needs scoring function `which`. Errors are reported on contexts[0]. */
+int pxd_score_adjoint_multi_dev(pxd_context* const* contexts, int32_t n_contexts, int32_t which,
+                                int32_t n_poses, int32_t max_atoms, const int32_t* context_ids_dev,
+                                const int32_t* ligand_ids_dev, const float* lig_xyz_dev,
+                                const float* rec_tors_dev, const double* weights_dev,
+                                const float* tables_dev, const double* grad_out_dev,
+                                double* score_dev, double* features_dev, float* dxyz_dev,
+                                double* dweights_dev, double* dtables_dev, void* stream);
+
+/* Host-buffer version for one ligand (double in/out; tables may be NULL, grad_out NULL
+ * means 1 for every pose). */
+int pxd_score_adjoint(pxd_context* ctx, int32_t which, int32_t ligand_id, int32_t n_poses,
+                      const double* lig_xyz, const double* rec_tors, const double* weights,
+                      const double* tables, const double* grad_out, double* score,
+                      double* features, double* dxyz, double* dweights, double* dtables);
+
+/* Device-buffer pose kinematics for gradient pipelines (no reference counterpart beyond
+ * free_ligand::apply_parameters, data.cpp:592-641). Pose p: centre [3], orientation as a
+ * quaternion (w, x, y, z) [4], normalised on use and turned into a matrix as
+ * get_rotation_matrix does (math.cpp:22-42), torsions [T]. xyz_in [N][3] is the
+ * ligand's reference pose; xyz_out [P][N][3]. */
+int pxd_ligand_pose_dev(pxd_context* ctx, int32_t ligand_id, int32_t n_poses, const float* xyz_in_dev,
+                        const float* centers_dev, const float* quats_dev, const float* torsions_dev,
+                        float* xyz_out_dev, void* stream);
+
+/* Backward of pxd_ligand_pose_dev: from dL/dx [P][N][3] at xyz [P][N][3], writes
+ * dL/dcentre [P][3], dL/dquaternion [P][4] (through the normalisation) and
+ * dL/dtorsions [P][T]. */
+int pxd_ligand_pose_backward_dev(pxd_context* ctx, int32_t ligand_id, int32_t n_poses,
+                                 const float* xyz_dev, const float* centers_dev, const float* quats_dev,
+                                 const float* atom_grad_dev, float* center_grad_dev, float* quat_grad_dev,
+                                 float* torsion_grad_dev, void* stream);
+
 /* ------------------------------------------------------- Monte-Carlo search */
 
 /* Constants of one Monte-Carlo search (monte_carlo_searcher, searcher.h:29-41 and the

@@ -81,6 +81,13 @@ def port_lib():
         lib.po_score.argtypes = [C.POINTER(abi.SfParams), C.c_int, f64p, f64p, f64p, f64p,
                                  C.POINTER(abi.ScoreLists), C.c_int, f64p, f64p, i32p,
                                  C.POINTER(abi.ScoreLists), f64p]
+        lib.po_score_diff.restype = C.c_double
+        lib.po_score_diff.argtypes = [C.POINTER(abi.SfParams), C.c_int, f64p, f64p, f64p, f64p,
+                                      C.POINTER(abi.ScoreLists), C.c_int, f64p, f64p, i32p,
+                                      C.POINTER(abi.ScoreLists), f64p, f64p, C.c_double, f64p, f64p, f64p,
+                                      f64p]
+        lib.po_combine_features.restype = C.c_double
+        lib.po_combine_features.argtypes = [f64p, f64p]
         lib.po_vdw_check.restype = C.c_double
         lib.po_vdw_check.argtypes = [C.POINTER(abi.SfParams), C.c_int, f64p, f64p, f64p, C.c_int,
                                      f64p, i32p]
@@ -319,6 +326,30 @@ def port_score(sf, receptor, ligand, rec_xyz, lig_xyz):
                      _p(lx), _p(ligand.ff.charge), _p(ligand.vdw_type, C.c_int32), C.byref(ll),
                      _p(terms))
     return v, terms
+
+
+def port_score_diff(sf, receptor, ligand, rec_xyz, lig_xyz, weights, table=None, g=1.0, grads=True):
+    """FP64 differentiable empirical score of one pose: (score, features[28], and with
+    grads: g dS/dx [N][3], g dS/dw [36], g dS/dT [32*256])."""
+    lib = port_lib()
+    keep = []
+    rl = receptor.lists.to_c(keep)
+    ll = ligand.lists.to_c(keep)
+    rx = _d(rec_xyz).reshape(-1)
+    lx = _d(lig_xyz).reshape(-1)
+    w = _d(weights)
+    tab = None if table is None else _d(table).reshape(-1)
+    f = np.zeros(28)
+    gx = np.zeros(ligand.n_atoms * 3) if grads else None
+    gw = np.zeros(36) if grads else None
+    gt = np.zeros(32 * 256) if grads and tab is not None else None
+    v = lib.po_score_diff(C.byref(sf), receptor.n_atoms, _p(rx), _p(receptor.ff.charge), _p(receptor.ff.sigma),
+                          _p(receptor.ff.epsilon), C.byref(rl), ligand.n_atoms, _p(lx), _p(ligand.ff.charge),
+                          _p(ligand.vdw_type, C.c_int32), C.byref(ll), _p(w), _p(tab), g, _p(f), _p(gx), _p(gw),
+                          _p(gt))
+    if not grads:
+        return v, f
+    return v, f, gx.reshape(-1, 3), gw, gt
 
 
 class RefSystem:

@@ -1980,3 +1980,421 @@ void po_mc_randomize(po_system* s, const pxd_sf_params* sf, const double* lo, co
     po_rng_seed(&rg, seed + (uint32_t)walker);
     mc_randomize(&e, start, first_pose, lo, hi, &rg, out);
 }
+
+/* ============================== differentiable empirical score (no reference code) */
+/* The weights / features / pair-table split of the empirical score and its analytic
+ * adjoint, in FP64. The features are the unweighted sums of the leaf scorers above
+ * (scorer.cpp:222-613); combining them with pxd_sf_weights(sf) and every term active
+ * gives po_score. Gradients: ramps -1/(hi-lo) inside [lo, hi]; clamped LJ 0 beyond the
+ * cut-off; acos' = -1/sqrt(1-c^2) inside the clamp; ring centroids share their gradient
+ * equally, normals through n = (p1-p0) x (p1-p2) and its normalisation; dihedrals by
+ * po_dihedral_and_gradient. */
+static double ramp_down_d(double v, double lo, double hi) {
+    return (v >= lo && v <= hi) ? -1.0 / (hi - lo) : 0.0;
+}
+static double ramp_c_vd(double v, double c, double lo, double hi, double* dv) {
+    if (v < c) {
+        *dv = -ramp_down_d(c - v, lo, hi);
+        return ramp_down(c - v, lo, hi);
+    }
+    *dv = ramp_down_d(v - c, lo, hi);
+    return ramp_down(v - c, lo, hi);
+}
+static void gacc(double* G, int i, const double* g, double s) {
+    if (!G) return;
+    G[3 * i] += s * g[0];
+    G[3 * i + 1] += s * g[1];
+    G[3 * i + 2] += s * g[2];
+}
+/* gradient on a ligand ring's centroid (gc) and unit normal (gn) onto its atoms */
+static void ring_backward(const double* x, const int32_t* r, const double* gc, const double* gn, double* G) {
+    if (!G) return;
+    const int n = ring_size(r);
+    for (int k = 0; k < n; ++k) gacc(G, r[k], gc, 1.0 / n);
+    double a[3], b[3], nv[3], u[3], gnn[3], ga[3], gb[3];
+    v_sub(x + 3 * r[1], x + 3 * r[0], a);
+    v_sub(x + 3 * r[1], x + 3 * r[2], b);
+    v_cross(a, b, nv);
+    const double len = v_norm(nv);
+    v_scale(nv, 1.0 / len, u);
+    const double gu = v_dot(gn, u);
+    for (int d = 0; d < 3; ++d) gnn[d] = (gn[d] - gu * u[d]) / len;
+    v_cross(b, gnn, ga);
+    v_cross(gnn, a, gb);
+    gacc(G, r[0], ga, -1.0);
+    gacc(G, r[1], ga, 1.0);
+    gacc(G, r[1], gb, 1.0);
+    gacc(G, r[2], gb, -1.0);
+}
+static int pair_class_d(int rec, int z) {
+    if (z < 2) return -1;
+    if (z == 6) return 0;
+    if (z == 7) return 1;
+    if (z == 8) return 2;
+    if (rec) return 3;
+    switch (z) {
+        case 16: return 3;
+        case 15: return 4;
+        case 9: return 5;
+        case 17: return 6;
+        default: return 7;
+    }
+}
+
+double po_combine_features(const double* w, const double* f) {
+    double s = w[PXD_W_COEF + PXD_TERM_COULOMB] * f[0];
+    s += w[PXD_W_COEF + PXD_TERM_VDW] * w[PXD_W_VDW_SCALE] * f[1];
+    s += w[PXD_W_COEF + PXD_TERM_IONIC] * (w[PXD_W_IONIC] * f[2] + w[PXD_W_IONIC + 1] * f[3]);
+    double t = 0.0;
+    for (int k = 0; k < 4; ++k) t += w[PXD_W_PICAT + k] * f[4 + k];
+    s += w[PXD_W_COEF + PXD_TERM_PI_CATION] * t;
+    for (int q = 0; q < 2; ++q) {
+        t = 0.0;
+        for (int k = 0; k < 4; ++k) t += w[PXD_W_STACK + 4 * q + k] * f[8 + 4 * q + k];
+        s += w[PXD_W_COEF + PXD_TERM_F2F + q] * t;
+    }
+    t = 0.0;
+    for (int k = 0; k < 8; ++k) t += w[PXD_W_HBOND + k] * f[16 + k];
+    s += w[PXD_W_COEF + PXD_TERM_HBOND] * w[PXD_W_HBOND_SCALE] * t;
+    s += w[PXD_W_COEF + PXD_TERM_HYDROPHOBIC] * w[PXD_W_HYDRO_SCALE] * f[24];
+    s += w[PXD_W_COEF + PXD_TERM_TSTRAIN] * f[25];
+    s += w[PXD_W_COEF + PXD_TERM_ROTATABLE] * f[26];
+    return s + f[27];
+}
+
+void po_combine_grad(const double* w, const double* f, double g, double* dw) {
+    double hb = 0.0, pc = 0.0, st[2] = {0.0, 0.0};
+    for (int k = 0; k < 8; ++k) hb += w[PXD_W_HBOND + k] * f[16 + k];
+    for (int k = 0; k < 4; ++k) pc += w[PXD_W_PICAT + k] * f[4 + k];
+    for (int q = 0; q < 2; ++q)
+        for (int k = 0; k < 4; ++k) st[q] += w[PXD_W_STACK + 4 * q + k] * f[8 + 4 * q + k];
+    double d[PXD_NUM_SF_WEIGHTS] = {0};
+    d[PXD_W_COEF + PXD_TERM_COULOMB] = f[0];
+    d[PXD_W_COEF + PXD_TERM_VDW] = w[PXD_W_VDW_SCALE] * f[1];
+    d[PXD_W_COEF + PXD_TERM_IONIC] = w[PXD_W_IONIC] * f[2] + w[PXD_W_IONIC + 1] * f[3];
+    d[PXD_W_COEF + PXD_TERM_PI_CATION] = pc;
+    d[PXD_W_COEF + PXD_TERM_F2F] = st[0];
+    d[PXD_W_COEF + PXD_TERM_E2F] = st[1];
+    d[PXD_W_COEF + PXD_TERM_HBOND] = w[PXD_W_HBOND_SCALE] * hb;
+    d[PXD_W_COEF + PXD_TERM_HYDROPHOBIC] = w[PXD_W_HYDRO_SCALE] * f[24];
+    d[PXD_W_COEF + PXD_TERM_TSTRAIN] = f[25];
+    d[PXD_W_COEF + PXD_TERM_ROTATABLE] = f[26];
+    d[PXD_W_VDW_SCALE] = w[PXD_W_COEF + PXD_TERM_VDW] * f[1];
+    d[PXD_W_HYDRO_SCALE] = w[PXD_W_COEF + PXD_TERM_HYDROPHOBIC] * f[24];
+    d[PXD_W_HBOND_SCALE] = w[PXD_W_COEF + PXD_TERM_HBOND] * hb;
+    for (int k = 0; k < 2; ++k) d[PXD_W_IONIC + k] = w[PXD_W_COEF + PXD_TERM_IONIC] * f[2 + k];
+    for (int k = 0; k < 4; ++k) d[PXD_W_PICAT + k] = w[PXD_W_COEF + PXD_TERM_PI_CATION] * f[4 + k];
+    for (int q = 0; q < 2; ++q)
+        for (int k = 0; k < 4; ++k) d[PXD_W_STACK + 4 * q + k] = w[PXD_W_COEF + PXD_TERM_F2F + q] * f[8 + 4 * q + k];
+    for (int k = 0; k < 8; ++k) d[PXD_W_HBOND + k] = w[PXD_W_COEF + PXD_TERM_HBOND] * w[PXD_W_HBOND_SCALE] * f[16 + k];
+    for (int k = 0; k < PXD_NUM_SF_WEIGHTS; ++k) dw[k] += g * d[k];
+}
+
+/* pi_stacking_batch::calculate for one ring pair; adds s * d(value) to glc / gln */
+static double stack_pair_diff(const double* rc, const double* rn, const double* lc, const double* ln, const double* p,
+                              double center, double s, double* glc, double* gln) {
+    double t[3], t2[3];
+    v_sub(lc, rc, t);
+    const double dist = v_norm(t);
+    if (dist > p[1]) return 0.0;
+    const double D = ramp_down(dist, p[0], p[1]);
+    const double dp1 = v_dot(rn, t);
+    const double s1 = sqrt(v_sqsum(t) - dp1 * dp1);
+    v_sub(rc, lc, t2);
+    const double dp2 = v_dot(ln, t2);
+    const double s2 = sqrt(v_sqsum(t2) - dp2 * dp2);
+    const int first = s1 < s2;
+    const double sg = first ? s1 : s2;
+    if (sg > p[5]) return 0.0;
+    const double SG = ramp_down(sg, p[4], p[5]);
+    const double c = clampd(v_dot(rn, ln), -1.0, 1.0);
+    double th = acos(c) / kPi * 180.0, sign = 1.0;
+    if (180.0 - th < th) {
+        th = 180.0 - th;
+        sign = -1.0;
+    }
+    double dTH;
+    const double TH = ramp_c_vd(th, center, p[2], p[3], &dTH);
+    if (glc && s != 0.0) {
+        const double dD = ramp_down_d(dist, p[0], p[1]), dSG = ramp_down_d(sg, p[4], p[5]);
+        double g_lc[3] = {0, 0, 0}, g_ln[3] = {0, 0, 0};
+        if (dD != 0.0 && dist > 0.0)
+            for (int d = 0; d < 3; ++d) g_lc[d] += t[d] * dD * SG * TH / dist;
+        if (dSG != 0.0 && sg > 0.0) {
+            const double k = D * dSG * TH / sg;
+            for (int d = 0; d < 3; ++d) {
+                if (first) {
+                    g_lc[d] += (t[d] - rn[d] * dp1) * k;
+                } else {
+                    g_lc[d] -= (t2[d] - ln[d] * dp2) * k;
+                    g_ln[d] -= t2[d] * dp2 * k;
+                }
+            }
+        }
+        const double dot = v_dot(rn, ln);
+        if (dTH != 0.0 && dot > -1.0 && dot < 1.0) {
+            const double dth_dc = -(180.0 / kPi) / sqrt(1.0 - c * c);
+            for (int d = 0; d < 3; ++d) g_ln[d] += rn[d] * D * SG * dTH * sign * dth_dc;
+        }
+        for (int d = 0; d < 3; ++d) {
+            glc[d] -= s * g_lc[d];
+            gln[d] -= s * g_ln[d];
+        }
+    }
+    return -D * SG * TH;
+}
+
+/* hbond_interactions_ga_tuning_param::calculate for one pair; adds s * d(value) */
+static double hbond_pair_diff(const double* dpos, const double* hpos, const double* apos, const double* p, double s,
+                              double* gd, double* gh, double* ga) {
+    double ha[3], u[3], v[3];
+    v_sub(hpos, apos, ha);
+    const double D = v_norm(ha);
+    double ddd;
+    const double dd = ramp_c_vd(D, p[4], p[0], p[1], &ddd);
+    if (dd < EPS) return 0.0;
+    v_sub(dpos, hpos, u);
+    v_sub(apos, hpos, v);
+    const double lu = v_norm(u), lv = v_norm(v), L = lu * lv + EPS, uv = v_dot(u, v);
+    const double cr = uv / L;
+    const double c = clampd(cr, -1.0, 1.0);
+    const double ang = acos(c) / kPi * 180.0;
+    double dAR;
+    const double AR = ramp_c_vd(ang, p[5], p[2], p[3], &dAR);
+    if (gh && s != 0.0) {
+        if (ddd != 0.0 && D > 0.0)
+            for (int d = 0; d < 3; ++d) {
+                const double g = -s * ddd * AR / D * ha[d];
+                gh[d] += g;
+                ga[d] -= g;
+            }
+        if (dAR != 0.0 && cr > -1.0 && cr < 1.0 && lu > 0.0 && lv > 0.0) {
+            const double k = -s * dd * dAR * (-(180.0 / kPi) / sqrt(1.0 - c * c));
+            for (int d = 0; d < 3; ++d) {
+                const double dcu = v[d] / L - u[d] * uv * lv / (lu * L * L);
+                const double dcv = u[d] / L - v[d] * uv * lu / (lv * L * L);
+                gd[d] += k * dcu;
+                ga[d] += k * dcv;
+                gh[d] -= k * (dcu + dcv);
+            }
+        }
+    }
+    return -dd * AR;
+}
+
+double po_score_diff(const pxd_sf_params* sf, int n_rec, const double* rec_xyz, const double* rec_q,
+                     const double* rec_sigma, const double* rec_eps, const pxd_score_lists* rl, int n_lig,
+                     const double* x, const double* lig_q, const int32_t* lig_type, const pxd_score_lists* ll,
+                     const double* w, const double* table, double g, double* f, double* G, double* dw, double* dtab) {
+    double fl[PXD_NUM_SCORE_FEATURES] = {0};
+    const double s_coul = g * w[PXD_W_COEF + PXD_TERM_COULOMB] * kCoulomb;
+    const double s_vdw = g * w[PXD_W_COEF + PXD_TERM_VDW] * w[PXD_W_VDW_SCALE];
+    const int use_tab = table && rl->atomic_numbers && ll->atomic_numbers;
+    /* Coulomb, clamped LJ (scorer.cpp:222-276) and the pair table */
+    for (int i = 0; i < n_lig; ++i) {
+        const int t = lig_type[i];
+        const double s1 = PXD_VDW_SIGMA[t] * sf->vdw_sigma_scale[t];
+        const double e1 = PXD_VDW_EPSILON[t] * sf->vdw_epsilon_scale[t];
+        const int ci = use_tab ? pair_class_d(0, ll->atomic_numbers[i]) : -1;
+        for (int j = 0; j < n_rec; ++j) {
+            double dv[3];
+            v_sub(x + 3 * i, rec_xyz + 3 * j, dv);
+            const double d = v_norm(dv);
+            const double rinv = 1.0 / (d + EPS);
+            fl[0] += lig_q[i] * rec_q[j] * rinv * kCoulomb;
+            const double u6 = pow((s1 + rec_sigma[j]) * 0.5 * rinv, 6.0);
+            const double fused = sqrt(e1 * rec_eps[j]) * 4.0;
+            const double v = (u6 * u6 - u6) * fused;
+            fl[1] += clampd(v, -sf->vdw_cutoff, sf->vdw_cutoff);
+            double de_dd = -s_coul * lig_q[i] * rec_q[j] * rinv * rinv;
+            if (v <= sf->vdw_cutoff && v >= -sf->vdw_cutoff) de_dd -= s_vdw * fused * rinv * (12.0 * u6 * u6 - 6.0 * u6);
+            const int cj = ci >= 0 ? pair_class_d(1, rl->atomic_numbers[j]) : -1;
+            const double tt = d / PXD_PAIR_BIN_WIDTH;
+            if (cj >= 0 && tt < PXD_PAIR_BINS - 1) {
+                const int b = (int)tt;
+                const double fr = tt - b;
+                const int p = (4 * ci + cj) * PXD_PAIR_BINS + b;
+                fl[27] += table[p] + fr * (table[p + 1] - table[p]);
+                de_dd += g * (table[p + 1] - table[p]) / PXD_PAIR_BIN_WIDTH;
+                if (dtab) {
+                    dtab[p] += g * (1.0 - fr);
+                    dtab[p + 1] += g * fr;
+                }
+            }
+            if (d > 0.0) gacc(G, i, dv, de_dd / d);
+        }
+    }
+    /* hydrophobic (scorer.cpp:278-311) */
+    {
+        const double sh = g * w[PXD_W_COEF + PXD_TERM_HYDROPHOBIC] * w[PXD_W_HYDRO_SCALE];
+        for (int a = 0; a < ll->n_hydrophobic; ++a) {
+            const int i = ll->hydrophobic[a];
+            const double s1 = PXD_VDW_SIGMA[lig_type[i]];
+            for (int b = 0; b < rl->n_hydrophobic; ++b) {
+                const int j = rl->hydrophobic[b];
+                const double r1 = (s1 + rec_sigma[j]) * sf->hydro_scale_factor + sf->hydro_dist_min;
+                const double r2 = r1 + sf->hydro_dist_max;
+                double dv[3];
+                v_sub(x + 3 * i, rec_xyz + 3 * j, dv);
+                const double d = v_norm(dv);
+                fl[24] -= ramp_down(d, r1, r2);
+                if (d > 0.0) gacc(G, i, dv, -sh * ramp_down_d(d, r1, r2) / d);
+            }
+        }
+    }
+    /* ionic (scorer.cpp:313-368) */
+    for (int k = 0; k < 2; ++k) {
+        const double sk = g * w[PXD_W_COEF + PXD_TERM_IONIC] * w[PXD_W_IONIC + k];
+        const int na = k == 0 ? ll->n_cation : ll->n_anion;
+        const int32_t* la = k == 0 ? ll->cation : ll->anion;
+        const int nb = k == 0 ? rl->n_anion : rl->n_cation;
+        const int32_t* rb = k == 0 ? rl->anion : rl->cation;
+        for (int a = 0; a < na; ++a)
+            for (int b = 0; b < nb; ++b) {
+                double dv[3];
+                v_sub(x + 3 * la[a], rec_xyz + 3 * rb[b], dv);
+                const double d = v_norm(dv);
+                fl[2 + k] -= ramp_down(d, sf->ionic[k][0], sf->ionic[k][1]);
+                if (d > 0.0) gacc(G, la[a], dv, -sk * ramp_down_d(d, sf->ionic[k][0], sf->ionic[k][1]) / d);
+            }
+    }
+    /* cation-pi (scorer.cpp:370-462) */
+    for (int k = 0; k < 2; ++k) {
+        const double sk = g * w[PXD_W_COEF + PXD_TERM_PI_CATION] * w[PXD_W_PICAT + k];
+        const int nr = k == 0 ? rl->n_ring5 : rl->n_ring6;
+        const int32_t* rr = k == 0 ? rl->ring5 : rl->ring6;
+        for (int r = 0; r < nr; ++r) {
+            double c[3];
+            ring_centroid(rec_xyz, rr + 6 * r, c);
+            for (int a = 0; a < ll->n_cation; ++a) {
+                const int i = ll->cation[a];
+                double dv[3];
+                v_sub(x + 3 * i, c, dv);
+                const double d = v_norm(dv);
+                fl[4 + k] -= ramp_down(d, sf->picat[k][0], sf->picat[k][1]);
+                if (d > 0.0) gacc(G, i, dv, -sk * ramp_down_d(d, sf->picat[k][0], sf->picat[k][1]) / d);
+            }
+        }
+    }
+    for (int k = 2; k < 4; ++k) {
+        const double sk = g * w[PXD_W_COEF + PXD_TERM_PI_CATION] * w[PXD_W_PICAT + k];
+        const int nr = k == 2 ? ll->n_ring5 : ll->n_ring6;
+        const int32_t* lr = k == 2 ? ll->ring5 : ll->ring6;
+        for (int r = 0; r < nr; ++r) {
+            double c[3], gc[3] = {0, 0, 0}, zero[3] = {0, 0, 0};
+            ring_centroid(x, lr + 6 * r, c);
+            for (int b = 0; b < rl->n_cation; ++b) {
+                double dv[3];
+                v_sub(c, rec_xyz + 3 * rl->cation[b], dv);
+                const double d = v_norm(dv);
+                fl[4 + k] -= ramp_down(d, sf->picat[k][0], sf->picat[k][1]);
+                if (d > 0.0) {
+                    const double q = -sk * ramp_down_d(d, sf->picat[k][0], sf->picat[k][1]) / d;
+                    for (int u = 0; u < 3; ++u) gc[u] += q * dv[u];
+                }
+            }
+            ring_backward(x, lr + 6 * r, gc, zero, G);
+        }
+    }
+    /* pi stacking (scorer.cpp:638-724) */
+    for (int q = 0; q < 2; ++q) {
+        const double center = q == 0 ? 0.0 : 90.0;
+        for (int lk = 0; lk < 2; ++lk) {      /* ligand ring5, ring6 */
+            const int nlr = lk == 0 ? ll->n_ring5 : ll->n_ring6;
+            const int32_t* lr = lk == 0 ? ll->ring5 : ll->ring6;
+            for (int j = 0; j < nlr; ++j) {
+                double lc[3], ln[3], glc[3] = {0, 0, 0}, gln[3] = {0, 0, 0};
+                ring_centroid(x, lr + 6 * j, lc);
+                ring_normal(x, lr + 6 * j, ln);
+                for (int rk = 0; rk < 2; ++rk) {  /* receptor ring5, ring6 */
+                    const int k = 2 * lk + rk;     /* l5r5 l5r6 l6r5 l6r6 */
+                    const double sk = g * w[PXD_W_COEF + PXD_TERM_F2F + q] * w[PXD_W_STACK + 4 * q + k];
+                    const int nrr = rk == 0 ? rl->n_ring5 : rl->n_ring6;
+                    const int32_t* rr = rk == 0 ? rl->ring5 : rl->ring6;
+                    for (int i = 0; i < nrr; ++i) {
+                        double rc[3], rn[3];
+                        ring_centroid(rec_xyz, rr + 6 * i, rc);
+                        ring_normal(rec_xyz, rr + 6 * i, rn);
+                        fl[8 + 4 * q + k] +=
+                            stack_pair_diff(rc, rn, lc, ln, sf->stack[q][k], center, sk, G ? glc : NULL, gln);
+                    }
+                }
+                ring_backward(x, lr + 6 * j, glc, gln, G);
+            }
+        }
+    }
+    /* hydrogen bonds (scorer.cpp:464-577) */
+    {
+        const double shb = g * w[PXD_W_COEF + PXD_TERM_HBOND] * w[PXD_W_HBOND_SCALE];
+        for (int c = 0; c < 2; ++c) {  /* ligand donors x receptor acceptors */
+            const int nd = c == 0 ? ll->n_don_charged : ll->n_don_neutral;
+            const int32_t* dl = c == 0 ? ll->don_charged : ll->don_neutral;
+            for (int a = 0; a < nd; ++a) {
+                double gd[3] = {0, 0, 0}, gh[3] = {0, 0, 0}, gx[3] = {0, 0, 0};
+                for (int u = 0; u < 2; ++u) {
+                    const int na = u == 0 ? rl->n_acc_charged : rl->n_acc_neutral;
+                    const int32_t* al = u == 0 ? rl->acc_charged : rl->acc_neutral;
+                    const int k = 2 * c + u;
+                    for (int b = 0; b < na; ++b)
+                        fl[16 + k] += hbond_pair_diff(x + 3 * dl[2 * a], x + 3 * dl[2 * a + 1], rec_xyz + 3 * al[b],
+                                                      sf->hbond[k], shb * w[PXD_W_HBOND + k], gd, gh, gx);
+                }
+                gacc(G, dl[2 * a], gd, 1.0);
+                gacc(G, dl[2 * a + 1], gh, 1.0);
+            }
+        }
+        for (int u = 0; u < 2; ++u) {  /* ligand acceptors x receptor donors */
+            const int na = u == 0 ? ll->n_acc_charged : ll->n_acc_neutral;
+            const int32_t* al = u == 0 ? ll->acc_charged : ll->acc_neutral;
+            for (int a = 0; a < na; ++a) {
+                double ga[3] = {0, 0, 0}, gd[3] = {0, 0, 0}, gh[3] = {0, 0, 0};
+                for (int c = 0; c < 2; ++c) {
+                    const int nd = c == 0 ? rl->n_don_charged : rl->n_don_neutral;
+                    const int32_t* dl = c == 0 ? rl->don_charged : rl->don_neutral;
+                    const int k = 4 + 2 * c + u;
+                    for (int b = 0; b < nd; ++b)
+                        fl[16 + k] += hbond_pair_diff(rec_xyz + 3 * dl[2 * b], rec_xyz + 3 * dl[2 * b + 1], x + 3 * al[a],
+                                                      sf->hbond[k], shb * w[PXD_W_HBOND + k], gd, gh, ga);
+                }
+                gacc(G, al[a], ga, 1.0);
+            }
+        }
+    }
+    /* torsion strain (scorer.cpp:579-613) */
+    {
+        static const double per[4] = {1.0, 2.0, 3.0, 4.0};
+        static const double ph[4] = {0.0, 3.141592653589793, 0.0, 3.141592653589793};
+        const double sts = g * w[PXD_W_COEF + PXD_TERM_TSTRAIN];
+        for (int e = 0; e < ll->n_tstrain; ++e) {
+            const double* co = ll->tstrain_coefs + 4 * e;
+            int cnt = 0;
+            for (int q = ll->tstrain_offsets[e]; q < ll->tstrain_offsets[e + 1]; ++q) {
+                if (ll->tstrain_quads[4 * q] == ll->tstrain_quads[4 * q + 1]) break;
+                ++cnt;
+            }
+            if (cnt == 0) continue;
+            double tmp = 0.0;
+            for (int j = 0; j < cnt; ++j) {
+                const int32_t* a = ll->tstrain_quads + 4 * (ll->tstrain_offsets[e] + j);
+                double gi[3], gj[3], gk[3], gl[3];
+                const double th = po_dihedral_and_gradient(x + 3 * a[0], x + 3 * a[1], x + 3 * a[2], x + 3 * a[3],
+                                                           gi, gj, gk, gl);
+                double df = 0.0;
+                for (int m = 0; m < 4; ++m) {
+                    tmp += (1 + cos(th * per[m] - ph[m])) * co[m];
+                    df -= per[m] * sin(th * per[m] - ph[m]) * co[m];
+                }
+                const double k = sts * df / cnt;
+                gacc(G, a[0], gi, k);
+                gacc(G, a[1], gj, k);
+                gacc(G, a[2], gk, k);
+                gacc(G, a[3], gl, k);
+            }
+            fl[25] += tmp / cnt;
+        }
+    }
+    fl[26] = -1.0 / (2.620643 + ll->n_rotatable);
+    if (f) memcpy(f, fl, sizeof(fl));
+    if (dw) po_combine_grad(w, fl, g, dw);
+    return po_combine_features(w, fl);
+}

@@ -76,6 +76,18 @@ double po_gbsa_parts(int n_rec, const double* rec_xyz, const double* rec_q,
                      const pxd_score_lists* rec_l, int n_lig, const double* lig_xyz,
                      const double* lig_q, const pxd_score_lists* lig_l, double* parts);
 
+/* ---- differentiable empirical score (no reference counterpart; see pxd_score_adjoint) ----
+ * Features [PXD_NUM_SCORE_FEATURES], S = po_combine_features(w, f), and, with g = dL/dS:
+ * G [n_lig][3] += g dS/dx, dw [36] += g dS/dw, dtab [32*256] += g dS/dT (each may be NULL;
+ * table NULL: no pair-table term; the table needs atomic_numbers in both lists). */
+double po_score_diff(const pxd_sf_params* sf, int n_rec, const double* rec_xyz, const double* rec_q,
+                     const double* rec_sigma, const double* rec_eps, const pxd_score_lists* rec_l,
+                     int n_lig, const double* lig_xyz, const double* lig_q, const int32_t* lig_type,
+                     const pxd_score_lists* lig_l, const double* weights, const double* table, double g,
+                     double* features, double* dxyz, double* dweights, double* dtable);
+double po_combine_features(const double* weights, const double* features);
+void po_combine_grad(const double* weights, const double* features, double g, double* dweights);
+
 /* ---- Monte-Carlo walker (engine/src/core/searcher.cpp:46-223) ---- */
 int po_mc_walker(po_system* s, const pxd_sf_params* sf, const pxd_score_lists* rl,
                  const pxd_score_lists* ll, const double* lo, const double* hi, uint32_t seed,

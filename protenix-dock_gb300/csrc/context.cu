@@ -415,21 +415,6 @@ int refresh_ligand_slots(pxd_context* ctx) {
 
 using namespace pxd;
 
-// Host-buffer wrappers stage their arrays in stream-ordered device allocations.
-struct Staging {
-    pxd_context* ctx;
-    std::vector<void*> dev;
-    ~Staging() {
-        for (void* p : dev) cudaFreeAsync(p, ctx->stream);
-    }
-    template <class T>
-    T* alloc(size_t n, int* rc) {
-        void* p = nullptr;
-        *rc = cuda_check(ctx, cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T), ctx->stream), "staging");
-        if (!*rc) dev.push_back(p);
-        return static_cast<T*>(p);
-    }
-};
 
 
 extern "C" {

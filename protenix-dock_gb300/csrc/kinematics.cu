@@ -20,10 +20,22 @@ struct LigKinArgs {
     int n_poses;
     const float* xyz_in;   // [N][3] reference pose (atom order)
     const float* centers;  // [P][3]
-    const float* rots;     // [P][9]
+    const float* rots;     // [P][9] (when quats is NULL)
     const float* tors;     // [P][T]
     float* out;            // [P][N][3]
+    const float* quats;    // [P][4] (w, x, y, z) or NULL
 };
+
+// Rotation of the normalised quaternion q (get_rotation_matrix, math.cpp:22-42).
+__device__ __forceinline__ Mat3 quat_rotation(const float* q4) {
+    const float inv = rsqrtf(q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
+    const float a = q4[0] * inv, b = q4[1] * inv, c = q4[2] * inv, d = q4[3] * inv;
+    Mat3 m;
+    m.r0 = make_float3(a * a + b * b - c * c - d * d, 2.f * (b * c - a * d), 2.f * (a * c + b * d));
+    m.r1 = make_float3(2.f * (a * d + b * c), a * a - b * b + c * c - d * d, 2.f * (c * d - a * b));
+    m.r2 = make_float3(2.f * (b * d - a * c), 2.f * (a * b + c * d), a * a - b * b - c * c + d * d);
+    return m;
+}
 
 __global__ void __launch_bounds__(kKinWarps * kWarp) ligand_kinematics_kernel(const LigKinArgs a) {
     __shared__ float4 s_c[kKinWarps][PXD_MAX_LIGAND_ATOMS];
@@ -53,11 +65,15 @@ __global__ void __launch_bounds__(kKinWarps * kWarp) ligand_kinematics_kernel(co
             c[p] = make_float4(a.xyz_in[3 * atom], a.xyz_in[3 * atom + 1], a.xyz_in[3 * atom + 2], 0.f);
         }
         __syncwarp();
-        const float* r = a.rots + 9 * static_cast<size_t>(pose);
         Mat3 rot;
-        rot.r0 = make_float3(r[0], r[1], r[2]);
-        rot.r1 = make_float3(r[3], r[4], r[5]);
-        rot.r2 = make_float3(r[6], r[7], r[8]);
+        if (a.quats) {
+            rot = quat_rotation(a.quats + 4 * static_cast<size_t>(pose));
+        } else {
+            const float* r = a.rots + 9 * static_cast<size_t>(pose);
+            rot.r0 = make_float3(r[0], r[1], r[2]);
+            rot.r1 = make_float3(r[3], r[4], r[5]);
+            rot.r2 = make_float3(r[6], r[7], r[8]);
+        }
         const float* cc = a.centers + 3 * static_cast<size_t>(pose);
         ligand_forward(L, c, s_frag, s_mine, s_parent, make_float3(cc[0], cc[1], cc[2]), rot,
                        a.tors + static_cast<size_t>(pose) * L.n_tors, s_ks[w], lane);
@@ -78,7 +94,20 @@ int launch_ligand_kinematics(pxd_context* ctx, int lig, int n_poses, const float
     const DevLigand& L = ctx->ligands[lig].dev;
     if (L.n_frags > kMaxFrags) return set_error(ctx, PXD_ERR_INVALID, "too many fragments");
     if (L.n_tors > kWarp) return set_error(ctx, PXD_ERR_INVALID, "more than 32 torsions");
-    LigKinArgs a{L, n_poses, xyz_in, centers, rots, tors, xyz_out};
+    LigKinArgs a{L, n_poses, xyz_in, centers, rots, tors, xyz_out, nullptr};
+    int blocks = (n_poses + kKinWarps - 1) / kKinWarps;
+    if (blocks > ctx->n_sm * 8) blocks = ctx->n_sm * 8;
+    if (blocks < 1) blocks = 1;
+    ligand_kinematics_kernel<<<blocks, kKinWarps * kWarp, 0, s>>>(a);
+    return cuda_check(ctx, cudaGetLastError(), "ligand_kinematics_kernel launch");
+}
+
+int launch_ligand_pose(pxd_context* ctx, int lig, int n_poses, const float* xyz_in, const float* centers,
+                       const float* quats, const float* tors, float* xyz_out, cudaStream_t s) {
+    const DevLigand& L = ctx->ligands[lig].dev;
+    if (L.n_frags > kMaxFrags) return set_error(ctx, PXD_ERR_INVALID, "too many fragments");
+    if (L.n_tors > kWarp) return set_error(ctx, PXD_ERR_INVALID, "more than 32 torsions");
+    LigKinArgs a{L, n_poses, xyz_in, centers, nullptr, tors, xyz_out, quats};
     int blocks = (n_poses + kKinWarps - 1) / kKinWarps;
     if (blocks > ctx->n_sm * 8) blocks = ctx->n_sm * 8;
     if (blocks < 1) blocks = 1;
@@ -158,6 +187,8 @@ struct LigBackArgs {
     float* out_center;     // [P][3]
     float* out_torque;     // [P][3]
     float* out_tors;       // [P][T]
+    const float* quats;    // [P][4] orientation used by the forward map, or NULL
+    float* out_quat;       // [P][4] dE/dq through the normalisation (with quats)
 };
 
 __global__ void __launch_bounds__(kKinWarps * kWarp) ligand_backward_kernel(const LigBackArgs a) {
@@ -210,13 +241,33 @@ __global__ void __launch_bounds__(kKinWarps * kWarp) ligand_backward_kernel(cons
                 s_t[w][q.y] = add3(s_t[w][q.y], st);
             }
             float* oc = a.out_center + 3 * static_cast<size_t>(pose);
-            float* oq = a.out_torque + 3 * static_cast<size_t>(pose);
             oc[0] = ftot.x;
             oc[1] = ftot.y;
             oc[2] = ftot.z;
-            oq[0] = ttot.x;
-            oq[1] = ttot.y;
-            oq[2] = ttot.z;
+            if (a.out_torque) {
+                float* oq = a.out_torque + 3 * static_cast<size_t>(pose);
+                oq[0] = ttot.x;
+                oq[1] = ttot.y;
+                oq[2] = ttot.z;
+            }
+            if (a.out_quat) {
+                // A perturbation dq of the unit quaternion (w, v) turns the pose by the
+                // rotation vector 2 vec(dq q*) = 2 (w dv - dw v + v x dv), so with torque t
+                // dE/dw = -2 t.v and dE/dv = 2 (w t + t x v); the normalisation projects
+                // out the radial part and divides by |q|.
+                const float* q4 = a.quats + 4 * static_cast<size_t>(pose);
+                const float len = sqrtf(q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
+                const float w = q4[0] / len;
+                const float3 v = make_float3(q4[1] / len, q4[2] / len, q4[3] / len);
+                const float gw = -2.f * dot3(ttot, v);
+                const float3 gv = mul3(add3(mul3(ttot, w), cross3(ttot, v)), 2.f);
+                const float radial = gw * w + dot3(gv, v);
+                float* og = a.out_quat + 4 * static_cast<size_t>(pose);
+                og[0] = (gw - radial * w) / len;
+                og[1] = (gv.x - radial * v.x) / len;
+                og[2] = (gv.y - radial * v.y) / len;
+                og[3] = (gv.z - radial * v.z) / len;
+            }
         }
         __syncwarp();
     }
@@ -227,7 +278,20 @@ int launch_ligand_backward(pxd_context* ctx, int lig, int n_poses, const float* 
                            cudaStream_t s) {
     const DevLigand& L = ctx->ligands[lig].dev;
     if (L.n_frags > kMaxFrags) return set_error(ctx, PXD_ERR_INVALID, "too many fragments");
-    LigBackArgs a{L, n_poses, xyz, centers, grad, out_center, out_torque, out_tors};
+    LigBackArgs a{L, n_poses, xyz, centers, grad, out_center, out_torque, out_tors, nullptr, nullptr};
+    int blocks = (n_poses + kKinWarps - 1) / kKinWarps;
+    if (blocks > ctx->n_sm * 8) blocks = ctx->n_sm * 8;
+    if (blocks < 1) blocks = 1;
+    ligand_backward_kernel<<<blocks, kKinWarps * kWarp, 0, s>>>(a);
+    return cuda_check(ctx, cudaGetLastError(), "ligand_backward_kernel launch");
+}
+
+int launch_ligand_pose_backward(pxd_context* ctx, int lig, int n_poses, const float* xyz, const float* centers,
+                                const float* quats, const float* grad, float* out_center, float* out_quat,
+                                float* out_tors, cudaStream_t s) {
+    const DevLigand& L = ctx->ligands[lig].dev;
+    if (L.n_frags > kMaxFrags) return set_error(ctx, PXD_ERR_INVALID, "too many fragments");
+    LigBackArgs a{L, n_poses, xyz, centers, grad, out_center, nullptr, out_tors, quats, out_quat};
     int blocks = (n_poses + kKinWarps - 1) / kKinWarps;
     if (blocks > ctx->n_sm * 8) blocks = ctx->n_sm * 8;
     if (blocks < 1) blocks = 1;

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -68,6 +69,7 @@ struct DevRecScore {
     const int2* donn;
     const int* accc;
     const int* accn;
+    const int* pclass;         // [n_all] pair-table class (C N O other: 0-3), -1 none; NULL: no table term
 };
 
 struct DevLigScore {
@@ -85,6 +87,7 @@ struct DevLigScore {
     const float4* ts_coef;     // torsion-strain coefficients
     const int2* ts_range;      // quads [first, first + count)
     const int4* ts_quad;
+    const int* pclass;         // [N] 4 * pair-table class (C N O S P F Cl other), -1 none; NULL: no table term
 };
 
 struct DevLigand {
@@ -228,9 +231,31 @@ int launch_ligand_backward(pxd_context* ctx, int lig, int n_poses, const float* 
                            cudaStream_t s);
 int launch_receptor_kinematics(pxd_context* ctx, int n_poses, const float* tors, float* out,
                                cudaStream_t s);
+int launch_ligand_pose(pxd_context* ctx, int lig, int n_poses, const float* xyz_in, const float* centers,
+                       const float* quats, const float* tors, float* xyz_out, cudaStream_t s);
+int launch_ligand_pose_backward(pxd_context* ctx, int lig, int n_poses, const float* xyz, const float* centers,
+                                const float* quats, const float* grad, float* out_center, float* out_quat,
+                                float* out_tors, cudaStream_t s);
+int pair_class(int is_receptor, int z);
 int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l);
 int upload_ligand_scoring(pxd_context* ctx, LigandEntry& e, const pxd_score_lists* l);
 void gbsa_properties(const pxd_score_lists* l, int n, std::vector<double>& radius,
                      std::vector<double>& screen);
+
+// Host-buffer wrappers stage their arrays in stream-ordered device allocations.
+struct Staging {
+    pxd_context* ctx;
+    std::vector<void*> dev;
+    ~Staging() {
+        for (void* p : dev) cudaFreeAsync(p, ctx->stream);
+    }
+    template <class T>
+    T* alloc(size_t n, int* rc) {
+        void* p = nullptr;
+        *rc = cuda_check(ctx, cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T), ctx->stream), "staging");
+        if (!*rc) dev.push_back(p);
+        return static_cast<T*>(p);
+    }
+};
 
 }  // namespace pxd

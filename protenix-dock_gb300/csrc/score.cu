@@ -61,6 +61,37 @@ void gbsa_properties(const pxd_score_lists* l, int n, std::vector<double>& radiu
     }
 }
 
+// Pair-table class of an atom: ligand C N O S P F Cl other-heavy (0-7), receptor
+// C N O other-heavy (0-3); hydrogens (and unknown elements, Z < 2) take none (-1).
+int pair_class(int is_receptor, int z) {
+    if (z < 2) return -1;
+    switch (z) {
+        case 6: return 0;
+        case 7: return 1;
+        case 8: return 2;
+        default: break;
+    }
+    if (is_receptor) return 3;
+    switch (z) {
+        case 16: return 3;
+        case 15: return 4;
+        case 9: return 5;
+        case 17: return 6;
+        default: return 7;
+    }
+}
+
+static std::vector<int> pair_classes(const pxd_score_lists* l, int n, int is_receptor) {
+    std::vector<int> c;
+    if (!l || !l->atomic_numbers) return c;
+    c.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const int k = pair_class(is_receptor, l->atomic_numbers[i]);
+        c[i] = k < 0 ? -1 : (is_receptor ? k : 4 * k);
+    }
+    return c;
+}
+
 static bool ids_ok(const int32_t* p, int n, int limit) {
     for (int i = 0; i < n; ++i)
         if (p[i] < 0 || p[i] >= limit) return false;
@@ -144,6 +175,8 @@ int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l) {
     const size_t o_donn = pk.put(pairs2(l->don_neutral, l->n_don_neutral));
     const size_t o_accc = pk.put(ints(l->acc_charged, l->n_acc_charged));
     const size_t o_accn = pk.put(ints(l->acc_neutral, l->n_acc_neutral));
+    const std::vector<int> pcls = pair_classes(l, M, 1);
+    const size_t o_pcl = pk.put(pcls);
     int rc_ = cuda_check(ctx, cudaMalloc(&ctx->rec_score_mem, pk.bytes.size()), "receptor score lists");
     if (rc_) return rc_;
     rc_ = cuda_check(ctx, cudaMemcpy(ctx->rec_score_mem, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice),
@@ -171,6 +204,7 @@ int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l) {
     d.donn = at<int2>(b, o_donn);
     d.accc = at<int>(b, o_accc);
     d.accn = at<int>(b, o_accn);
+    d.pclass = pcls.empty() ? nullptr : at<int>(b, o_pcl);
     return PXD_OK;
 }
 
@@ -208,6 +242,8 @@ int upload_ligand_scoring(pxd_context* ctx, LigandEntry& e, const pxd_score_list
     const size_t o_accc = pk.put(ints(l->acc_charged, l->n_acc_charged));
     const size_t o_accn = pk.put(ints(l->acc_neutral, l->n_acc_neutral));
     const size_t o_tsc = pk.put(tsc), o_tsr = pk.put(tsr), o_tsq = pk.put(tsq);
+    const std::vector<int> pcls = pair_classes(l, e.n_atoms, 0);
+    const size_t o_pcl = pk.put(pcls);
     void* b = nullptr;
     int rc = cuda_check(ctx, cudaMalloc(&b, pk.bytes.size()), "ligand score lists");
     if (rc) return rc;
@@ -242,6 +278,7 @@ int upload_ligand_scoring(pxd_context* ctx, LigandEntry& e, const pxd_score_list
     d.ts_coef = at<float4>(b, o_tsc);
     d.ts_range = at<int2>(b, o_tsr);
     d.ts_quad = at<int4>(b, o_tsq);
+    d.pclass = pcls.empty() ? nullptr : at<int>(b, o_pcl);
     return PXD_OK;
 }
 

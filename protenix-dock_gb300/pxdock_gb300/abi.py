@@ -194,3 +194,41 @@ TERM_NAMES = ["InteractionCoulomb_oriEnergy", "InteractionVDW_Energy", "Ionic_En
               "Pi_Cationic_Energy", "F2FPiStacking_Energy", "E2FPiStacking_Energy",
               "Hbond_Energy", "Hydrophobic_Energy", "TorsionStrain_Penalty", "rotatable_energy",
               "Gbsa_Com_Energy-Gbsa_Lig_Energy-Gbsa_Pro_Energy"]
+
+# Differentiable empirical score (pxd_score_adjoint): weight vector layout, feature
+# count and pair-table shape, as in include/pxdock_gb300.h.
+NUM_SF_WEIGHTS = 36
+NUM_SCORE_FEATURES = 28
+PAIR_TYPES, PAIR_BINS, PAIR_BIN_WIDTH = 32, 256, 0.03125
+W_COEF, W_VDW_SCALE, W_HYDRO_SCALE, W_HBOND_SCALE = 0, 11, 12, 13
+W_IONIC, W_PICAT, W_STACK, W_HBOND = 14, 16, 20, 28
+
+
+def sf_weights(sf):
+    """The 36 weights of a scoring function in pxd_sf_weight order (pxd_sf_weights)."""
+    import numpy as np
+    w = np.zeros(NUM_SF_WEIGHTS)
+    w[W_COEF:W_COEF + 11] = list(sf.coef)
+    w[W_VDW_SCALE], w[W_HYDRO_SCALE], w[W_HBOND_SCALE] = sf.vdw_scale, sf.hydro_scale, sf.hbond_scale
+    w[W_IONIC:W_IONIC + 2] = list(sf.ionic_coef)
+    w[W_PICAT:W_PICAT + 4] = list(sf.picat_coef)
+    w[W_STACK:W_STACK + 8] = [sf.stack_coef[q][k] for q in range(2) for k in range(4)]
+    w[W_HBOND:W_HBOND + 8] = list(sf.hbond_coef)
+    return w
+
+
+def smooth_pair_tables(seed=0):
+    """Seeded smooth pair tables [32][256] (FP32 values): a soft wall plus one well per
+    atom-type pair, zero at the cut-off."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    r = np.arange(PAIR_BINS) * PAIR_BIN_WIDTH
+    t = np.zeros((PAIR_TYPES, PAIR_BINS))
+    for p in range(PAIR_TYPES):
+        r0 = rng.uniform(3.2, 4.4)
+        depth = rng.uniform(0.05, 0.4)
+        width = rng.uniform(0.4, 0.9)
+        wall = 2.0 * np.exp(-(r - 1.0) / 0.35)
+        t[p] = wall - depth * np.exp(-((r - r0) / width) ** 2)
+        t[p] *= np.clip((r[-1] - r) / 1.0, 0.0, 1.0)  # taper to zero at the cut-off
+    return t.astype(np.float32).astype(np.float64)

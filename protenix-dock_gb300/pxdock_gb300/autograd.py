@@ -1,0 +1,138 @@
+"""torch.autograd bindings of the differentiable score and the pose kinematics.
+
+Each Function calls the library's hand-written kernels on the current torch stream:
+
+- ``empirical_score(ctx, lig_ids, xyz, weights, tables)``: per-pose empirical score
+  S(x; w, T) (pxd_score_adjoint_multi_dev, over one context or several in one launch).
+  Forward runs the value kernel; backward recomputes the pose inside the adjoint kernel
+  (no activations are stored besides the inputs) and returns dL/dx, dL/dw and dL/dT.
+- ``ligand_pose(ctx, lig, xyz_ref, centers, quats, torsions)``: torsion-tree forward
+  kinematics (pxd_ligand_pose_dev) with its backward (pxd_ligand_pose_backward_dev):
+  atom gradients become centre, quaternion and torsion gradients.
+- ``docking_energy(ctx, lig_ids, xyz)``: the docking objective (grid maps + intra-ligand
+  force field, pxd_score_grad_dev) with its analytic coordinate gradient; it has no
+  parameters.
+
+Torch is only the autograd and memory plumbing here; there is no torch fallback.
+"""
+import torch
+
+from . import abi, native
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def _stream():
+    """The current torch stream as a CUDA stream handle. torch's default stream has the
+    handle 0, which the library reads as "the context's own stream", so it is passed as
+    cudaStreamLegacy (1), the same legacy default stream."""
+    return torch.cuda.current_stream().cuda_stream or 1
+
+
+class _EmpiricalScore(torch.autograd.Function):
+    @staticmethod
+    def forward(fctx, xyz, weights, tables, pctxs, which, ctx_ids, lig_ids, rec_tors):
+        P, A, _ = xyz.shape
+        x = xyz.detach().to(torch.float32).contiguous()
+        w = weights.detach().to(torch.float64).contiguous()
+        t = None if tables is None else tables.detach().to(torch.float32).contiguous()
+        score = torch.empty(P, dtype=torch.float64, device=xyz.device)
+        native.score_adjoint_multi_dev(pctxs, which, P, A, _ptr(ctx_ids), _ptr(lig_ids), _ptr(x), _ptr(rec_tors),
+                                       _ptr(w), _ptr(t), None, _ptr(score), None, None, None, None, _stream())
+        empty = torch.empty(0, device=xyz.device)
+        fctx.save_for_backward(x, w, t if t is not None else empty, lig_ids,
+                               ctx_ids if ctx_ids is not None else empty, rec_tors if rec_tors is not None else empty)
+        fctx.meta = (pctxs, which, tables is not None, xyz.dtype, weights.dtype,
+                     None if tables is None else tables.dtype)
+        return score
+
+    @staticmethod
+    def backward(fctx, grad_score):
+        x, w, t, lig_ids, ctx_ids, rec_tors = fctx.saved_tensors
+        pctxs, which, has_tab, xdt, wdt, tdt = fctx.meta
+        P, A, _ = x.shape
+        g = grad_score.detach().to(torch.float64).contiguous()
+        dx = torch.empty_like(x)
+        dw = torch.zeros(abi.NUM_SF_WEIGHTS, dtype=torch.float64, device=x.device)
+        dt = torch.zeros(abi.PAIR_TYPES * abi.PAIR_BINS, dtype=torch.float64, device=x.device) if has_tab else None
+        native.score_adjoint_multi_dev(pctxs, which, P, A, _ptr(ctx_ids if ctx_ids.numel() else None), _ptr(lig_ids),
+                                       _ptr(x), _ptr(rec_tors if rec_tors.numel() else None), _ptr(w),
+                                       _ptr(t if has_tab else None), _ptr(g), None, None, _ptr(dx), _ptr(dw),
+                                       _ptr(dt), _stream())
+        gt = dt.view(abi.PAIR_TYPES, abi.PAIR_BINS).to(tdt) if has_tab else None
+        return dx.to(xdt), dw.to(wdt), gt, None, None, None, None, None
+
+
+def empirical_score(pctx, lig_ids, xyz, weights, tables=None, which=0, rec_tors=None, ctx_ids=None):
+    """S per pose [P] (float64) for poses xyz [P][max_atoms][3] of the ligands lig_ids
+    [P] (int32, device). pctx is one Context, or a list of Contexts with ctx_ids [P]
+    (int32, device) naming each pose's context (one launch over all of them). weights
+    [36]; tables [32][256] or None."""
+    pctxs = list(pctx) if isinstance(pctx, (list, tuple)) else [pctx]
+    if len(pctxs) > 1 and ctx_ids is None:
+        raise ValueError("ctx_ids is required with several contexts")
+    return _EmpiricalScore.apply(xyz, weights, tables, pctxs, which, ctx_ids if len(pctxs) > 1 else None, lig_ids,
+                                 rec_tors)
+
+
+class _LigandPose(torch.autograd.Function):
+    @staticmethod
+    def forward(fctx, centers, quats, torsions, pctx, lig, xyz_ref):
+        P = centers.shape[0]
+        N = xyz_ref.shape[0]
+        c = centers.detach().to(torch.float32).contiguous()
+        q = quats.detach().to(torch.float32).contiguous()
+        tq = torsions.detach().to(torch.float32).contiguous()
+        out = torch.empty((P, N, 3), dtype=torch.float32, device=centers.device)
+        pctx.ligand_pose_dev(lig, P, _ptr(xyz_ref), _ptr(c), _ptr(q), _ptr(tq) if tq.numel() else None, _ptr(out),
+                             _stream())
+        fctx.save_for_backward(out, c, q)
+        fctx.meta = (pctx, lig, centers.dtype, quats.dtype, torsions.dtype, torsions.shape[1])
+        return out
+
+    @staticmethod
+    def backward(fctx, grad_xyz):
+        out, c, q = fctx.saved_tensors
+        pctx, lig, cdt, qdt, tdt, T = fctx.meta
+        P = out.shape[0]
+        g = grad_xyz.detach().to(torch.float32).contiguous()
+        gc = torch.empty((P, 3), dtype=torch.float32, device=out.device)
+        gq = torch.empty((P, 4), dtype=torch.float32, device=out.device)
+        gt = torch.empty((P, max(T, 1)), dtype=torch.float32, device=out.device)
+        pctx.ligand_pose_backward_dev(lig, P, _ptr(out), _ptr(c), _ptr(q), _ptr(g), _ptr(gc), _ptr(gq), _ptr(gt),
+                                      _stream())
+        return gc.to(cdt), gq.to(qdt), gt[:, :T].to(tdt), None, None, None
+
+
+def ligand_pose(pctx, lig, xyz_ref, centers, quats, torsions):
+    """Atom coordinates [P][N][3] (float32) of ligand lig for centres [P][3], quaternions
+    [P][4] (w, x, y, z; normalised inside) and torsions [P][T]; xyz_ref [N][3] float32 on
+    the device is the ligand's reference pose."""
+    return _LigandPose.apply(centers, quats, torsions, pctx, lig, xyz_ref)
+
+
+class _DockingEnergy(torch.autograd.Function):
+    @staticmethod
+    def forward(fctx, xyz, pctx, lig_ids, rec_tors):
+        P, A, _ = xyz.shape
+        x = xyz.detach().to(torch.float32).contiguous()
+        e = torch.empty(P, dtype=torch.float64, device=xyz.device)
+        g = torch.empty_like(x)
+        R = pctx.n_rotors
+        tg = torch.empty((P, max(R, 1)), dtype=torch.float32, device=xyz.device)
+        pctx.score_grad_dev(P, A, _ptr(lig_ids), _ptr(x), _ptr(rec_tors), _ptr(e), _ptr(g), _ptr(tg), _stream())
+        fctx.save_for_backward(g)
+        fctx.xdt = xyz.dtype
+        return e
+
+    @staticmethod
+    def backward(fctx, grad_e):
+        (g,) = fctx.saved_tensors
+        return (g * grad_e.to(torch.float32)[:, None, None]).to(fctx.xdt), None, None, None
+
+
+def docking_energy(pctx, lig_ids, xyz, rec_tors=None):
+    """Docking objective per pose [P] (grid maps + intra-ligand terms) with its gradient."""
+    return _DockingEnergy.apply(xyz, pctx, lig_ids, rec_tors)

@@ -79,6 +79,13 @@ def load(auto_build=False):
                                         abi.i32p, abi.i32p, abi.f64p, abi.f64p, abi.f64p, abi.f64p,
                                         abi.f64p, abi.i32p, abi.i32p, abi.f64p]
     lib.pxd_rng_draws.argtypes = [vp, C.c_uint32, C.c_int32, abi.i32p, abi.i32p, abi.f64p]
+    lib.pxd_sf_weights.argtypes = [C.POINTER(abi.SfParams), abi.f64p]
+    lib.pxd_sf_weights.restype = None
+    lib.pxd_score_adjoint_dev.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32] + [vp] * 12
+    lib.pxd_score_adjoint.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32] + [abi.f64p] * 10
+    lib.pxd_score_adjoint_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 13
+    lib.pxd_ligand_pose_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 6
+    lib.pxd_ligand_pose_backward_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 8
     _lib = lib
     return lib
 
@@ -89,6 +96,19 @@ def _p(a, t=C.c_double):
 
 def _f64(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def score_adjoint_multi_dev(contexts, which, n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr, tors_ptr,
+                            weights_ptr, tables_ptr, grad_out_ptr, score_ptr, features_ptr, dxyz_ptr, dweights_ptr,
+                            dtables_ptr, stream=None):
+    """pxd_score_adjoint_multi_dev over a list of Contexts (integer device addresses)."""
+    lib = load()
+    arr = (C.c_void_p * len(contexts))(*[c.h.value for c in contexts])
+    rc = lib.pxd_score_adjoint_multi_dev(arr, len(contexts), which, n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr,
+                                         tors_ptr, weights_ptr, tables_ptr, grad_out_ptr, score_ptr, features_ptr,
+                                         dxyz_ptr, dweights_ptr, dtables_ptr, stream)
+    if rc != 0:
+        raise NativeError(rc, lib.pxd_last_error(contexts[0].h).decode())
 
 
 class Context:
@@ -257,6 +277,47 @@ class Context:
         self._check(self.lib.pxd_score(self.h, which, lig, n, _p(xyz),
                                        _p(tors if tors.size else dummy), _p(s), _p(terms)))
         return s, terms
+
+    def score_adjoint(self, which, lig, xyz, weights, tables=None, grad_out=None, tors=None, grads=True):
+        """Differentiable empirical score of poses of one ligand (pxd_score_adjoint):
+        returns (score [P], features [P][28]) and, with grads, (dxyz [P][N][3], dweights [36],
+        dtables [32][256]) of sum_p grad_out_p * S_p (grad_out defaults to ones)."""
+        N = self.ligands[lig].n_atoms
+        xyz = _f64(xyz).reshape(-1, N, 3)
+        n = xyz.shape[0]
+        tors = _f64(np.zeros((n, self.n_rotors)) if tors is None else tors).reshape(n, self.n_rotors)
+        dummy = np.zeros(1)
+        w = _f64(weights).reshape(abi.NUM_SF_WEIGHTS)
+        tab = None if tables is None else _f64(tables).reshape(-1)
+        g = None if grad_out is None else _f64(grad_out).reshape(n)
+        s = np.zeros(n)
+        f = np.zeros((n, abi.NUM_SCORE_FEATURES))
+        dx = np.zeros((n, N, 3)) if grads else None
+        dw = np.zeros(abi.NUM_SF_WEIGHTS) if grads else None
+        dt = np.zeros(abi.PAIR_TYPES * abi.PAIR_BINS) if grads else None
+        opt = lambda a: None if a is None else _p(a)
+        self._check(self.lib.pxd_score_adjoint(self.h, which, lig, n, _p(xyz), _p(tors if tors.size else dummy),
+                                               _p(w), opt(tab), opt(g), _p(s), _p(f), opt(dx), opt(dw), opt(dt)))
+        if not grads:
+            return s, f
+        return s, f, dx, dw, dt.reshape(abi.PAIR_TYPES, abi.PAIR_BINS)
+
+    def score_adjoint_dev(self, which, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, weights_ptr, tables_ptr,
+                          grad_out_ptr, score_ptr, features_ptr, dxyz_ptr, dweights_ptr, dtables_ptr, stream=None):
+        """pxd_score_adjoint_dev on integer device addresses (None for NULL)."""
+        self._check(self.lib.pxd_score_adjoint_dev(self.h, which, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr,
+                                                   weights_ptr, tables_ptr, grad_out_ptr, score_ptr, features_ptr,
+                                                   dxyz_ptr, dweights_ptr, dtables_ptr, stream))
+
+    def ligand_pose_dev(self, lig, n_poses, xyz_in_ptr, centers_ptr, quats_ptr, tors_ptr, out_ptr, stream=None):
+        self._check(self.lib.pxd_ligand_pose_dev(self.h, lig, n_poses, xyz_in_ptr, centers_ptr, quats_ptr, tors_ptr,
+                                                 out_ptr, stream))
+
+    def ligand_pose_backward_dev(self, lig, n_poses, xyz_ptr, centers_ptr, quats_ptr, grad_ptr, out_center_ptr,
+                                 out_quat_ptr, out_tors_ptr, stream=None):
+        self._check(self.lib.pxd_ligand_pose_backward_dev(self.h, lig, n_poses, xyz_ptr, centers_ptr, quats_ptr,
+                                                          grad_ptr, out_center_ptr, out_quat_ptr, out_tors_ptr,
+                                                          stream))
 
     def gbsa(self, lig, xyz, tors=None):
         xyz = _f64(xyz).reshape(-1)
