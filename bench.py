@@ -499,6 +499,7 @@ def run_differentiate(args):
         if k >= args.warmup:
             e2e_ms.append(a.elapsed_time(b))
     t_ms, e_ms = float(np.mean(ms)), float(np.mean(e2e_ms))
+    cpu = None if args.no_cpu_baseline else diff_cpu_baseline(cplx, dofs, box, pose_sf, w0, t0)
     h2d = sum(x.numel() * 4 for d in h_dofs for x in d) + h_w.numel() * 8 + h_t.numel() * 4
     d2h = sum(x.numel() * 4 for d in h_out for x in d) + h_gw.numel() * 8 + h_gt.numel() * 4
     sizes = [l.n_atoms for _, l in cplx]
@@ -513,10 +514,53 @@ def run_differentiate(args):
                                    % (len(cplx), P, min(sizes), max(sizes)),
                        "l2": "flushed between steps (256 MiB write); 64 map sets exceed L2"},
             "total_score": float(total.item())}
+    if cpu:
+        line["cpu_baseline"] = cpu
     print(json.dumps(line))
     for c in ctxs:
         c.close()
     return 0
+
+
+def diff_cpu_baseline(cplx, dofs, box, sf, weights, tables, target_s=10.0):
+    """The same per-pose work on the host cores in FP64 (the port): forward kinematics,
+    the empirical score with its analytic adjoint (coordinates, weights, tables) and the
+    docking energy with its gradient, over the poses of the first complexes."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle
+
+    threads = cpu_threads()
+    rec, lig = cplx[0]
+    port = oracle.PortSystem(rec, lig)
+    port.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)), nthreads=threads)
+    port.set_slope(SLOPE)
+    centers, quats, tors = dofs[0]
+    x0 = lig.poses[0] - lig.poses[0].mean(axis=0)
+
+    def one(p):
+        q = quats[p] / np.linalg.norm(quats[p])
+        a, b, c, d = q
+        rot = np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (a * c + b * d)],
+                        [2 * (a * d + b * c), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                        [2 * (b * d - a * c), 2 * (a * b + c * d), a * a - b * b - c * c + d * d]])
+        x = port.ligand_apply(x0, centers[p], rot, tors[p])
+        oracle.port_score_diff(sf, rec, lig, rec.xyz, x, weights, tables)
+        port.score_grad([], x)
+
+    n = threads
+    with ThreadPoolExecutor(threads) as ex:
+        while True:
+            t0 = time.perf_counter()
+            list(ex.map(one, [k % len(centers) for k in range(n)]))
+            dt = time.perf_counter() - t0
+            if dt >= target_s or n >= 1 << 16:
+                break
+            n = int(n * max(2.0, target_s / max(dt, 1e-3) * 1.1))
+    return {"value": n / dt, "unit": "poses/s", "cores": threads, "kind": "port",
+            "sample": "%d pose evaluations of complex 0 (%d atoms), FP64 C port: kinematics, empirical score "
+                      "with its analytic adjoint, docking energy and gradient; %d threads, %.1f s"
+                      % (n, lig.n_atoms, threads, dt)}
 
 
 def run_evaluate(args):

@@ -10,6 +10,7 @@
 // table gradient's shared atomics leave its last bits to the order of arrival.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "device_adjoint.cuh"
@@ -60,8 +61,8 @@ __device__ void adj_receptor_rotors(const DevReceptor& R, const float* t, float4
     __syncwarp();
 }
 
-template <bool kGrad, bool kMulti>
-__global__ void __launch_bounds__(kAdjWarps * kWarp) score_adjoint_kernel(const __grid_constant__ AdjArgs a) {
+template <bool kGrad, bool kMulti, int kMinBlocks>
+__global__ void __launch_bounds__(kAdjWarps * kWarp, kMinBlocks) score_adjoint_kernel(const __grid_constant__ AdjArgs a) {
     extern __shared__ __align__(16) unsigned char adj_smem[];
     double* s_w = reinterpret_cast<double*>(adj_smem);  // [36] weights
     double* s_dw = s_w + kNumW;                         // [warps][36] weight gradient per warp
@@ -229,10 +230,24 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t
     const bool tgrad = grad && dtables && tables;
     const size_t smem = adj_smem_bytes(max_atoms, max_mov, tgrad);
     if (smem > 227 * 1024) return set_error(ctx, PXD_ERR_INVALID, "adjoint shared memory beyond 227 KB: lower max_atoms");
-    const void* fn = grad ? (multi ? reinterpret_cast<const void*>(score_adjoint_kernel<true, true>)
-                                   : reinterpret_cast<const void*>(score_adjoint_kernel<true, false>))
-                          : (multi ? reinterpret_cast<const void*>(score_adjoint_kernel<false, true>)
-                                   : reinterpret_cast<const void*>(score_adjoint_kernel<false, false>));
+    // register budget: 128 per thread (2 resident blocks) or 80 (3 blocks); PXD_ADJ_MIN_BLOCKS
+    // overrides the default of 2
+    static const int min_blocks = [] {
+        const char* e = std::getenv("PXD_ADJ_MIN_BLOCKS");
+        return e && std::atoi(e) == 3 ? 3 : 2;
+    }();
+    const bool three = min_blocks == 3;
+    const void* fn;
+    if (grad)
+        fn = multi ? (three ? reinterpret_cast<const void*>(score_adjoint_kernel<true, true, 3>)
+                            : reinterpret_cast<const void*>(score_adjoint_kernel<true, true, 2>))
+                   : (three ? reinterpret_cast<const void*>(score_adjoint_kernel<true, false, 3>)
+                            : reinterpret_cast<const void*>(score_adjoint_kernel<true, false, 2>));
+    else
+        fn = multi ? (three ? reinterpret_cast<const void*>(score_adjoint_kernel<false, true, 3>)
+                            : reinterpret_cast<const void*>(score_adjoint_kernel<false, true, 2>))
+                   : (three ? reinterpret_cast<const void*>(score_adjoint_kernel<false, false, 3>)
+                            : reinterpret_cast<const void*>(score_adjoint_kernel<false, false, 2>));
     int rc = cuda_check(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   static_cast<int>(smem)), "adjoint smem");
     if (rc) return rc;
@@ -281,10 +296,13 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t
     if (grad) a.part_w = reinterpret_cast<double*>(base + cbytes);
     if (tgrad) a.part_t = reinterpret_cast<float*>(base + cbytes + wbytes);
     if (!rc) {
-        if (grad && multi) score_adjoint_kernel<true, true><<<blocks, kAdjWarps * kWarp, smem, s>>>(a);
-        else if (grad) score_adjoint_kernel<true, false><<<blocks, kAdjWarps * kWarp, smem, s>>>(a);
-        else if (multi) score_adjoint_kernel<false, true><<<blocks, kAdjWarps * kWarp, smem, s>>>(a);
-        else score_adjoint_kernel<false, false><<<blocks, kAdjWarps * kWarp, smem, s>>>(a);
+        void* params[] = {&a};
+        rc = cuda_check(ctx, cudaLaunchKernel(fn, dim3(blocks), dim3(kAdjWarps * kWarp), params, smem, s),
+                        "score_adjoint_kernel launch");
+        if (rc) {
+            if (mem) cudaFreeAsync(mem, s);
+            return rc;
+        }
         rc = cuda_check(ctx, cudaGetLastError(), "score_adjoint_kernel launch");
     }
     if (!rc && grad && dweights) {

@@ -643,7 +643,7 @@ int pxd_set_receptor(pxd_context* ctx, const pxd_receptor_desc* r) {
     ctx->n_ex_all = M;
     ctx->n_ex_mov = static_cast<int>(movs.size());
     point_explicit(ctx, false);
-    rc = upload_receptor_scoring(ctx, r->lists);
+    rc = upload_receptor_scoring(ctx, r->lists, local_of);
     if (rc) return rc;
     ctx->has_receptor = true;
     ctx->ligands_dirty = true;

@@ -247,29 +247,33 @@ __device__ void score_adjoint_pose(const ScoreEnv& env, const DevLigand& L, cons
     const int N = L.n_atoms;
     const float s_coul = g * W[PXD_W_COEF + PXD_TERM_COULOMB] * kCoulombF;
     const float s_vdw = g * W[PXD_W_COEF + PXD_TERM_VDW] * W[PXD_W_VDW_SCALE];
-    const bool table = ap.tab && rs.pclass && ls.pclass;
+    const bool table = ap.tab && ls.pclass;  // receptor atoms without a class carry -1
     // Coulomb, clamped LJ and the pair table over every ligand x receptor pair
     DS a_coul{0.f, 0.f}, a_vdw{0.f, 0.f}, a_tab{0.f, 0.f};
     for (int i = 0; i < N; ++i) {
         const float3 xi = xyz(X[i]);
         const float qi = __ldg(&L.charge[i]);
         const float2 ti = sf.vdw_type[__ldg(&L.type[i])];
+        const float sei4 = sqrtf(ti.y) * 4.f;
         const int ci = table ? __ldg(&ls.pclass[i]) : -1;
         float ec = 0.f, ev = 0.f, et = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
+#pragma unroll 2
         for (int j = lane; j < rs.n_all; j += kWarp) {
             const float4 rj = __ldg(&rs.all_xyzq[j]);
-            const int l = __ldg(&rs.all_local[j]);
+            const float4 pr = __ldg(&rs.pair_rec[j]);  // sigma, sqrt(eps), class, local
+            const int l = __float_as_int(pr.w);
             const float3 xj = l >= 0 ? xyz(loc_xyz[l]) : xyz(rj);
             const float3 dv = sub3(xi, xj);
-            const float d = sqrtf(dot3(dv, dv));
-            const float rinv = 1.f / (d + kEpsF);
+            const float r2 = dot3(dv, dv);
+            // 1 / (d + 1e-20) of the reference is 1 / d away from d = 0
+            const float rinv = r2 > 0.f ? rsqrtf(r2) : 1.f / kEpsF;
+            const float d = r2 * rinv;
             ec = fmaf(qi * rj.w, rinv, ec);
-            const float2 sej = __ldg(&rs.all_se[j]);
-            const float s = (ti.x + sej.x) * 0.5f * rinv;
+            const float s = (ti.x + pr.x) * 0.5f * rinv;
             const float s2 = s * s;
             const float u6 = s2 * s2 * s2;
-            const float fused = sqrtf(ti.y * sej.y) * 4.f;
+            const float fused = sei4 * pr.y;
             const float v = (u6 * u6 - u6) * fused;
             ev += fminf(fmaxf(v, -sf.vdw_cutoff), sf.vdw_cutoff);
             float de_dd = 0.f;
@@ -279,7 +283,7 @@ __device__ void score_adjoint_pose(const ScoreEnv& env, const DevLigand& L, cons
                     de_dd -= s_vdw * fused * rinv * (12.f * u6 * u6 - 6.f * u6);
             }
             if (ci >= 0) {
-                const int cj = __ldg(&rs.pclass[j]);
+                const int cj = __float_as_int(pr.z);
                 const float tt = d * kTabInvWidth;
                 if (cj >= 0 && tt < static_cast<float>(PXD_PAIR_BINS - 1)) {
                     const int b = static_cast<int>(tt);
@@ -296,7 +300,7 @@ __device__ void score_adjoint_pose(const ScoreEnv& env, const DevLigand& L, cons
                     }
                 }
             }
-            if (kGrad && d > 0.f) gi = add3(gi, mul3(dv, de_dd / d));
+            if (kGrad) gi = add3(gi, mul3(dv, de_dd * rinv));
         }
         ds_add(a_coul, ec * kCoulombF);
         ds_add(a_vdw, ev);

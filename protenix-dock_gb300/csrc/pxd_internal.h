@@ -70,6 +70,7 @@ struct DevRecScore {
     const int* accc;
     const int* accn;
     const int* pclass;         // [n_all] pair-table class (C N O other: 0-3), -1 none; NULL: no table term
+    const float4* pair_rec;    // [n_all] sigma, sqrt(epsilon), pair-table class, rotor local index (int bits)
 };
 
 struct DevLigScore {
@@ -237,7 +238,7 @@ int launch_ligand_pose_backward(pxd_context* ctx, int lig, int n_poses, const fl
                                 const float* quats, const float* grad, float* out_center, float* out_quat,
                                 float* out_tors, cudaStream_t s);
 int pair_class(int is_receptor, int z);
-int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l);
+int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l, const std::vector<int>& local_of);
 int upload_ligand_scoring(pxd_context* ctx, LigandEntry& e, const pxd_score_lists* l);
 void gbsa_properties(const pxd_score_lists* l, int n, std::vector<double>& radius,
                      std::vector<double>& screen);

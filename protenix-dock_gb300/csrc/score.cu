@@ -81,6 +81,12 @@ int pair_class(int is_receptor, int z) {
     }
 }
 
+static float __int_as_float_host(int v) {
+    float f;
+    std::memcpy(&f, &v, sizeof(f));
+    return f;
+}
+
 static std::vector<int> pair_classes(const pxd_score_lists* l, int n, int is_receptor) {
     std::vector<int> c;
     if (!l || !l->atomic_numbers) return c;
@@ -124,7 +130,7 @@ static bool lists_ok(const pxd_score_lists* l, int n_atoms) {
     return true;
 }
 
-int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l) {
+int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l, const std::vector<int>& local_of) {
     DevRecScore& d = ctx->rec_score;
     d = DevRecScore{};
     if (ctx->rec_score_mem) cudaFree(ctx->rec_score_mem);
@@ -135,8 +141,27 @@ int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l) {
     d.all_se = at<float2>(ctx->rec_ex_all, ctx->ex_all_off[1]);
     d.all_local = at<int>(ctx->rec_ex_all, ctx->ex_all_off[2]);
     gbsa_properties(l, M, ctx->rec_gb_radius, ctx->rec_gb_screen);
-    if (!l) return PXD_OK;
-    if (!lists_ok(l, M)) return set_error(ctx, PXD_ERR_INVALID, "receptor interaction list atom out of range");
+    if (l && !lists_ok(l, M)) return set_error(ctx, PXD_ERR_INVALID, "receptor interaction list atom out of range");
+    // per-atom record of the differentiable score's pair loop: sigma, sqrt(epsilon),
+    // pair-table class, rotor-atom local index (-1: fixed)
+    const std::vector<int> pcls = pair_classes(l, M, 1);
+    std::vector<float4> pairrec(M);
+    for (int a = 0; a < M; ++a)
+        pairrec[a] = make_float4(static_cast<float>(ctx->rec_sigma[a]),
+                                 static_cast<float>(std::sqrt(ctx->rec_epsilon[a])),
+                                 __int_as_float_host(pcls.empty() ? -1 : pcls[a]),
+                                 __int_as_float_host(ctx->is_mov[a] ? local_of[a] : -1));
+    Pack pk;
+    const size_t o_pair = pk.put(pairrec);
+    if (!l) {
+        int rc0 = cuda_check(ctx, cudaMalloc(&ctx->rec_score_mem, pk.bytes.size()), "receptor score lists");
+        if (rc0) return rc0;
+        rc0 = cuda_check(ctx, cudaMemcpy(ctx->rec_score_mem, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice),
+                         "receptor score lists copy");
+        if (rc0) return rc0;
+        d.pair_rec = at<float4>(ctx->rec_score_mem, o_pair);
+        return PXD_OK;
+    }
     // ring centroids and normals (to_ring_centroid / to_ring_normal, scorer.cpp:128-172)
     std::vector<float4> rc[2], rn[2];
     for (int k = 0; k < 2; ++k) {
@@ -166,7 +191,6 @@ int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l) {
                                         static_cast<float>(nn[2] / len), 0.f));
         }
     }
-    Pack pk;
     const size_t o_hyd = pk.put(ints(l->hydrophobic, l->n_hydrophobic));
     const size_t o_cat = pk.put(ints(l->cation, l->n_cation));
     const size_t o_an = pk.put(ints(l->anion, l->n_anion));
@@ -175,7 +199,6 @@ int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l) {
     const size_t o_donn = pk.put(pairs2(l->don_neutral, l->n_don_neutral));
     const size_t o_accc = pk.put(ints(l->acc_charged, l->n_acc_charged));
     const size_t o_accn = pk.put(ints(l->acc_neutral, l->n_acc_neutral));
-    const std::vector<int> pcls = pair_classes(l, M, 1);
     const size_t o_pcl = pk.put(pcls);
     int rc_ = cuda_check(ctx, cudaMalloc(&ctx->rec_score_mem, pk.bytes.size()), "receptor score lists");
     if (rc_) return rc_;
@@ -205,6 +228,7 @@ int upload_receptor_scoring(pxd_context* ctx, const pxd_score_lists* l) {
     d.accc = at<int>(b, o_accc);
     d.accn = at<int>(b, o_accn);
     d.pclass = pcls.empty() ? nullptr : at<int>(b, o_pcl);
+    d.pair_rec = at<float4>(b, o_pair);
     return PXD_OK;
 }
 
