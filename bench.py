@@ -438,48 +438,53 @@ def run_differentiate(args):
         dofs.append((rng.uniform(-4.0, 4.0, size=(P, 3)), q / np.linalg.norm(q, axis=1, keepdims=True),
                      rng.uniform(-np.pi, np.pi, size=(P, lig.n_torsions))))
     A = max(l.n_atoms for _, l in cplx)
+    Tmax = max(l.n_torsions for _, l in cplx)
+    D = 7 + Tmax
     n = P * len(cplx)
     ctx_ids = torch.tensor(np.repeat(np.arange(len(cplx)), P).astype(np.int32), device=dev)
     lig_ids = torch.tensor(np.repeat(np.array(lids), P).astype(np.int32), device=dev)
-    per_ids = [torch.full((P,), lid, dtype=torch.int32, device=dev) for lid in lids]
+    xyz_ref = torch.zeros((n, A, 3), dtype=torch.float32, device=dev)
+    q_all = np.zeros((n, D), np.float32)
+    for c, ((_, lig), (cen, qu, tq)) in enumerate(zip(cplx, dofs)):
+        xyz_ref[c * P:(c + 1) * P, : lig.n_atoms] = refs[c]
+        q_all[c * P:(c + 1) * P, :3] = cen
+        q_all[c * P:(c + 1) * P, 3:7] = qu
+        q_all[c * P:(c + 1) * P, 7:7 + lig.n_torsions] = tq
     w0 = abi.sf_weights(pose_sf)
     t0 = abi.smooth_pair_tables(1)
     # pinned host inputs (the e2e leg copies them in and the gradients out every step)
-    h_dofs = [tuple(torch.from_numpy(a.astype(np.float32)).pin_memory() for a in d) for d in dofs]
+    h_q = torch.from_numpy(q_all).pin_memory()
     h_w = torch.from_numpy(w0).pin_memory()
     h_t = torch.from_numpy(t0.astype(np.float32)).pin_memory()
-    d_dofs = [tuple(a.to(dev) for a in d) for d in h_dofs]
-    d_w = h_w.to(dev)
-    d_t = h_t.to(dev)
+    d_q, d_w, d_t = h_q.to(dev), h_w.to(dev), h_t.to(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(dev)
 
-    def step(dofs_dev, w_dev, t_dev):
-        leaves = [tuple(a.detach().requires_grad_(True) for a in d) for d in dofs_dev]
+    def step(q_dev, w_dev, t_dev):
+        q = q_dev.detach().requires_grad_(True)
         w = w_dev.detach().requires_grad_(True)
         t = t_dev.detach().requires_grad_(True)
-        xs = [AG.ligand_pose(ctxs[c], lids[c], refs[c], *leaves[c]) for c in range(len(ctxs))]
-        xyz = torch.cat([torch.nn.functional.pad(x, (0, 0, 0, A - x.shape[1])) for x in xs])
+        xyz = AG.ligand_pose_multi(ctxs, ctx_ids, lig_ids, xyz_ref, q)
         s = AG.empirical_score(ctxs, lig_ids, xyz, w, t, ctx_ids=ctx_ids)
-        e = torch.cat([AG.docking_energy(ctxs[c], per_ids[c], xs[c]) for c in range(len(ctxs))])
+        e = AG.docking_energy(ctxs, lig_ids, xyz, ctx_ids=ctx_ids)
         total = (s + e).sum()
         total.backward()
-        return total, leaves, w, t
+        return total, q, w, t
 
     ms, e2e_ms = [], []
-    launches = 3 * len(ctxs) + 3 + 1
+    launches = 7  # pose, score value, docking energy; adjoint + 2 partial sums, pose backward
     for k in range(args.warmup + args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            total, leaves, w, t = step(d_dofs, d_w, d_t)
+            total, q, w, t = step(d_q, d_w, d_t)
             b.record(stream)
         torch.cuda.synchronize()
         if k >= args.warmup:
             ms.append(a.elapsed_time(b))
     # end to end: pinned host DOFs and parameters in, every gradient back to pinned host memory
-    h_out = [tuple(torch.empty(a.shape, dtype=torch.float32).pin_memory() for a in d) for d in h_dofs]
+    h_gq = torch.empty(h_q.shape, dtype=torch.float32).pin_memory()
     h_gw = torch.empty(abi.NUM_SF_WEIGHTS, dtype=torch.float64).pin_memory()
     h_gt = torch.empty(t0.shape, dtype=torch.float32).pin_memory()
     for k in range(args.warmup + args.steps):
@@ -487,11 +492,9 @@ def run_differentiate(args):
             flush.fill_(1.0)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            dd = [tuple(x.to(dev, non_blocking=True) for x in d) for d in h_dofs]
-            total, leaves, w, t = step(dd, h_w.to(dev, non_blocking=True), h_t.to(dev, non_blocking=True))
-            for lv, ho in zip(leaves, h_out):
-                for x, y in zip(lv, ho):
-                    y.copy_(x.grad, non_blocking=True)
+            total, q, w, t = step(h_q.to(dev, non_blocking=True), h_w.to(dev, non_blocking=True),
+                                  h_t.to(dev, non_blocking=True))
+            h_gq.copy_(q.grad, non_blocking=True)
             h_gw.copy_(w.grad, non_blocking=True)
             h_gt.copy_(t.grad, non_blocking=True)
             b.record(stream)
@@ -500,8 +503,8 @@ def run_differentiate(args):
             e2e_ms.append(a.elapsed_time(b))
     t_ms, e_ms = float(np.mean(ms)), float(np.mean(e2e_ms))
     cpu = None if args.no_cpu_baseline else diff_cpu_baseline(cplx, dofs, box, pose_sf, w0, t0)
-    h2d = sum(x.numel() * 4 for d in h_dofs for x in d) + h_w.numel() * 8 + h_t.numel() * 4
-    d2h = sum(x.numel() * 4 for d in h_out for x in d) + h_gw.numel() * 8 + h_gt.numel() * 4
+    h2d = h_q.numel() * 4 + h_w.numel() * 8 + h_t.numel() * 4
+    d2h = h_gq.numel() * 4 + h_gw.numel() * 8 + h_gt.numel() * 4
     sizes = [l.n_atoms for _, l in cplx]
     line = {"metric": "differentiated poses/s (score + gradients in coordinates, DOFs, 36 weights, 32x256 "
                       "pair tables)", "value": n / t_ms * 1e3, "unit": "poses/s", "n_gpus": 1, "steps": args.steps,
@@ -510,7 +513,7 @@ def run_differentiate(args):
             "e2e": {"value": n / e_ms * 1e3, "unit": "poses/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "config": {"workload": "differentiation through fixed poses: %d complexes x %d poses, 55^3 maps each, "
-                                   "ligands %d-%d atoms, forward + backward through torch.autograd"
+                                   "ligands %d-%d atoms, forward + backward through torch.autograd, every complex in one launch per kernel"
                                    % (len(cplx), P, min(sizes), max(sizes)),
                        "l2": "flushed between steps (256 MiB write); 64 map sets exceed L2"},
             "total_score": float(total.item())}

@@ -292,6 +292,17 @@ int pxd_score_grad_dev(pxd_context* ctx, int32_t n_poses, int32_t max_atoms,
                        const float* rec_tors_dev, double* energy_dev, float* lig_grad_dev,
                        float* tors_grad_dev, void* stream);
 
+/* pxd_score_grad_dev over poses of several contexts (one receptor and map set each, all
+ * on one device) in one launch: contexts [n_contexts] is a host array, ctx_ids_dev [P]
+ * picks each pose's context and ligand_ids_dev the ligand in it; rec_tors / tors_grad
+ * rows have the largest receptor-torsion count of the contexts. lig_grad padding rows
+ * are zero. Errors are reported on contexts[0]. */
+int pxd_score_grad_multi_dev(pxd_context* const* contexts, int32_t n_contexts, int32_t n_poses,
+                             int32_t max_atoms, const int32_t* ctx_ids_dev,
+                             const int32_t* ligand_ids_dev, const float* lig_xyz_dev,
+                             const float* rec_tors_dev, double* energy_dev, float* lig_grad_dev,
+                             float* tors_grad_dev, void* stream);
+
 /* Host-buffer version of pxd_score_grad_dev for one ligand (double in/out). */
 int pxd_score_grad(pxd_context* ctx, int32_t ligand_id, int32_t n_poses,
                    const double* lig_xyz, const double* rec_tors, double* energy,
@@ -466,6 +477,18 @@ int pxd_score_adjoint(pxd_context* ctx, int32_t which, int32_t ligand_id, int32_
 int pxd_ligand_pose_dev(pxd_context* ctx, int32_t ligand_id, int32_t n_poses, const float* xyz_in_dev,
                         const float* centers_dev, const float* quats_dev, const float* torsions_dev,
                         float* xyz_out_dev, void* stream);
+
+/* Pose kinematics over poses of several contexts (no reference counterpart beyond
+ * free_ligand::apply_parameters, data.cpp:592-641): pose p is ligand lig_ids[p] of
+ * contexts[ctx_ids[p]]; dofs [P][dof] (centre, quaternion w x y z, torsions padded to
+ * dof); xyz_ref [P][max_atoms][3] each pose's reference coordinates. With atom_grad NULL,
+ * writes xyz_out [P][max_atoms][3] (padding rows zero). With atom_grad [P][max_atoms][3]
+ * (dE/dx at xyz_out), writes dofs_grad [P][dof] instead (backward; xyz_out is read). */
+int pxd_ligand_pose_multi_dev(pxd_context* const* contexts, int32_t n_contexts, int32_t n_poses,
+                              int32_t max_atoms, int32_t dof, const int32_t* ctx_ids_dev,
+                              const int32_t* lig_ids_dev, const float* xyz_ref_dev,
+                              const float* dofs_dev, float* xyz_out_dev, const float* atom_grad_dev,
+                              float* dofs_grad_dev, void* stream);
 
 /* Backward of pxd_ligand_pose_dev: from dL/dx [P][N][3] at xyz [P][N][3], writes
  * dL/dcentre [P][3], dL/dquaternion [P][4] (through the normalisation) and

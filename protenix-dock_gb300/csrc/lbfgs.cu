@@ -218,6 +218,62 @@ int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_id
     return cuda_check(ctx, cudaGetLastError(), "score_kernel launch");
 }
 
+// score_kernel over poses of several contexts (one receptor and map set each): pose p
+// is ligand lig_ids[p] of context ctx_ids[p]; the per-warp buffers are sized for the
+// largest ligand and rotor-atom set of the batch.
+struct ScoreMultiArgs {
+    const EvalEnv* envs;           // [n_ctx]
+    const DevLigand* const* tabs;  // [n_ctx] device ligand tables
+    const int* n_ligs;             // [n_ctx]
+    const int* ctx_ids;
+    const int* lig_ids;
+    const float* xyz;
+    const float* tors;             // [P][tors_stride]
+    int tors_stride;
+    int max_atoms;
+    double* energy;
+    float* lig_grad;
+    float* tors_grad;
+    int n_poses;
+    int n_local;
+    int D_pad;
+};
+
+__global__ void __launch_bounds__(kWarpsPerBlock * kWarp) score_multi_kernel(const __grid_constant__ ScoreMultiArgs a) {
+    extern __shared__ __align__(16) float smem[];
+    const int lane = threadIdx.x & (kWarp - 1);
+    const int wib = threadIdx.x / kWarp;
+    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + 2 * a.D_pad;
+    float* base = smem + wib * per_warp;
+    const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
+    float* x = base + pose_bufs_floats(a.max_atoms, a.n_local);
+    float* g = x + a.D_pad;
+    const int nw = gridDim.x * kWarpsPerBlock;
+    for (int pose = blockIdx.x * kWarpsPerBlock + wib; pose < a.n_poses; pose += nw) {
+        const int c = a.ctx_ids[pose];
+        const int lid = a.lig_ids[pose];
+        if (lid < 0 || lid >= a.n_ligs[c] || a.tabs[c][lid].n_atoms > a.max_atoms) {
+            if (lane == 0) a.energy[pose] = nan("");
+            continue;
+        }
+        const EvalEnv& env = a.envs[c];
+        const DevLigand L = a.tabs[c][lid];
+        const int N = L.n_atoms;
+        const int R = env.rec.n_rotors;
+        const float* px = a.xyz + static_cast<size_t>(pose) * a.max_atoms * 3;
+        for (int e = lane; e < 3 * N; e += kWarp) x[e] = px[e];
+        for (int r = lane; r < R; r += kWarp) x[3 * N + r] = a.tors[static_cast<size_t>(pose) * a.tors_stride + r];
+        __syncwarp();
+        const double e = eval_pose_body(env, L, x, nullptr, 0.f, g, b, lane);
+        float* og = a.lig_grad + static_cast<size_t>(pose) * a.max_atoms * 3;
+        for (int k = lane; k < 3 * a.max_atoms; k += kWarp) og[k] = k < 3 * N ? g[k] : 0.f;
+        for (int r = lane; r < R; r += kWarp)
+            a.tors_grad[static_cast<size_t>(pose) * a.tors_stride + r] = g[3 * N + r];
+        if (lane == 0) a.energy[pose] = e;
+        __syncwarp();
+    }
+}
+
 // Size classes of the batched launch: poses are grouped by their ligand's atom count so
 // that each persistent launch sizes its per-warp shared memory (and so its residency)
 // for its own class instead of the largest ligand of the batch.
@@ -513,3 +569,74 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
 }
 
 }  // namespace pxd
+
+using namespace pxd;
+
+extern "C" int pxd_score_grad_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t n_poses, int32_t max_atoms,
+                                        const int32_t* ctx_ids, const int32_t* lig_ids, const float* xyz,
+                                        const float* tors, double* energy, float* lig_grad, float* tors_grad,
+                                        void* stream) {
+    if (!ctxs || n_ctx < 1 || !ctxs[0]) return PXD_ERR_INVALID;
+    pxd_context* ctx = ctxs[0];  // errors are reported here
+    if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS || !ctx_ids || !lig_ids || !xyz ||
+        !energy || !lig_grad)
+        return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");
+    cudaSetDevice(ctx->device);
+    std::vector<EvalEnv> envs(n_ctx);
+    std::vector<const DevLigand*> tabs(n_ctx);
+    std::vector<int> n_ligs(n_ctx);
+    int max_local = 0, max_rot = 0;
+    for (int c = 0; c < n_ctx; ++c) {
+        pxd_context* k = ctxs[c];
+        if (!k || k->device != ctx->device) return set_error(ctx, PXD_ERR_INVALID, "contexts must be on one device");
+        if (!k->has_receptor) return set_error(ctx, PXD_ERR_STATE, "set a receptor first");
+        int rc = sync_ligand_table(k);
+        if (rc) return set_error(ctx, rc, k->error);
+        envs[c] = make_env(k);
+        tabs[c] = k->d_ligands;
+        n_ligs[c] = static_cast<int>(k->ligands.size());
+        max_local = std::max(max_local, k->rec.n_local);
+        max_rot = std::max(max_rot, k->rec.n_rotors);
+    }
+    if (max_rot > 0 && (!tors || !tors_grad))
+        return set_error(ctx, PXD_ERR_INVALID, "receptor torsion buffers required");
+    if (n_poses == 0) return PXD_OK;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const size_t e_bytes = (sizeof(EvalEnv) * n_ctx + 255) / 256 * 256;
+    const size_t t_bytes = (sizeof(void*) * n_ctx + 255) / 256 * 256;
+    void* mem = nullptr;
+    int rc = cuda_check(ctx, cudaMallocAsync(&mem, e_bytes + t_bytes + sizeof(int) * n_ctx, s), "context tables");
+    if (rc) return rc;
+    char* base = static_cast<char*>(mem);
+    cudaMemcpyAsync(base, envs.data(), sizeof(EvalEnv) * n_ctx, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(base + e_bytes, tabs.data(), sizeof(void*) * n_ctx, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(base + e_bytes + t_bytes, n_ligs.data(), sizeof(int) * n_ctx, cudaMemcpyHostToDevice, s);
+    ScoreMultiArgs a;
+    a.envs = reinterpret_cast<const EvalEnv*>(base);
+    a.tabs = reinterpret_cast<const DevLigand* const*>(base + e_bytes);
+    a.n_ligs = reinterpret_cast<const int*>(base + e_bytes + t_bytes);
+    a.ctx_ids = ctx_ids;
+    a.lig_ids = lig_ids;
+    a.xyz = xyz;
+    a.tors = tors;
+    a.tors_stride = max_rot;
+    a.max_atoms = max_atoms;
+    a.energy = energy;
+    a.lig_grad = lig_grad;
+    a.tors_grad = tors_grad;
+    a.n_poses = n_poses;
+    a.n_local = max_local;
+    a.D_pad = padded(3 * max_atoms + max_rot);
+    const size_t smem = sizeof(float) * kWarpsPerBlock * (pose_bufs_floats(max_atoms, a.n_local) + 2 * a.D_pad);
+    rc = cuda_check(ctx, cudaFuncSetAttribute(score_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              static_cast<int>(smem)),
+                    "score smem attribute");
+    if (!rc) {
+        int blocks = (n_poses + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        if (blocks > ctx->n_sm * 16) blocks = ctx->n_sm * 16;
+        score_multi_kernel<<<blocks, kWarpsPerBlock * kWarp, smem, s>>>(a);
+        rc = cuda_check(ctx, cudaGetLastError(), "score_multi_kernel launch");
+    }
+    cudaFreeAsync(mem, s);
+    return rc;
+}

@@ -9,9 +9,11 @@ Each Function calls the library's hand-written kernels on the current torch stre
 - ``ligand_pose(ctx, lig, xyz_ref, centers, quats, torsions)``: torsion-tree forward
   kinematics (pxd_ligand_pose_dev) with its backward (pxd_ligand_pose_backward_dev):
   atom gradients become centre, quaternion and torsion gradients.
+- ``ligand_pose_multi(ctxs, ctx_ids, lig_ids, xyz_ref, dofs)``: the same over poses of
+  many contexts in one launch (pxd_ligand_pose_multi_dev).
 - ``docking_energy(ctx, lig_ids, xyz)``: the docking objective (grid maps + intra-ligand
-  force field, pxd_score_grad_dev) with its analytic coordinate gradient; it has no
-  parameters.
+  force field, pxd_score_grad_dev, or pxd_score_grad_multi_dev over several contexts) with
+  its analytic coordinate gradient; it has no parameters.
 
 Torch is only the autograd and memory plumbing here; there is no torch fallback.
 """
@@ -115,14 +117,19 @@ def ligand_pose(pctx, lig, xyz_ref, centers, quats, torsions):
 
 class _DockingEnergy(torch.autograd.Function):
     @staticmethod
-    def forward(fctx, xyz, pctx, lig_ids, rec_tors):
+    def forward(fctx, xyz, pctxs, ctx_ids, lig_ids, rec_tors):
         P, A, _ = xyz.shape
         x = xyz.detach().to(torch.float32).contiguous()
         e = torch.empty(P, dtype=torch.float64, device=xyz.device)
         g = torch.empty_like(x)
-        R = pctx.n_rotors
+        R = max(c.n_rotors for c in pctxs)
         tg = torch.empty((P, max(R, 1)), dtype=torch.float32, device=xyz.device)
-        pctx.score_grad_dev(P, A, _ptr(lig_ids), _ptr(x), _ptr(rec_tors), _ptr(e), _ptr(g), _ptr(tg), _stream())
+        if ctx_ids is None:
+            pctxs[0].score_grad_dev(P, A, _ptr(lig_ids), _ptr(x), _ptr(rec_tors), _ptr(e), _ptr(g), _ptr(tg),
+                                    _stream())
+        else:
+            native.score_grad_multi_dev(pctxs, P, A, _ptr(ctx_ids), _ptr(lig_ids), _ptr(x), _ptr(rec_tors), _ptr(e),
+                                        _ptr(g), _ptr(tg), _stream())
         fctx.save_for_backward(g)
         fctx.xdt = xyz.dtype
         return e
@@ -130,9 +137,45 @@ class _DockingEnergy(torch.autograd.Function):
     @staticmethod
     def backward(fctx, grad_e):
         (g,) = fctx.saved_tensors
-        return (g * grad_e.to(torch.float32)[:, None, None]).to(fctx.xdt), None, None, None
+        return (g * grad_e.to(torch.float32)[:, None, None]).to(fctx.xdt), None, None, None, None
 
 
-def docking_energy(pctx, lig_ids, xyz, rec_tors=None):
-    """Docking objective per pose [P] (grid maps + intra-ligand terms) with its gradient."""
-    return _DockingEnergy.apply(xyz, pctx, lig_ids, rec_tors)
+def docking_energy(pctx, lig_ids, xyz, rec_tors=None, ctx_ids=None):
+    """Docking objective per pose [P] (grid maps + intra-ligand terms) with its gradient;
+    pctx is one Context, or a list of Contexts with ctx_ids [P] (one launch)."""
+    pctxs = list(pctx) if isinstance(pctx, (list, tuple)) else [pctx]
+    if len(pctxs) > 1 and ctx_ids is None:
+        raise ValueError("ctx_ids is required with several contexts")
+    return _DockingEnergy.apply(xyz, pctxs, ctx_ids if len(pctxs) > 1 else None, lig_ids, rec_tors)
+
+
+class _LigandPoseMulti(torch.autograd.Function):
+    @staticmethod
+    def forward(fctx, dofs, pctxs, ctx_ids, lig_ids, xyz_ref):
+        P, D = dofs.shape
+        A = xyz_ref.shape[1]
+        q = dofs.detach().to(torch.float32).contiguous()
+        out = torch.empty((P, A, 3), dtype=torch.float32, device=dofs.device)
+        native.ligand_pose_multi_dev(pctxs, P, A, D, _ptr(ctx_ids), _ptr(lig_ids), _ptr(xyz_ref), _ptr(q), _ptr(out),
+                                     None, None, _stream())
+        fctx.save_for_backward(out, q, ctx_ids, lig_ids)
+        fctx.meta = (pctxs, dofs.dtype)
+        return out
+
+    @staticmethod
+    def backward(fctx, grad_xyz):
+        out, q, ctx_ids, lig_ids = fctx.saved_tensors
+        pctxs, qdt = fctx.meta
+        P, D = q.shape
+        gq = torch.empty_like(q)
+        native.ligand_pose_multi_dev(pctxs, P, out.shape[1], D, _ptr(ctx_ids), _ptr(lig_ids), None, _ptr(q),
+                                     _ptr(out), _ptr(grad_xyz.detach().to(torch.float32).contiguous()), _ptr(gq),
+                                     _stream())
+        return gq.to(qdt), None, None, None, None
+
+
+def ligand_pose_multi(pctxs, ctx_ids, lig_ids, xyz_ref, dofs):
+    """Atom coordinates [P][A][3] of poses of several contexts in one launch: pose p is
+    ligand lig_ids[p] of pctxs[ctx_ids[p]], xyz_ref [P][A][3] its reference coordinates,
+    dofs [P][D] its centre, quaternion (normalised inside) and torsions (padded to D)."""
+    return _LigandPoseMulti.apply(dofs, list(pctxs), ctx_ids, lig_ids, xyz_ref)

@@ -84,6 +84,8 @@ def load(auto_build=False):
     lib.pxd_score_adjoint_dev.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32] + [vp] * 12
     lib.pxd_score_adjoint.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32] + [abi.f64p] * 10
     lib.pxd_score_adjoint_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 13
+    lib.pxd_ligand_pose_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 8
+    lib.pxd_score_grad_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32] + [vp] * 8
     lib.pxd_ligand_pose_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 6
     lib.pxd_ligand_pose_backward_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 8
     _lib = lib
@@ -96,6 +98,28 @@ def _p(a, t=C.c_double):
 
 def _f64(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def ligand_pose_multi_dev(contexts, n_poses, max_atoms, dof, ctx_ids_ptr, lig_ids_ptr, xyz_ref_ptr, dofs_ptr,
+                          xyz_ptr, atom_grad_ptr, dofs_grad_ptr, stream=None):
+    """pxd_ligand_pose_multi_dev over a list of Contexts (forward, or backward with atom_grad)."""
+    lib = load()
+    arr = (C.c_void_p * len(contexts))(*[c.h.value for c in contexts])
+    rc = lib.pxd_ligand_pose_multi_dev(arr, len(contexts), n_poses, max_atoms, dof, ctx_ids_ptr, lig_ids_ptr,
+                                       xyz_ref_ptr, dofs_ptr, xyz_ptr, atom_grad_ptr, dofs_grad_ptr, stream)
+    if rc != 0:
+        raise NativeError(rc, lib.pxd_last_error(contexts[0].h).decode())
+
+
+def score_grad_multi_dev(contexts, n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
+                         lig_grad_ptr, tors_grad_ptr, stream=None):
+    """pxd_score_grad_multi_dev over a list of Contexts (integer device addresses)."""
+    lib = load()
+    arr = (C.c_void_p * len(contexts))(*[c.h.value for c in contexts])
+    rc = lib.pxd_score_grad_multi_dev(arr, len(contexts), n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr, tors_ptr,
+                                      energy_ptr, lig_grad_ptr, tors_grad_ptr, stream)
+    if rc != 0:
+        raise NativeError(rc, lib.pxd_last_error(contexts[0].h).decode())
 
 
 def score_adjoint_multi_dev(contexts, which, n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr, tors_ptr,

@@ -220,3 +220,61 @@ def test_autograd_dofs_match_finite_differences(adj):
         checked += smooth.sum()
         assert np.max(np.abs(g - want)[smooth]) <= 1e-4 * scale, (p, g, want, smooth)
     assert checked >= 0.75 * total  # a DOF step moves every atom: kinks are common at h = 1e-4
+
+
+def test_multi_context_launches_match_single_context(adj, golden):
+    """Poses of two receptors in one launch (pose kinematics forward and backward, docking
+    energy, score adjoint) equal the per-context launches bit for bit."""
+    torch = pytest.importorskip("torch")
+    from pxdock_gb300 import autograd as AG
+    dev = torch.device("cuda", 0)
+    rec2 = model.Receptor.from_json(synth.make_receptor(seed=5, n_heavy=500, cube=18.0, cavity=6.0))
+    lig2 = model.Ligand.from_json(synth.make_ligand(seed=7, n_heavy=18, n_rot=3))
+    c2 = native.Context(0)
+    c2.set_receptor(rec2)
+    c2.build_grid(model.make_box((0.0, 0.0, 0.0), (16.0,) * 3, 0.375), sorted(set(int(t) for t in lig2.vdw_type)))
+    c2.set_scoring_function(0, adj["sf"])
+    l2 = c2.add_ligand(lig2)
+    c1 = adj["ctx"]
+    c1.build_grid(model.make_box((0.0, 0.0, 0.0), (16.0,) * 3, 0.375),
+                  sorted(set(int(t) for t in adj["lig"].vdw_type)))
+    ligs = [adj["lig"], lig2]
+    A = max(l.n_atoms for l in ligs)
+    D = 7 + max(l.n_torsions for l in ligs)
+    P = 6
+    rng = np.random.default_rng(11)
+    order = np.array([0, 1, 1, 0, 1, 0])  # interleaved contexts
+    ref = np.zeros((P, A, 3), np.float32)
+    q = np.zeros((P, D), np.float32)
+    for p, c in enumerate(order):
+        l = ligs[c]
+        ref[p, : l.n_atoms] = l.poses[0] - l.poses[0].mean(axis=0)
+        qq = rng.normal(size=4)
+        q[p, :3] = rng.uniform(-2, 2, 3)
+        q[p, 3:7] = qq / np.linalg.norm(qq)
+        q[p, 7:7 + l.n_torsions] = rng.uniform(-1, 1, l.n_torsions)
+    t = lambda a, dt=torch.float32: torch.tensor(a, dtype=dt, device=dev)
+    ctx_ids = t(order, torch.int32)
+    lig_ids = t([adj["lid"] if c == 0 else l2 for c in order], torch.int32)
+    qt = t(q).requires_grad_(True)
+    xyz = AG.ligand_pose_multi([c1, c2], ctx_ids, lig_ids, t(ref), qt)
+    e = AG.docking_energy([c1, c2], lig_ids, xyz, ctx_ids=ctx_ids,
+                          rec_tors=torch.zeros((P, 3), dtype=torch.float32, device=dev))
+    wt = t(adj["w"], torch.float64)
+    tab = t(adj["tab"])
+    s = AG.empirical_score([c1, c2], lig_ids, xyz, wt, tab, ctx_ids=ctx_ids,
+                           rec_tors=torch.zeros((P, 3), dtype=torch.float32, device=dev))
+    (e + s).sum().backward()
+    for p, c in enumerate(order):
+        l, ctx, lid = ligs[c], [c1, c2][c], lig_ids[p:p + 1]
+        n, T = l.n_atoms, l.n_torsions
+        qp = qt.detach()[p:p + 1]
+        one = AG.ligand_pose(ctx, int(lid.item()), t(ref[p, :n]), qp[:, :3].clone().requires_grad_(True),
+                             qp[:, 3:7].clone().requires_grad_(True), qp[:, 7:7 + T].clone().requires_grad_(True))
+        torch.testing.assert_close(one, xyz.detach()[p:p + 1, :n], rtol=0, atol=0)
+        rt = torch.zeros((1, 3), dtype=torch.float32, device=dev) if ctx.n_rotors else None
+        e1 = AG.docking_energy(ctx, lid, one.detach(), rec_tors=rt)
+        assert e1.item() == e.detach()[p].item()
+        s1 = AG.empirical_score(ctx, lid, one.detach(), wt, tab, rec_tors=rt)
+        assert s1.item() == s.detach()[p].item()
+    c2.close()
