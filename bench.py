@@ -566,6 +566,166 @@ def diff_cpu_baseline(cplx, dofs, box, sf, weights, tables, target_s=10.0):
                       % (n, lig.n_atoms, threads, dt)}
 
 
+def unroll_complexes(n_complexes, n_receptors=64, seed0=200):
+    """Seeded complexes of the unrolled-optimisation configuration: n_receptors pockets
+    (600 heavy atoms + polar H in a 20 A cube) x distinct ligands of U{15..50} heavy atoms
+    and U{0..12} rotatable bonds, complex c = (pocket c % n_receptors, its own ligand)."""
+    from pxdock_gb300 import model, synth
+
+    rng = np.random.default_rng(seed0)
+    recs = [model.Receptor.from_json(synth.make_receptor(seed=seed0 + r, n_heavy=600, cube=20.0, cavity=6.0))
+            for r in range(min(n_receptors, n_complexes))]
+    ligs, k = [], 0
+    while len(ligs) < n_complexes:
+        h, r = int(rng.integers(15, 51)), int(rng.integers(0, 13))
+        k += 1
+        try:
+            lj = synth.make_ligand(seed=9000 + k, n_heavy=h, n_rot=min(r, h // 3), n_n=max(1, round(0.12 * h)),
+                                   n_o=max(1, round(0.15 * h)), n_other=round(0.03 * h))
+        except RuntimeError:
+            continue
+        ligs.append(model.Ligand.from_json(lj))
+    return recs, ligs
+
+
+def run_unroll(args):
+    """Differentiation through optimisation: 50 unrolled L-BFGS steps (checkpoints every
+    10) over pose DOFs on the differentiable empirical score, for every pose of every
+    complex, then the gradient of a pose-RMSD loss against seeded target poses with
+    respect to the 36 weights and the 32 x 256 pair tables. A step is forward + backward."""
+    import torch
+
+    from pxdock_gb300 import abi, model, native
+    from pxdock_gb300 import unroll as UN
+
+    torch.cuda.set_device(0)
+    native.load(auto_build=True)
+    dev = torch.device("cuda", 0)
+    sf, _ = model.load_scoring_function(os.path.join(REPO, "protenix-dock_gb300", "pxdock_gb300", "data",
+                                                     "scoring_function.json"))
+    n_cplx, P_each, K = args.complexes, args.poses_per_ligand, args.unroll_steps
+    recs, ligs = unroll_complexes(n_cplx)
+    ctxs = []
+    for r in recs:
+        c = native.Context(0)
+        c.set_receptor(r)
+        c.set_scoring_function(0, sf)
+        ctxs.append(c)
+    lig_of = [ctxs[c % len(ctxs)].add_ligand(ligs[c]) for c in range(n_cplx)]
+    A = max(l.n_atoms for l in ligs)
+    D = 7 + max(l.n_torsions for l in ligs)
+    n = n_cplx * P_each
+    cplx = np.repeat(np.arange(n_cplx), P_each)
+    ref = np.zeros((n, A, 3), np.float32)
+    for c, l in enumerate(ligs):
+        ref[c * P_each:(c + 1) * P_each, : l.n_atoms] = l.poses[0] - l.poses[0].mean(axis=0)
+    rng = np.random.default_rng(5)
+    nt = [ligs[c].n_torsions for c in cplx]
+    # seeded target poses; each start is its target perturbed (centre ~0.7 A, orientation
+    # ~0.1 per quaternion component, torsions ~0.4 rad)
+    qt = UN.random_dofs(rng, nt, D, centre_scale=2.0, tors_scale=np.pi)
+    q0 = qt.copy()
+    q0[:, :3] += rng.normal(scale=0.7, size=(n, 3))
+    q0[:, 3:7] += rng.normal(scale=0.1, size=(n, 4))
+    q0[:, 3:7] /= np.linalg.norm(q0[:, 3:7], axis=1, keepdims=True)
+    for p in range(n):
+        q0[p, 7:7 + nt[p]] += rng.normal(scale=0.4, size=nt[p])
+    n_atoms = torch.tensor([ligs[c].n_atoms for c in cplx], device=dev)
+
+    def backend(sel):
+        return UN.KernelBackend(ctxs, torch.tensor((cplx[sel] % len(ctxs)).astype(np.int32), device=dev),
+                                torch.tensor(np.array(lig_of)[cplx[sel]].astype(np.int32), device=dev),
+                                torch.tensor(ref[sel], device=dev), D)
+
+    def train_step(be, sel, steps=K):
+        w = torch.tensor(abi.sf_weights(sf), dtype=torch.float64, device=dev, requires_grad=True)
+        t = torch.tensor(abi.smooth_pair_tables(1), dtype=torch.float32, device=dev, requires_grad=True)
+        q = torch.tensor(q0[sel], dtype=torch.float32, device=dev)
+        target = UN.place(be, torch.tensor(qt[sel], dtype=torch.float32, device=dev)).detach()
+        qK = UN.lbfgs_unroll(be, q, w, t, steps=steps, history=8, cap=0.3, every=10)
+        loss = UN.rmsd_loss(UN.place(be, qK), target, n_atoms[sel])
+        loss.backward()
+        return loss, w.grad, t.grad
+
+    allsel = np.arange(n)
+    be = backend(allsel)
+    stream = torch.cuda.Stream(dev)
+    ms = []
+    torch.cuda.reset_peak_memory_stats(dev)
+    free0, total_mem = torch.cuda.mem_get_info(dev)
+    for k in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            loss, gw, gt = train_step(be, allsel)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            ms.append(a.elapsed_time(b))
+    peak_torch = torch.cuda.max_memory_allocated(dev)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    t_ms = float(np.mean(ms))
+    line = {"metric": "unrolled-optimisation training steps/s (50 L-BFGS steps, checkpoints every 10, "
+                      "RMSD loss to 36 weights + 32x256 pair tables)", "value": 1e3 / t_ms, "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "gpu_launches": int(be.launches // max(1, args.warmup + args.steps)) * args.steps,
+            "config": {"workload": "differentiation through optimisation: %d complexes (%d pockets x own ligand, "
+                                   "ligands %d-%d atoms, 0-%d torsions) x %d poses, %d unrolled L-BFGS steps "
+                                   "(m=8, step cap 0.3), checkpoints every 10; objective = differentiable "
+                                   "empirical score (no maps needed)"
+                                   % (n_cplx, len(ctxs), min(l.n_atoms for l in ligs), max(l.n_atoms for l in ligs),
+                                      max(l.n_torsions for l in ligs), P_each, K),
+                       "poses": n},
+            "poses_per_s": n / t_ms * 1e3,
+            "peak_hbm": {"torch_max_allocated_gb": peak_torch / 1e9,
+                         "device_used_gb": (total_mem - min(free0, free1)) / 1e9},
+            "loss": float(loss.item())}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"], line["gradient_error"] = unroll_cpu_check(args, ctxs, recs, ligs, lig_of, ref, q0, qt,
+                                                                        sf, D, K, P_each, backend, train_step)
+        _, line["gradient_error_5_steps"] = unroll_cpu_check(args, ctxs, recs, ligs, lig_of, ref, q0, qt, sf, D, 5,
+                                                             P_each, backend, train_step)
+    print(json.dumps(line))
+    for c in ctxs:
+        c.close()
+    return 0
+
+
+def unroll_cpu_check(args, ctxs, recs, ligs, lig_of, ref, q0, qt, sf, D, K, P_each, backend, train_step,
+                     n_check=8):
+    """The same unroll on the first n_check complexes in FP64 on the host cores (the
+    oracle's port as backend): its time, and the relative error of the GPU gradient."""
+    import torch
+
+    import unroll_ref as U
+    from pxdock_gb300 import abi
+    from pxdock_gb300 import unroll as UN
+
+    sel = np.arange(n_check * P_each)
+    gl, gw, gt = train_step(backend(sel), sel, K)
+    cplx = sel // P_each
+    threads = cpu_threads()
+    be = U.PortBackend([U.Pose(recs[c % len(recs)], ligs[c], sf, ref[p, : ligs[c].n_atoms], D)
+                        for p, c in zip(sel, cplx)], threads=threads)
+    w = torch.tensor(abi.sf_weights(sf), requires_grad=True)
+    t = torch.tensor(abi.smooth_pair_tables(1), requires_grad=True)
+    t0 = time.perf_counter()
+    target = UN.place(be, torch.tensor(qt[sel])).detach()
+    qK = UN.lbfgs_unroll(be, torch.tensor(q0[sel]), w, t, steps=K, history=8, cap=0.3, every=10)
+    loss = UN.rmsd_loss(UN.place(be, qK), target, torch.tensor([ligs[c].n_atoms for c in cplx]))
+    loss.backward()
+    dt = time.perf_counter() - t0
+    rw = np.linalg.norm(gw.cpu().numpy() - w.grad.numpy()) / np.linalg.norm(w.grad.numpy())
+    rt = np.linalg.norm(gt.cpu().numpy().reshape(-1) - t.grad.numpy().reshape(-1)) / np.linalg.norm(t.grad.numpy())
+    cpu = {"value": 1.0 / dt * (n_check * P_each) / len(q0), "unit": "steps/s", "cores": threads, "kind": "port",
+           "sample": "%d complexes x %d poses (of %d), the same unroll on the FP64 C port, %d threads, %.1f s; "
+                     "value scaled to the full workload" % (n_check, P_each, len(q0) // P_each, threads, dt)}
+    err = {"complexes": n_check, "unrolled_steps": K, "loss_gpu": float(gl.item()), "loss_fp64": float(loss.item()),
+           "weights_rel_l2": float(rw), "tables_rel_l2": float(rt)}
+    return cpu, err
+
+
 def run_evaluate(args):
     """Score+gradient evaluations/s of the bench workload's poses (one evaluation per pose
     per launch, pxd_score_grad_dev), inputs resident in HBM, L2 flushed between launches."""
@@ -622,11 +782,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "docking", "differentiate"],
+    ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "docking", "differentiate", "unroll"],
                     help="optimize: the headline (one ligand, 65,536 poses); screening: uneven "
                          "ligands batched in one launch")
     ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
-    ap.add_argument("--complexes", type=int, default=DIFF_COMPLEXES, help="differentiate: number of complexes")
+    ap.add_argument("--complexes", type=int, default=None,
+                    help="differentiate / unroll: number of complexes (64 / 1024)")
+    ap.add_argument("--unroll-steps", type=int, default=50, help="unroll: L-BFGS steps")
     ap.add_argument("--walkers", type=int, default=64, help="docking: Monte-Carlo walkers (exhaustiveness)")
     ap.add_argument("--mc-steps", type=int, default=2000, help="docking: Monte-Carlo steps per walker")
     ap.add_argument("--relax-steps", type=int, default=300, help="docking: L-BFGS iterations per step")
@@ -642,7 +804,13 @@ def main():
     if args.workload == "docking":
         return run_docking(args)
     if args.workload == "differentiate":
+        args.complexes = args.complexes or DIFF_COMPLEXES
         return run_differentiate(args)
+    if args.workload == "unroll":
+        args.complexes = args.complexes or 1024
+        if args.poses_per_ligand == 256:
+            args.poses_per_ligand = 32
+        return run_unroll(args)
     if args.workload == "evaluate":
         return run_evaluate(args)
 

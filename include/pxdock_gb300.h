@@ -462,6 +462,23 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* contexts, int32_t n_contexts
                                 double* score_dev, double* features_dev, float* dxyz_dev,
                                 double* dweights_dev, double* dtables_dev, void* stream);
 
+/* Second-order products of the same score along a direction of the ligand coordinates
+ * (forward-mode over the adjoint, derivatives almost everywhere): for each pose p with
+ * direction xyz_dir [P][max_atoms][3] and output weight grad_out[p],
+ *   dxyz_dir [P][max_atoms][3] = grad_out_p * H_p xyz_dir_p   (H_p = d2 S_p / dx2),
+ *   features_dir [P][28]       = the features' derivatives along xyz_dir_p,
+ *   dweights_dir [36], dtables_dir [32][256] += sum_p grad_out_p * d/dw, d/dT of
+ *                                (xyz_dir_p . dS_p/dx)  (the mixed derivatives).
+ * Outputs may be NULL; the same context rules as pxd_score_adjoint_multi_dev. */
+int pxd_score_hvp_multi_dev(pxd_context* const* contexts, int32_t n_contexts, int32_t which,
+                            int32_t n_poses, int32_t max_atoms, const int32_t* context_ids_dev,
+                            const int32_t* ligand_ids_dev, const float* lig_xyz_dev,
+                            const float* xyz_dir_dev, const float* rec_tors_dev,
+                            const double* weights_dev, const float* tables_dev,
+                            const double* grad_out_dev, double* features_dir_dev,
+                            float* dxyz_dir_dev, double* dweights_dir_dev,
+                            double* dtables_dir_dev, void* stream);
+
 /* Host-buffer version for one ligand (double in/out; tables may be NULL, grad_out NULL
  * means 1 for every pose). */
 int pxd_score_adjoint(pxd_context* ctx, int32_t which, int32_t ligand_id, int32_t n_poses,
@@ -489,6 +506,20 @@ int pxd_ligand_pose_multi_dev(pxd_context* const* contexts, int32_t n_contexts, 
                               const int32_t* lig_ids_dev, const float* xyz_ref_dev,
                               const float* dofs_dev, float* xyz_out_dev, const float* atom_grad_dev,
                               float* dofs_grad_dev, void* stream);
+
+/* Directional derivatives of the multi-context pose kinematics along a DOF direction
+ * dofs_dir [P][dof] at the poses xyz [P][max_atoms][3] = placed from dofs:
+ *   atom_grad NULL:  out_dir [P][max_atoms][3] = dx along dofs_dir (forward mode);
+ *   atom_grad set:   out_dir [P][dof] = derivative along dofs_dir of the backward map
+ *                    (dofs, x, dE/dx) -> dE/dq, with xyz_dir = dx along dofs_dir and
+ *                    atom_grad_dir = d(dE/dx) along it (H_x xyz_dir). This is the
+ *                    DOF-space Hessian-vector product of E. */
+int pxd_ligand_pose_dir_multi_dev(pxd_context* const* contexts, int32_t n_contexts, int32_t n_poses,
+                                  int32_t max_atoms, int32_t dof, const int32_t* ctx_ids_dev,
+                                  const int32_t* lig_ids_dev, const float* xyz_dev, const float* dofs_dev,
+                                  const float* dofs_dir_dev, const float* xyz_dir_dev,
+                                  const float* atom_grad_dev, const float* atom_grad_dir_dev,
+                                  float* out_dir_dev, void* stream);
 
 /* Backward of pxd_ligand_pose_dev: from dL/dx [P][N][3] at xyz [P][N][3], writes
  * dL/dcentre [P][3], dL/dquaternion [P][4] (through the normalisation) and

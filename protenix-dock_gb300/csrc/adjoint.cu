@@ -35,6 +35,7 @@ struct AdjArgs {
     int tors_stride;         // receptor torsions per pose row
     const int* lig_ids;
     const float* xyz;
+    const float* xyz_t;      // [n_poses][max_atoms][3] direction (tangent launches)
     const float* tors;
     int max_atoms;
     int n_poses;
@@ -61,8 +62,9 @@ __device__ void adj_receptor_rotors(const DevReceptor& R, const float* t, float4
     __syncwarp();
 }
 
-template <bool kGrad, bool kMulti, int kMinBlocks>
-__global__ void __launch_bounds__(kAdjWarps * kWarp, kMinBlocks) score_adjoint_kernel(const __grid_constant__ AdjArgs a) {
+// S = float: scores, features and gradients; S = Dual: their derivatives along xyz_t.
+template <bool kGrad, bool kMulti, class S>
+__global__ void __launch_bounds__(kAdjWarps * kWarp, 2) score_adjoint_kernel(const __grid_constant__ AdjArgs a) {
     extern __shared__ __align__(16) unsigned char adj_smem[];
     double* s_w = reinterpret_cast<double*>(adj_smem);  // [36] weights
     double* s_dw = s_w + kNumW;                         // [warps][36] weight gradient per warp
@@ -72,10 +74,12 @@ __global__ void __launch_bounds__(kAdjWarps * kWarp, kMinBlocks) score_adjoint_k
     float* warp_base = tgrad ? s_tg + kTabN : s_tg;
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
-    const int per_warp = 4 * (2 * a.max_atoms + a.max_mov + 1) + PXD_MAX_RECEPTOR_TORSIONS;
+    constexpr int kSlices = IsDual<S>::value ? 3 : 2;  // X, G (and the tangents XT)
+    const int per_warp = 4 * (kSlices * a.max_atoms + a.max_mov + 1) + PXD_MAX_RECEPTOR_TORSIONS;
     float4* X = reinterpret_cast<float4*>(warp_base + wib * per_warp);
     float4* G = X + a.max_atoms;
-    float4* loc = G + a.max_atoms;
+    float4* XT = G + a.max_atoms;
+    float4* loc = G + (kSlices - 1) * a.max_atoms;
     float* tq = reinterpret_cast<float*>(loc + a.max_mov + 1);
     for (int k = threadIdx.x; k < kNumW; k += blockDim.x) {
         s_w[k] = a.weights[k];
@@ -102,6 +106,10 @@ __global__ void __launch_bounds__(kAdjWarps * kWarp, kMinBlocks) score_adjoint_k
             X[i] = make_float4(px[3 * i], px[3 * i + 1], px[3 * i + 2], 0.f);
             G[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        if (IsDual<S>::value) {
+            const float* pt = a.xyz_t + static_cast<size_t>(pose) * a.max_atoms * 3;
+            for (int i = lane; i < L.n_atoms; i += kWarp) XT[i] = make_float4(pt[3 * i], pt[3 * i + 1], pt[3 * i + 2], 0.f);
+        }
         for (int r = lane; r < R; r += kWarp) tq[r] = a.tors[static_cast<size_t>(pose) * a.tors_stride + r];
         __syncwarp();
         adj_receptor_rotors(C.rec, tq, loc, lane);
@@ -111,8 +119,8 @@ __global__ void __launch_bounds__(kAdjWarps * kWarp, kMinBlocks) score_adjoint_k
         ap.tgrad = tgrad ? s_tg : nullptr;
         ap.g = kGrad ? static_cast<float>(a.grad_out[pose]) : 0.f;
         double f[kNumF];
-        score_adjoint_pose<kGrad>(C.env, L, X, loc, ap, G, lane, f);
-        if (a.score && lane == 0) a.score[pose] = combine_features(s_w, f);
+        score_adjoint_pose<kGrad, S>(C.env, L, X, XT, loc, ap, G, lane, f);
+        if (!IsDual<S>::value && a.score && lane == 0) a.score[pose] = combine_features(s_w, f);
         if (a.features) {
             double* fo = a.features + static_cast<size_t>(pose) * kNumF;
 #pragma unroll
@@ -156,8 +164,9 @@ __global__ void partial_sum_kernel(const T* __restrict__ part, int n_blocks, int
     out[k] += s;
 }
 
-static size_t adj_smem_bytes(int max_atoms, int n_mov, bool tgrad) {
-    const size_t per_warp = 4 * (2 * static_cast<size_t>(max_atoms) + n_mov + 1) + PXD_MAX_RECEPTOR_TORSIONS;
+static size_t adj_smem_bytes(int max_atoms, int n_mov, bool tgrad, bool tangent) {
+    const size_t per_warp =
+        4 * ((tangent ? 3 : 2) * static_cast<size_t>(max_atoms) + n_mov + 1) + PXD_MAX_RECEPTOR_TORSIONS;
     return sizeof(double) * (1 + kAdjWarps) * kNumW + sizeof(float) * (kNumW + 4) +
            (tgrad ? sizeof(float) * kTabN : 0) +
            sizeof(float) * per_warp * kAdjWarps;
@@ -192,11 +201,16 @@ int pxd_score_adjoint_dev(pxd_context* ctx, int32_t which, int32_t n_poses, int3
                                        grad_out, score, features, dxyz, dweights, dtables, stream);
 }
 
-int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t which, int32_t n_poses,
-                                int32_t max_atoms, const int32_t* ctx_ids, const int32_t* ids, const float* xyz,
-                                const float* tors, const double* weights, const float* tables,
-                                const double* grad_out, double* score, double* features, float* dxyz,
-                                double* dweights, double* dtables, void* stream) {
+}  // extern "C"
+
+namespace pxd {
+
+// Shared launcher of the value, adjoint (xyz_t NULL) and tangent (xyz_t set) launches.
+static int launch_adjoint(pxd_context* const* ctxs, int32_t n_ctx, int32_t which, int32_t n_poses,
+                          int32_t max_atoms, const int32_t* ctx_ids, const int32_t* ids, const float* xyz,
+                          const float* xyz_t, const float* tors, const double* weights, const float* tables,
+                          const double* grad_out, double* score, double* features, float* dxyz, double* dweights,
+                          double* dtables, void* stream) {
     if (!ctxs || n_ctx < 1 || !ctxs[0]) return PXD_ERR_INVALID;
     pxd_context* ctx = ctxs[0];  // errors are reported here
     if (which < 0 || which > 1 || n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS || !weights ||
@@ -204,6 +218,8 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t
         return set_error(ctx, PXD_ERR_INVALID, "bad adjoint batch");
     if (grad_out && !dweights && !dxyz && !dtables)
         return set_error(ctx, PXD_ERR_INVALID, "adjoint call without a gradient output");
+    const bool tangent = xyz_t != nullptr;
+    if (tangent && !grad_out) return set_error(ctx, PXD_ERR_INVALID, "a tangent launch needs grad_out");
     cudaSetDevice(ctx->device);
     const bool multi = n_ctx > 1;
     std::vector<AdjCtx> table(n_ctx);
@@ -228,26 +244,18 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t
     if (n_poses == 0) return PXD_OK;
     const bool grad = grad_out != nullptr;
     const bool tgrad = grad && dtables && tables;
-    const size_t smem = adj_smem_bytes(max_atoms, max_mov, tgrad);
+    const size_t smem = adj_smem_bytes(max_atoms, max_mov, tgrad, tangent);
     if (smem > 227 * 1024) return set_error(ctx, PXD_ERR_INVALID, "adjoint shared memory beyond 227 KB: lower max_atoms");
-    // register budget: 128 per thread (2 resident blocks) or 80 (3 blocks); PXD_ADJ_MIN_BLOCKS
-    // overrides the default of 2
-    static const int min_blocks = [] {
-        const char* e = std::getenv("PXD_ADJ_MIN_BLOCKS");
-        return e && std::atoi(e) == 3 ? 3 : 2;
-    }();
-    const bool three = min_blocks == 3;
     const void* fn;
-    if (grad)
-        fn = multi ? (three ? reinterpret_cast<const void*>(score_adjoint_kernel<true, true, 3>)
-                            : reinterpret_cast<const void*>(score_adjoint_kernel<true, true, 2>))
-                   : (three ? reinterpret_cast<const void*>(score_adjoint_kernel<true, false, 3>)
-                            : reinterpret_cast<const void*>(score_adjoint_kernel<true, false, 2>));
+    if (tangent)
+        fn = multi ? reinterpret_cast<const void*>(score_adjoint_kernel<true, true, Dual>)
+                   : reinterpret_cast<const void*>(score_adjoint_kernel<true, false, Dual>);
+    else if (grad)
+        fn = multi ? reinterpret_cast<const void*>(score_adjoint_kernel<true, true, float>)
+                   : reinterpret_cast<const void*>(score_adjoint_kernel<true, false, float>);
     else
-        fn = multi ? (three ? reinterpret_cast<const void*>(score_adjoint_kernel<false, true, 3>)
-                            : reinterpret_cast<const void*>(score_adjoint_kernel<false, true, 2>))
-                   : (three ? reinterpret_cast<const void*>(score_adjoint_kernel<false, false, 3>)
-                            : reinterpret_cast<const void*>(score_adjoint_kernel<false, false, 2>));
+        fn = multi ? reinterpret_cast<const void*>(score_adjoint_kernel<false, true, float>)
+                   : reinterpret_cast<const void*>(score_adjoint_kernel<false, false, float>);
     int rc = cuda_check(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   static_cast<int>(smem)), "adjoint smem");
     if (rc) return rc;
@@ -267,13 +275,14 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t
     a.tors_stride = max_rot;
     a.lig_ids = ids;
     a.xyz = xyz;
+    a.xyz_t = xyz_t;
     a.tors = tors;
     a.max_atoms = max_atoms;
     a.n_poses = n_poses;
     a.weights = weights;
     a.tables = tables;
     a.grad_out = grad_out;
-    a.score = score;
+    a.score = tangent ? nullptr : score;
     a.features = features;
     a.dxyz = dxyz;
     a.part_w = nullptr;
@@ -299,11 +308,6 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t
         void* params[] = {&a};
         rc = cuda_check(ctx, cudaLaunchKernel(fn, dim3(blocks), dim3(kAdjWarps * kWarp), params, smem, s),
                         "score_adjoint_kernel launch");
-        if (rc) {
-            if (mem) cudaFreeAsync(mem, s);
-            return rc;
-        }
-        rc = cuda_check(ctx, cudaGetLastError(), "score_adjoint_kernel launch");
     }
     if (!rc && grad && dweights) {
         partial_sum_kernel<double><<<1, 64, 0, s>>>(a.part_w, blocks, kNumW, dweights);
@@ -315,6 +319,29 @@ int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t
     }
     if (mem) cudaFreeAsync(mem, s);
     return rc;
+}
+
+}  // namespace pxd
+
+extern "C" {
+
+int pxd_score_adjoint_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t which, int32_t n_poses,
+                                int32_t max_atoms, const int32_t* ctx_ids, const int32_t* ids, const float* xyz,
+                                const float* tors, const double* weights, const float* tables,
+                                const double* grad_out, double* score, double* features, float* dxyz,
+                                double* dweights, double* dtables, void* stream) {
+    return launch_adjoint(ctxs, n_ctx, which, n_poses, max_atoms, ctx_ids, ids, xyz, nullptr, tors, weights, tables,
+                          grad_out, score, features, dxyz, dweights, dtables, stream);
+}
+
+int pxd_score_hvp_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t which, int32_t n_poses,
+                            int32_t max_atoms, const int32_t* ctx_ids, const int32_t* ids, const float* xyz,
+                            const float* xyz_dir, const float* tors, const double* weights, const float* tables,
+                            const double* grad_out, double* features_dir, float* dxyz_dir, double* dweights_dir,
+                            double* dtables_dir, void* stream) {
+    if (!xyz_dir) return ctxs && ctxs[0] ? set_error(ctxs[0], PXD_ERR_INVALID, "direction required") : PXD_ERR_INVALID;
+    return launch_adjoint(ctxs, n_ctx, which, n_poses, max_atoms, ctx_ids, ids, xyz, xyz_dir, tors, weights, tables,
+                          grad_out, nullptr, features_dir, dxyz_dir, dweights_dir, dtables_dir, stream);
 }
 
 int pxd_score_adjoint(pxd_context* ctx, int32_t which, int32_t lig, int32_t n_poses, const double* xyz,

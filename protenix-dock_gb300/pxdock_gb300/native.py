@@ -86,6 +86,8 @@ def load(auto_build=False):
     lib.pxd_score_adjoint_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 13
     lib.pxd_ligand_pose_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 8
     lib.pxd_score_grad_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32] + [vp] * 8
+    lib.pxd_score_hvp_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 13
+    lib.pxd_ligand_pose_dir_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 10
     lib.pxd_ligand_pose_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 6
     lib.pxd_ligand_pose_backward_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 8
     _lib = lib
@@ -118,6 +120,31 @@ def score_grad_multi_dev(contexts, n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz
     arr = (C.c_void_p * len(contexts))(*[c.h.value for c in contexts])
     rc = lib.pxd_score_grad_multi_dev(arr, len(contexts), n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr, tors_ptr,
                                       energy_ptr, lig_grad_ptr, tors_grad_ptr, stream)
+    if rc != 0:
+        raise NativeError(rc, lib.pxd_last_error(contexts[0].h).decode())
+
+
+def ligand_pose_dir_multi_dev(contexts, n_poses, max_atoms, dof, ctx_ids_ptr, lig_ids_ptr, xyz_ptr, dofs_ptr,
+                              dofs_dir_ptr, xyz_dir_ptr, atom_grad_ptr, atom_grad_dir_ptr, out_dir_ptr, stream=None):
+    """pxd_ligand_pose_dir_multi_dev: kinematics JVP, or the derivative of the pose backward."""
+    lib = load()
+    arr = (C.c_void_p * len(contexts))(*[c.h.value for c in contexts])
+    rc = lib.pxd_ligand_pose_dir_multi_dev(arr, len(contexts), n_poses, max_atoms, dof, ctx_ids_ptr, lig_ids_ptr,
+                                           xyz_ptr, dofs_ptr, dofs_dir_ptr, xyz_dir_ptr, atom_grad_ptr,
+                                           atom_grad_dir_ptr, out_dir_ptr, stream)
+    if rc != 0:
+        raise NativeError(rc, lib.pxd_last_error(contexts[0].h).decode())
+
+
+def score_hvp_multi_dev(contexts, which, n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr, xyz_dir_ptr, tors_ptr,
+                        weights_ptr, tables_ptr, grad_out_ptr, features_dir_ptr, dxyz_dir_ptr, dweights_dir_ptr,
+                        dtables_dir_ptr, stream=None):
+    """pxd_score_hvp_multi_dev over a list of Contexts (integer device addresses)."""
+    lib = load()
+    arr = (C.c_void_p * len(contexts))(*[c.h.value for c in contexts])
+    rc = lib.pxd_score_hvp_multi_dev(arr, len(contexts), which, n_poses, max_atoms, ctx_ids_ptr, ids_ptr, xyz_ptr,
+                                     xyz_dir_ptr, tors_ptr, weights_ptr, tables_ptr, grad_out_ptr, features_dir_ptr,
+                                     dxyz_dir_ptr, dweights_dir_ptr, dtables_dir_ptr, stream)
     if rc != 0:
         raise NativeError(rc, lib.pxd_last_error(contexts[0].h).decode())
 

@@ -278,3 +278,61 @@ def test_multi_context_launches_match_single_context(adj, golden):
         s1 = AG.empirical_score(ctx, lid, one.detach(), wt, tab, rec_tors=rt)
         assert s1.item() == s.detach()[p].item()
     c2.close()
+
+
+def test_hessian_vector_products_match_differences(adj):
+    """pxd_score_hvp_multi_dev (the adjoint run on dual numbers) against central FP64
+    differences (h = 1e-5) of the port's analytic adjoint along the same directions:
+    H v per pose, the features' derivatives, and the mixed weight / table derivatives.
+    Components whose differences change between h and h/4 (a kink inside the step) are
+    left out, at most 5 % of them."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    x, t = poses(adj, 8, 21)
+    rng = np.random.default_rng(22)
+    v = rng.normal(size=x.shape)
+    v /= np.linalg.norm(v.reshape(len(x), -1), axis=1)[:, None, None]
+    g = rng.normal(size=len(x))
+    N = adj["lig"].n_atoms
+    T = lambda a, dt=torch.float32: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    xt, vt, tt = T(x), T(v), T(t)
+    ids = torch.full((len(x),), adj["lid"], dtype=torch.int32, device=dev)
+    w, tab = T(adj["w"], torch.float64), T(adj["tab"])
+    hv = torch.zeros_like(xt)
+    fd_ = torch.zeros((len(x), abi.NUM_SCORE_FEATURES), dtype=torch.float64, device=dev)
+    dw = torch.zeros(abi.NUM_SF_WEIGHTS, dtype=torch.float64, device=dev)
+    dt = torch.zeros(abi.PAIR_TYPES * abi.PAIR_BINS, dtype=torch.float64, device=dev)
+    native.score_hvp_multi_dev([adj["ctx"]], 0, len(x), N, None, ids.data_ptr(), xt.data_ptr(), vt.data_ptr(),
+                               tt.data_ptr(), w.data_ptr(), tab.data_ptr(), T(g, torch.float64).data_ptr(),
+                               fd_.data_ptr(), hv.data_ptr(), dw.data_ptr(), dt.data_ptr(), 1)
+    torch.cuda.synchronize()
+    hv, fd_, dw, dt = hv.cpu().numpy(), fd_.cpu().numpy(), dw.cpu().numpy(), dt.cpu().numpy()
+
+    def diff(p, h):
+        a = port_diff(adj, x[p] + h * v[p], t[p], adj["w"], adj["tab"], g=g[p])
+        b = port_diff(adj, x[p] - h * v[p], t[p], adj["w"], adj["tab"], g=g[p])
+        return [(u - w_) / (2 * h) for u, w_ in zip(a[1:], b[1:])]
+
+    rw, rt, rt4 = np.zeros_like(dw), np.zeros_like(dt), np.zeros_like(dt)
+    checked = total = 0
+    for p in range(len(x)):
+        f1, gx1, gw1, gt1 = diff(p, 1e-5)
+        f4, gx4, _, gt4 = diff(p, 2.5e-6)
+        rw += gw1
+        rt += gt1
+        rt4 += gt4
+        scale = max(np.max(np.abs(gx1)), 1e-6)
+        smooth = np.abs(gx1 - gx4) <= 1e-5 * scale
+        total += smooth.size
+        checked += smooth.sum()
+        assert np.max(np.abs(hv[p] - gx1)[smooth]) <= 1e-4 * scale, (p, np.max(np.abs(hv[p] - gx1)[smooth]), scale)
+        fsmooth = np.abs(f1 - f4) <= 1e-5 * np.maximum(np.abs(f1), 1.0)
+        np.testing.assert_allclose(fd_[p][fsmooth], f1[fsmooth], rtol=1e-4, atol=1e-3)
+    assert checked >= 0.95 * total
+    np.testing.assert_allclose(dw, rw, rtol=1e-3, atol=1e-4 * np.max(np.abs(rw)))
+    # a pair crossing a bin edge inside the step moves its hat-weight derivative to the
+    # next bins: such bins differ between h and h/4 and are left out
+    tol = 1e-4 * np.max(np.abs(rt))
+    bins = np.abs(rt - rt4) <= tol
+    assert np.mean(bins[rt != 0]) >= 0.98
+    np.testing.assert_allclose(dt[bins], rt[bins], rtol=1e-3, atol=tol)
