@@ -22,6 +22,8 @@ recursion, step cap, loss), so the gradient is that of the unrolled algorithm it
 (derivatives almost everywhere of the piecewise-smooth score). Segments of `every` steps
 run under torch.utils.checkpoint and are recomputed in the backward pass.
 
+The optimiser state (DOFs, history, two-loop dots, step cap) should be FP64: with FP32
+state the two-loop products can overflow on steep LJ walls. The kernels take FP32 copies.
 The same unroll runs on a CPU FP64 backend (the oracle's port) for the error check.
 """
 import numpy as np
@@ -73,6 +75,7 @@ class KernelBackend:
     def grad(self, q, w, t):
         """(dE/dq, x, dE/dx) at q [P][D]."""
         q = q.to(torch.float32).contiguous()
+        w, t = w.to(torch.float64).contiguous(), t.to(torch.float32).contiguous()
         x = self.place(q)
         gx = torch.empty_like(x)
         native.score_adjoint_multi_dev(self.ctxs, self.which, self.P, self.A, _p(self.ctx_ids), _p(self.lig_ids),
@@ -83,9 +86,16 @@ class KernelBackend:
         return self.place_backward(q, x, gx), x, gx
 
     def hvp(self, q, u, x, gx, w, t):
-        """(H_q u, d(u.g)/dw [36], d(u.g)/dT [32*256]) at q."""
+        """(H_q u, d(u.g)/dw [36], d(u.g)/dT [32*256]) at q. Every product is linear in u,
+        so u is divided by its largest row norm N (FP64) before the FP32 kernels and the
+        results are multiplied by N in FP64: adjoints that grow over many unrolled steps
+        stay within FP32 range inside the kernels."""
         q = q.to(torch.float32).contiguous()
-        u = u.to(torch.float32).contiguous()
+        w, t = w.to(torch.float64).contiguous(), t.to(torch.float32).contiguous()
+        N = float(u.detach().to(torch.float64).norm(dim=1).max())
+        if not np.isfinite(N) or N == 0.0:
+            N = 1.0
+        u = (u.to(torch.float64) / N).to(torch.float32).contiguous()
         xd = torch.empty_like(x)
         native.ligand_pose_dir_multi_dev(self.ctxs, self.P, self.A, self.D, _p(self.ctx_ids), _p(self.lig_ids),
                                          _p(x), _p(q), _p(u), None, None, None, _p(xd), self._stream())
@@ -100,7 +110,7 @@ class KernelBackend:
                                          _p(x), _p(q), _p(u), _p(xd), _p(gx), _p(gxd), _p(hu), self._stream())
         self.launches += 5
         self.evals += self.P
-        return hu, dw, dt
+        return hu.to(torch.float64) * N, dw * N, dt * N
 
 
 class _DofGradient(torch.autograd.Function):
@@ -125,7 +135,7 @@ class _Place(torch.autograd.Function):
         x = backend.place(qq)
         fctx.save_for_backward(qq, x)
         fctx.backend, fctx.qdt = backend, q.dtype
-        return x
+        return x.to(q.dtype)
 
     @staticmethod
     def backward(fctx, gx):

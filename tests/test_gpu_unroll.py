@@ -92,14 +92,14 @@ def test_unrolled_gradient_matches_fp64(two):
     gpu, cpu, dev = two["gpu"], two["cpu"], two["dev"]
     K, hist, cap = 5, 4, 0.3
     out = {}
-    for name, be, dt_ in (("gpu", gpu, torch.float32), ("cpu", cpu, torch.float64)):
+    for name, be, dt_ in (("gpu", gpu, torch.float64), ("cpu", cpu, torch.float64)):
         d = dev if name == "gpu" else torch.device("cpu")
         w = torch.tensor(abi.sf_weights(two["sf"]), dtype=torch.float64, device=d, requires_grad=True)
-        t = torch.tensor(abi.smooth_pair_tables(1), dtype=dt_, device=d, requires_grad=True)
+        t = torch.tensor(abi.smooth_pair_tables(1), dtype=torch.float64, device=d, requires_grad=True)
         q0 = torch.tensor(two["q0"], dtype=dt_, device=d)
         target = UN.place(be, torch.tensor(two["qt"], dtype=dt_, device=d)).detach()
         qK = UN.lbfgs_unroll(be, q0, w, t, steps=K, history=hist, cap=cap, every=2)
-        loss = UN.rmsd_loss(UN.place(be, qK), target.to(dt_), torch.tensor(two["n_atoms"], device=d))
+        loss = UN.rmsd_loss(UN.place(be, qK).to(dt_), target.to(dt_), torch.tensor(two["n_atoms"], device=d))
         loss.backward()
         out[name] = (loss.item(), w.grad.cpu().numpy(), t.grad.cpu().numpy().reshape(-1))
     (lg, wg, tg), (lc, wc, tc) = out["gpu"], out["cpu"]
