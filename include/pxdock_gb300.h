@@ -500,7 +500,9 @@ int pxd_ligand_pose_dev(pxd_context* ctx, int32_t ligand_id, int32_t n_poses, co
  * contexts[ctx_ids[p]]; dofs [P][dof] (centre, quaternion w x y z, torsions padded to
  * dof); xyz_ref [P][max_atoms][3] each pose's reference coordinates. With atom_grad NULL,
  * writes xyz_out [P][max_atoms][3] (padding rows zero). With atom_grad [P][max_atoms][3]
- * (dE/dx at xyz_out), writes dofs_grad [P][dof] instead (backward; xyz_out is read). */
+ * (dE/dx at xyz_out), writes dofs_grad [P][dof] instead (backward; xyz_out is read). A
+ * pose whose ligand does not fit its row (atoms > max_atoms or 7 + torsions > dof) gets
+ * NaN outputs. */
 int pxd_ligand_pose_multi_dev(pxd_context* const* contexts, int32_t n_contexts, int32_t n_poses,
                               int32_t max_atoms, int32_t dof, const int32_t* ctx_ids_dev,
                               const int32_t* lig_ids_dev, const float* xyz_ref_dev,

@@ -54,6 +54,10 @@ __global__ void __launch_bounds__(kPoseWarps * kWarp) pose_multi_kernel(const __
     for (int pose = blockIdx.x * kPoseWarps + w; pose < a.n_poses; pose += gridDim.x * kPoseWarps) {
         const DevLigand& L = a.tabs[a.ctx_ids[pose]][a.lig_ids[pose]];
         const int N = L.n_atoms;
+        if (N > a.max_atoms || 7 + L.n_tors > a.dof) {  // the row cannot hold this ligand
+            for (int e = lane; e < 3 * a.max_atoms; e += kWarp) a.out[static_cast<size_t>(pose) * a.max_atoms * 3 + e] = nanf("");
+            continue;
+        }
         const float* xr = a.xyz_ref + static_cast<size_t>(pose) * a.max_atoms * 3;
         for (int p = lane; p < N; p += kWarp) {
             const int atom = __ldg(&L.perm[p]);
@@ -132,6 +136,11 @@ __global__ void __launch_bounds__(kPoseWarps * kWarp)
         const DevLigand& L = a.tabs[a.ctx_ids[pose]][a.lig_ids[pose]];
         const int N = L.n_atoms;
         const size_t xo = static_cast<size_t>(pose) * a.max_atoms * 3, qo = static_cast<size_t>(pose) * a.dof;
+        if (N > a.max_atoms || 7 + L.n_tors > a.dof) {
+            float* og = (IsDual<S>::value ? a.out_dir : a.dofs_grad) + qo;
+            for (int k = lane; k < a.dof; k += kWarp) og[k] = nanf("");
+            continue;
+        }
         const float* x = a.out + xo;
         const float* xt = a.xyz_dir ? a.xyz_dir + xo : nullptr;
         const float* g = a.grad + xo;
@@ -204,6 +213,10 @@ __global__ void __launch_bounds__(kPoseWarps * kWarp) pose_jvp_multi_kernel(cons
         const DevLigand& L = a.tabs[a.ctx_ids[pose]][a.lig_ids[pose]];
         const int N = L.n_atoms;
         const size_t xo = static_cast<size_t>(pose) * a.max_atoms * 3, qo = static_cast<size_t>(pose) * a.dof;
+        if (N > a.max_atoms || 7 + L.n_tors > a.dof) {
+            for (int e = lane; e < 3 * a.max_atoms; e += kWarp) a.out_dir[xo + e] = nanf("");
+            continue;
+        }
         const float* x = a.out + xo;
         const float* q = a.dofs + qo;
         const float* u = a.dofs_dir + qo;
@@ -282,8 +295,8 @@ int pxd_ligand_pose_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t n
         return set_error(ctx, PXD_ERR_INVALID, "bad pose batch");
     for (int c = 0; c < n_ctx; ++c)
         for (const LigandEntry& e : ctxs[c]->ligands)
-            if (e.dev.n_frags > kMaxFrags || e.dev.n_tors > kWarp || 7 + e.dev.n_tors > dof || e.n_atoms > max_atoms)
-                return set_error(ctx, PXD_ERR_INVALID, "a ligand exceeds the pose batch's limits");
+            if (e.dev.n_frags > kMaxFrags || e.dev.n_tors > kWarp)
+                return set_error(ctx, PXD_ERR_INVALID, "a ligand exceeds the kinematics limits (64 fragments, 32 torsions)");
     cudaSetDevice(ctx->device);
     if (n_poses == 0) return PXD_OK;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
@@ -319,8 +332,8 @@ int pxd_ligand_pose_dir_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32
         return set_error(ctx, PXD_ERR_INVALID, "bad pose batch");
     for (int c = 0; c < n_ctx; ++c)
         for (const LigandEntry& e : ctxs[c]->ligands)
-            if (e.dev.n_frags > kMaxFrags || e.dev.n_tors > kWarp || 7 + e.dev.n_tors > dof || e.n_atoms > max_atoms)
-                return set_error(ctx, PXD_ERR_INVALID, "a ligand exceeds the pose batch's limits");
+            if (e.dev.n_frags > kMaxFrags || e.dev.n_tors > kWarp)
+                return set_error(ctx, PXD_ERR_INVALID, "a ligand exceeds the kinematics limits (64 fragments, 32 torsions)");
     cudaSetDevice(ctx->device);
     if (n_poses == 0) return PXD_OK;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;

@@ -336,3 +336,45 @@ def test_hessian_vector_products_match_differences(adj):
     bins = np.abs(rt - rt4) <= tol
     assert np.mean(bins[rt != 0]) >= 0.98
     np.testing.assert_allclose(dt[bins], rt[bins], rtol=1e-3, atol=tol)
+
+
+def test_adjoint_edge_cases(adj):
+    """Empty batch, a bad ligand id (NaN score, zero gradient rows), an oversize row stride
+    (refused), and a rigid ligand (no torsions) through the multi-context kinematics."""
+    torch = pytest.importorskip("torch")
+    from pxdock_gb300 import autograd as AG
+    dev = torch.device("cuda", 0)
+    N = adj["lig"].n_atoms
+    w = torch.tensor(adj["w"], dtype=torch.float64, device=dev)
+    x = torch.tensor(np.tile(adj["lig"].poses[0], (2, 1, 1)), dtype=torch.float32, device=dev)
+    ids = torch.tensor([adj["lid"], 99], dtype=torch.int32, device=dev)
+    rt = torch.zeros((2, 3), dtype=torch.float32, device=dev)
+    s = torch.zeros(2, dtype=torch.float64, device=dev)
+    g = torch.ones(2, dtype=torch.float64, device=dev)
+    dx = torch.full_like(x, 7.0)
+    dw = torch.zeros(abi.NUM_SF_WEIGHTS, dtype=torch.float64, device=dev)
+    args = lambda n, a: (0, n, a, ids.data_ptr(), x.data_ptr(), rt.data_ptr(), w.data_ptr(), None, g.data_ptr(),
+                         s.data_ptr(), None, dx.data_ptr(), dw.data_ptr(), None, 1)
+    adj["ctx"].score_adjoint_dev(*args(0, N))
+    adj["ctx"].score_adjoint_dev(*args(2, N))
+    torch.cuda.synchronize()
+    assert np.isfinite(s[0].item()) and np.isnan(s[1].item())
+    assert torch.all(dx[1] == 0) and torch.any(dx[0] != 0)
+    with pytest.raises(native.NativeError):
+        adj["ctx"].score_adjoint_dev(*args(2, abi_max_atoms_plus_one()))
+    # a rigid ligand: DOF rows of 7, no torsion columns
+    rigid = model.Ligand.from_json(synth.make_ligand(seed=3, n_heavy=12, n_rot=0))
+    assert rigid.n_torsions == 0
+    lid = adj["ctx"].add_ligand(rigid)
+    ref = torch.tensor((rigid.poses[0] - rigid.poses[0].mean(axis=0))[None], dtype=torch.float32, device=dev)
+    q = torch.tensor([[0.5, -0.2, 0.1, 0.9, 0.1, -0.3, 0.2]], dtype=torch.float64, device=dev, requires_grad=True)
+    xyz = AG.ligand_pose_multi([adj["ctx"]], torch.zeros(1, dtype=torch.int32, device=dev),
+                               torch.tensor([lid], dtype=torch.int32, device=dev), ref, q)
+    xyz.sum().backward()
+    assert torch.allclose(q.grad[0, :3], torch.full((3,), float(rigid.n_atoms), dtype=torch.float64, device=dev))
+    adj["ctx"].clear_ligands()
+    adj["lid"] = adj["ctx"].add_ligand(adj["lig"])
+
+
+def abi_max_atoms_plus_one():
+    return 257
