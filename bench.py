@@ -668,8 +668,8 @@ def run_unroll(args):
     peak_torch = torch.cuda.max_memory_allocated(dev)
     free1, _ = torch.cuda.mem_get_info(dev)
     t_ms = float(np.mean(ms))
-    line = {"metric": "unrolled-optimisation training steps/s (50 L-BFGS steps, checkpoints every 10, "
-                      "RMSD loss to 36 weights + 32x256 pair tables)", "value": 1e3 / t_ms, "unit": "steps/s",
+    line = {"metric": "unrolled-optimisation training steps/s (%d L-BFGS steps, checkpoints every 10, "
+                      "RMSD loss to 36 weights + 32x256 pair tables)" % K, "value": 1e3 / t_ms, "unit": "steps/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "gpu_launches": int(be.launches // max(1, args.warmup + args.steps)) * args.steps,
