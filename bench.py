@@ -19,6 +19,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import threading
 import time
@@ -83,7 +84,7 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+        self.path = os.path.join(tempfile.gettempdir(), "pxdock_bench_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:

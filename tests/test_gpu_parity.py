@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path through the C ABI against the FP64 port (the oracle).
 
-Tolerances (the spec bar, written here once):
+Tolerances (the parity bar of the path, written here once):
   energy   |dE| <= 1e-3 kcal/mol on physically visited poses (ligand inside the pocket,
            no atom overlaps), relative 1e-6 of |E| elsewhere;
   gradient max|dg| <= 1e-4 * max|g| (relative to the largest component of the pose);
