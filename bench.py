@@ -374,6 +374,88 @@ def run_docking(args):
     return 0
 
 
+def run_screening_mc(args):
+    """Screening with Monte-Carlo search: --ligands uneven ligands (screening_ligands),
+    --poses-per-ligand walkers each, --mc-steps steps relaxed by up to --relax-steps L-BFGS
+    iterations (the reference search's defaults), every walker of every ligand in one
+    persistent launch over the 81^3 maps. The CPU line runs the FP64 port's walkers (same
+    seeds, moves, relaxations) on all host threads over a bounded sample, scaled."""
+    import concurrent.futures
+
+    import torch
+
+    import oracle
+    from pxdock_gb300 import model, native, synth
+
+    torch.cuda.set_device(0)
+    native.load(auto_build=True)
+    rec = model.Receptor.from_json(synth.make_receptor(seed=0))
+    box = model.make_box((0.0, 0.0, 0.0), (BOX_SIZE,) * 3, SPACING)
+    lo = np.array(box.init_xyz)
+    hi = lo + (np.array(box.npoints) - 1) * box.spacing
+    pose_sf, _ = model.load_scoring_function(os.path.join(REPO, "protenix-dock_gb300", "pxdock_gb300", "data",
+                                                          "scoring_function.json"))
+    ligs = screening_ligands(args.ligands)
+    ctx = native.Context(0)
+    ctx.set_receptor(rec)
+    types = sorted(set(int(t) for l in ligs for t in l.vdw_type))
+    ctx.build_grid(box, types)
+    ctx.set_slope(SLOPE)
+    ctx.set_scoring_function(0, pose_sf)
+    ids = [ctx.add_ligand(l) for l in ligs]
+    W = args.poses_per_ligand
+    A = max(l.n_atoms for l in ligs)
+    n = W * len(ligs)
+    starts = np.zeros((n, A, 3))
+    lig_ids = np.repeat(np.array(ids), W)
+    walker = np.tile(np.arange(W), len(ligs))
+    first = (walker == 0).astype(np.int32)
+    for k, l in enumerate(ligs):
+        starts[k * W:(k + 1) * W, : l.n_atoms] = l.poses[0]
+    p = native.mc_params(lo, hi, seed=0, max_nsteps=args.mc_steps, relax_nsteps=args.relax_steps)
+    times = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = ctx.mc_search_multi(p, lig_ids, starts, walker, first)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+    gpu_s = float(np.mean(times))
+    line = {"metric": "Monte-Carlo walker-steps/s, uneven ligands batched in one launch",
+            "value": n * args.mc_steps / gpu_s, "unit": "walker-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * gpu_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "gpu_launches": args.steps,
+            "config": {"workload": "screening with MC: %d ligands (%d-%d atoms, 0-%d torsions) x %d walkers x %d "
+                                   "MC steps, relax <= %d L-BFGS iterations, 81^3 maps, one launch"
+                                   % (len(ligs), min(l.n_atoms for l in ligs), max(l.n_atoms for l in ligs),
+                                      max(l.n_torsions for l in ligs), W, args.mc_steps, args.relax_steps)},
+            "e2e": {"value": n * args.mc_steps / gpu_s, "unit": "walker-steps/s",
+                    "h2d_bytes_per_step": int(starts.nbytes), "d2h_bytes_per_step": int(out["xyz"].nbytes + 24 * n)},
+            "status_counts": {str(k): int((out["status"] == k).sum()) for k in range(3)}}
+    if not args.no_cpu_baseline:
+        threads = cpu_threads()
+        sample = [(k, w) for k in range(0, len(ligs), max(1, len(ligs) // threads)) for w in (0,)][:threads]
+        ports = {}
+        for k, _ in sample:
+            pt = oracle.PortSystem(rec, ligs[k])
+            pt.build_grid(box, sorted(set(int(t) for t in ligs[k].vdw_type)), nthreads=threads)
+            pt.set_slope(SLOPE)
+            ports[k] = pt
+        t0 = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda kw: ports[kw[0]].mc_walker(pose_sf, lo, hi, 0, 1, ligs[kw[0]].poses[0], False,
+                                                          args.mc_steps, args.relax_steps), sample))
+        cpu_dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(sample) * args.mc_steps / cpu_dt, "unit": "walker-steps/s",
+                                "cores": threads, "kind": "port",
+                                "sample": "%d walkers (one per sampled ligand) x %d MC steps on %d threads in %.1f s"
+                                          % (len(sample), args.mc_steps, threads, cpu_dt)}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 DIFF_COMPLEXES = 64
 DIFF_POSES = 256
 DIFF_BOX = 20.0
@@ -817,7 +899,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "docking", "differentiate", "unroll"],
+    ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "screening_mc", "docking", "differentiate", "unroll"],
                     help="optimize: the headline (one ligand, 65,536 poses); screening: uneven "
                          "ligands batched in one launch")
     ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
@@ -836,6 +918,8 @@ def main():
         return run_reference(args)
     if args.workload == "screening":
         return run_screening(args)
+    if args.workload == "screening_mc":
+        return run_screening_mc(args)
     if args.workload == "docking":
         return run_docking(args)
     if args.workload == "differentiate":
