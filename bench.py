@@ -270,6 +270,9 @@ def run_screening(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     p = lbfgs_params()
     stream = torch.cuda.Stream(dev)
+    # the autotuner picks each size class's kernel variant from timed probes (on copies)
+    tuned = ctx.lbfgs_autotune_dev(p, n, max_atoms, d_ids.data_ptr(), start.data_ptr(), tors.data_ptr(),
+                                   sample=2048, probe_iters=40, stream=stream.cuda_stream)
     events = []
     for k in range(args.warmup + args.steps):
         with torch.cuda.stream(stream):
@@ -296,6 +299,7 @@ def run_screening(args):
                                       HISTORY, MAX_ITER, TOL_GRAD),
                        "l2": "flushed between steps (256 MiB write)"},
             "evals_per_s": ev / ms * 1e3, "evals_per_pose": ev / n,
+            "autotuned_variants": {str(k): v for k, v in tuned.items()},
             "status_counts": {str(k): int((status == k).sum().item()) for k in range(4)}}
     print(json.dumps(line))
     ctx.close()

@@ -339,6 +339,19 @@ int pxd_lbfgs(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t ligand_i
               int32_t n_poses, double* lig_xyz, double* rec_tors, double* energy,
               int32_t* nevals, int32_t* status);
 
+/* Autotuner of the batched optimiser (no reference counterpart). For every size class
+ * (ligands of <= 32, 64, ... 256 atoms) present in the batch, runs each register /
+ * occupancy variant of the optimiser kernel (resident blocks per SM: 4, 5, 6, unbounded)
+ * on up to `sample` of the class's poses with max_iter capped at probe_iters, times them
+ * with CUDA events, and keeps the variant with the most score+gradient evaluations per
+ * second for this context's later pxd_lbfgs* calls. Probes run on copies: the caller's
+ * poses are not modified. report [8][2] (may be NULL) receives (class bound, chosen
+ * variant), -1 after the last class. Synchronous. */
+int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t n_poses,
+                           int32_t max_atoms, const int32_t* ligand_ids_dev, const float* xyz_dev,
+                           const float* tors_dev, int32_t sample, int32_t probe_iters,
+                           int32_t* report, void* stream);
+
 /* Host-buffer version over poses of several ligands in one launch (the engine's
  * optimize over a whole ligand index): ligand_ids [n], xyz [n][max_atoms][3] and
  * torsions [n][R] (in/out, double), energy [n], nevals [n], status [n]. */

@@ -167,18 +167,29 @@ static int padded(int D) { return (D + kWarp - 1) / kWarp * kWarp; }
 using LbfgsKernelFn = void (*)(LbfgsArgs);
 
 // Register / occupancy variant of lbfgs_kernel: 0 = unconstrained registers, else the
-// minimum resident blocks per SM. PXD_LBFGS_MIN_BLOCKS overrides the default.
-static LbfgsKernelFn lbfgs_variant() {
-    static int choice = [] {
-        const char* v = std::getenv("PXD_LBFGS_MIN_BLOCKS");
-        return v ? std::atoi(v) : kDefaultMinBlocks;
-    }();
-    switch (choice) {
+// minimum resident blocks per SM.
+static LbfgsKernelFn variant_fn(int min_blocks) {
+    switch (min_blocks) {
         case 4: return lbfgs_kernel<4>;
         case 5: return lbfgs_kernel<5>;
         case 6: return lbfgs_kernel<6>;
         default: return lbfgs_kernel<0>;
     }
+}
+
+// Size class of a per-warp atom capacity: the smallest bound of 32, 64, ..., 256 it fits.
+static int class_bound(int cap) { return std::min(256, (cap + 31) / 32 * 32); }
+
+// The variant of a size class: the autotuner's choice for the class (pxd_lbfgs_autotune_dev),
+// else PXD_LBFGS_MIN_BLOCKS, else the default.
+static LbfgsKernelFn lbfgs_variant(const pxd_context* ctx, int cap) {
+    auto it = ctx->lbfgs_tuned.find(class_bound(cap));
+    if (it != ctx->lbfgs_tuned.end()) return variant_fn(it->second);
+    static int choice = [] {
+        const char* v = std::getenv("PXD_LBFGS_MIN_BLOCKS");
+        return v ? std::atoi(v) : kDefaultMinBlocks;
+    }();
+    return variant_fn(choice);
 }
 
 int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_ids,
@@ -357,16 +368,18 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     if (caps.empty() || caps.back() != max_atoms) caps.push_back(max_atoms);  // oversize / invalid ids
     const bool classes = caps.size() > 1 && n_poses >= 1024;
     if (!classes) caps.assign(1, max_atoms);
-    const LbfgsKernelFn kern = lbfgs_variant();
     struct Plan {
         int cap, dp, blocks;
         size_t smem, stride;
+        LbfgsKernelFn kern;
     };
     std::vector<Plan> plan;
     size_t hist_floats = 0;
     for (int cap : caps) {
         Plan q;
         q.cap = cap;
+        q.kern = lbfgs_variant(ctx, cap);
+        const LbfgsKernelFn kern = q.kern;
         q.dp = padded(3 * cap + ctx->rec.n_rotors);
         const int per_warp = pose_bufs_floats(cap, base.n_local) + 10 * q.dp + 4 * p.history;
         q.smem = sizeof(float) * kWarpsPerBlock * per_warp;
@@ -450,7 +463,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
             rc = cuda_check(ctx, cudaStreamWaitEvent(ks, ctx->class_events[n_cls], 0), "fork wait");
             if (rc) return rc;
         }
-        kern<<<plan[k].blocks, kWarpsPerBlock * kWarp, plan[k].smem, ks>>>(a);
+        plan[k].kern<<<plan[k].blocks, kWarpsPerBlock * kWarp, plan[k].smem, ks>>>(a);
         rc = cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
         if (rc) return rc;
         if (classes) {
@@ -538,7 +551,7 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
     const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + 10 * a.D_pad + 4 * p.history;
     const size_t smem = sizeof(float) * kWarpsPerBlock * per_warp;
-    const LbfgsKernelFn kern = lbfgs_variant();
+    const LbfgsKernelFn kern = lbfgs_variant(ctx, max_atoms);
     rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(smem)),
                     "lbfgs smem attribute");
@@ -639,4 +652,101 @@ extern "C" int pxd_score_grad_multi_dev(pxd_context* const* ctxs, int32_t n_ctx,
     }
     cudaFreeAsync(mem, s);
     return rc;
+}
+
+// ------------------------------------------------------------------ autotuner
+extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t n_poses,
+                                      int32_t max_atoms, const int32_t* ids, const float* xyz, const float* tors,
+                                      int32_t sample, int32_t probe_iters, int32_t* report, void* stream) {
+    if (!ctx) return PXD_ERR_INVALID;
+    if (!ctx->has_receptor) return set_error(ctx, PXD_ERR_STATE, "set a receptor first");
+    if (!params || n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS || sample < 1 ||
+        probe_iters < 1 || !ids || !xyz || (ctx->rec.n_rotors > 0 && !tors))
+        return set_error(ctx, PXD_ERR_INVALID, "bad autotune batch");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const int R = ctx->rec.n_rotors;
+    std::vector<int32_t> h_ids(n_poses);
+    int rc = cuda_check(ctx, cudaMemcpyAsync(h_ids.data(), ids, sizeof(int32_t) * n_poses, cudaMemcpyDeviceToHost, s),
+                        "autotune ids");
+    if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(s), "autotune ids");
+    if (rc) return rc;
+    // poses per size class (class of the pose's ligand), at most `sample` each
+    std::map<int, std::vector<int>> by_class;
+    for (int i = 0; i < n_poses; ++i) {
+        const int lid = h_ids[i];
+        if (lid < 0 || lid >= static_cast<int>(ctx->ligands.size())) continue;
+        const int n = ctx->ligands[lid].n_atoms;
+        if (n > max_atoms) continue;
+        std::vector<int>& v = by_class[class_bound(n)];
+        if (static_cast<int>(v.size()) < sample) v.push_back(i);
+    }
+    pxd_lbfgs_params p = *params;
+    p.max_iter = std::min(p.max_iter, probe_iters);
+    static const int kVariants[4] = {4, 5, 6, 0};
+    int n_report = 0;
+    for (auto& [bound, rows] : by_class) {
+        const int m = static_cast<int>(rows.size());
+        const int cap = std::min(bound, max_atoms);
+        std::vector<int> rid(m);
+        for (int k = 0; k < m; ++k) rid[k] = h_ids[rows[k]];
+        Staging st{ctx, {}};
+        int* d_ids = st.alloc<int>(m, &rc);
+        float* d_x0 = rc ? nullptr : st.alloc<float>(static_cast<size_t>(m) * cap * 3, &rc);
+        float* d_x = rc ? nullptr : st.alloc<float>(static_cast<size_t>(m) * cap * 3, &rc);
+        float* d_t0 = rc ? nullptr : st.alloc<float>(static_cast<size_t>(m) * std::max(R, 1), &rc);
+        float* d_t = rc ? nullptr : st.alloc<float>(static_cast<size_t>(m) * std::max(R, 1), &rc);
+        double* d_e = rc ? nullptr : st.alloc<double>(m, &rc);
+        int* d_n = rc ? nullptr : st.alloc<int>(m, &rc);
+        int* d_s = rc ? nullptr : st.alloc<int>(m, &rc);
+        if (rc) return rc;
+        cudaMemcpyAsync(d_ids, rid.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s);
+        for (int k = 0; k < m; ++k) {  // gather the sampled rows at the class's stride
+            cudaMemcpy2DAsync(d_x0 + static_cast<size_t>(k) * cap * 3, sizeof(float) * cap * 3,
+                              xyz + static_cast<size_t>(rows[k]) * max_atoms * 3, sizeof(float) * max_atoms * 3,
+                              sizeof(float) * cap * 3, 1, cudaMemcpyDeviceToDevice, s);
+            if (R > 0)
+                cudaMemcpyAsync(d_t0 + static_cast<size_t>(k) * R, tors + static_cast<size_t>(rows[k]) * R,
+                                sizeof(float) * R, cudaMemcpyDeviceToDevice, s);
+        }
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        double best_rate = -1.0;
+        int best = kDefaultMinBlocks;
+        std::vector<int> nev(m);
+        for (int v : kVariants) {
+            ctx->lbfgs_tuned[bound] = v;
+            cudaMemcpyAsync(d_x, d_x0, sizeof(float) * m * cap * 3, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(d_t, d_t0, sizeof(float) * m * std::max(R, 1), cudaMemcpyDeviceToDevice, s);
+            cudaEventRecord(a, s);
+            rc = launch_lbfgs(ctx, p, m, cap, d_ids, d_x, d_t, d_e, d_n, d_s, s);
+            cudaEventRecord(b, s);
+            if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(nev.data(), d_n, sizeof(int) * m, cudaMemcpyDeviceToHost, s),
+                                     "autotune evaluations");
+            if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(s), "autotune probe");
+            if (rc) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            double evals = 0.0;
+            for (int x : nev) evals += x;
+            const double rate = ms > 0.f ? evals / ms : 0.0;
+            if (rate > best_rate) {
+                best_rate = rate;
+                best = v;
+            }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        ctx->lbfgs_tuned[bound] = best;
+        if (rc) return rc;
+        if (report && n_report < kSizeClasses) {
+            report[2 * n_report] = bound;
+            report[2 * n_report + 1] = best;
+        }
+        ++n_report;
+    }
+    if (report)
+        for (int k = n_report; k < kSizeClasses; ++k) report[2 * k] = report[2 * k + 1] = -1;
+    return PXD_OK;
 }

@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -197,6 +198,8 @@ struct pxd_context {
     pxd::DevSf* d_sf[2] = {nullptr, nullptr};
     pxd_sf_params sf_host[2];
     bool sf_set[2] = {false, false};
+    // autotuned L-BFGS variant (minimum resident blocks per SM) per size-class bound
+    std::map<int, int> lbfgs_tuned;
     // scratch
     void* scratch = nullptr;
     size_t scratch_bytes = 0;

@@ -87,6 +87,8 @@ def load(auto_build=False):
     lib.pxd_ligand_pose_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 8
     lib.pxd_score_grad_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32] + [vp] * 8
     lib.pxd_score_hvp_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 13
+    lib.pxd_lbfgs_autotune_dev.argtypes = [vp, C.POINTER(abi.LbfgsParams), C.c_int32, C.c_int32, vp, vp, vp,
+                                           C.c_int32, C.c_int32, abi.i32p, vp]
     lib.pxd_ligand_pose_dir_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 10
     lib.pxd_ligand_pose_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 6
     lib.pxd_ligand_pose_backward_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 8
@@ -279,6 +281,15 @@ class Context:
         self._check(self.lib.pxd_lbfgs_dev(self.h, C.byref(params), n_poses, max_atoms, ids_ptr,
                                            xyz_ptr, tors_ptr, energy_ptr, nevals_ptr, status_ptr,
                                            stream))
+
+    def lbfgs_autotune_dev(self, params, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, sample=2048, probe_iters=40,
+                           stream=None):
+        """pxd_lbfgs_autotune_dev: times the optimiser's variants per size class on a sample of
+        the batch and keeps the fastest; returns {class bound: chosen variant}."""
+        rep = np.zeros(16, np.int32)
+        self._check(self.lib.pxd_lbfgs_autotune_dev(self.h, C.byref(params), n_poses, max_atoms, ids_ptr, xyz_ptr,
+                                                    tors_ptr, sample, probe_iters, _p(rep, C.c_int32), stream))
+        return {int(rep[2 * k]): int(rep[2 * k + 1]) for k in range(8) if rep[2 * k] >= 0}
 
     def lbfgs_dev_noalloc(self, params, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
                           nevals_ptr, status_ptr, stream=None):
