@@ -559,7 +559,7 @@ def run_differentiate(args):
         return total, q, w, t
 
     ms, e2e_ms = [], []
-    launches = 7  # pose, score value, docking energy; adjoint + 2 partial sums, pose backward
+    launches = 5  # pose, adjoint (+ its table partial sum), docking energy; pose backward
     for k in range(args.warmup + args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)

@@ -88,6 +88,8 @@ def port_lib():
                                       f64p]
         lib.po_combine_features.restype = C.c_double
         lib.po_combine_features.argtypes = [f64p, f64p]
+        lib.po_combine_grad.restype = None
+        lib.po_combine_grad.argtypes = [f64p, f64p, C.c_double, f64p]
         lib.po_vdw_check.restype = C.c_double
         lib.po_vdw_check.argtypes = [C.POINTER(abi.SfParams), C.c_int, f64p, f64p, f64p, C.c_int,
                                      f64p, i32p]

@@ -232,3 +232,46 @@ def smooth_pair_tables(seed=0):
         t[p] = wall - depth * np.exp(-((r - r0) / width) ** 2)
         t[p] *= np.clip((r[-1] - r) / 1.0, 0.0, 1.0)  # taper to zero at the cut-off
     return t.astype(np.float32).astype(np.float64)
+
+
+def weights_grad(w, f):
+    """d(sum_p g_p S_p)/dw from the weights w [36] and the g-weighted feature sum
+    f = sum_p g_p features_p [28]: the derivative of pxd's feature combination (S is
+    linear in each weight group), in the layout of pxd_sf_weights. Works on numpy arrays
+    and torch tensors."""
+    C = W_COEF
+    hb = sum(w[W_HBOND + k] * f[16 + k] for k in range(8))
+    pc = sum(w[W_PICAT + k] * f[4 + k] for k in range(4))
+    st = [sum(w[W_STACK + 4 * q + k] * f[8 + 4 * q + k] for k in range(4)) for q in range(2)]
+    d = [0.0] * NUM_SF_WEIGHTS
+    d[C + 0] = f[0]
+    d[C + 1] = w[W_VDW_SCALE] * f[1]
+    d[C + 2] = w[W_IONIC] * f[2] + w[W_IONIC + 1] * f[3]
+    d[C + 3] = pc
+    d[C + 4], d[C + 5] = st[0], st[1]
+    d[C + 6] = w[W_HBOND_SCALE] * hb
+    d[C + 7] = w[W_HYDRO_SCALE] * f[24]
+    d[C + 8] = f[25]
+    d[C + 9] = f[26]
+    d[C + 10] = 0.0 * f[0]  # GB/SA is not part of the differentiable score
+    d[W_VDW_SCALE] = w[C + 1] * f[1]
+    d[W_HYDRO_SCALE] = w[C + 7] * f[24]
+    d[W_HBOND_SCALE] = w[C + 6] * hb
+    for k in range(2):
+        d[W_IONIC + k] = w[C + 2] * f[2 + k]
+    for k in range(4):
+        d[W_PICAT + k] = w[C + 3] * f[4 + k]
+    for q in range(2):
+        for k in range(4):
+            d[W_STACK + 4 * q + k] = w[C + 4 + q] * f[8 + 4 * q + k]
+    for k in range(8):
+        d[W_HBOND + k] = w[C + 6] * w[W_HBOND_SCALE] * f[16 + k]
+    try:
+        import torch
+        if isinstance(f, torch.Tensor):
+            return torch.stack([x if isinstance(x, torch.Tensor) else torch.as_tensor(x, dtype=f.dtype,
+                                                                                     device=f.device) for x in d])
+    except ImportError:
+        pass
+    import numpy as np
+    return np.array(d, dtype=float)

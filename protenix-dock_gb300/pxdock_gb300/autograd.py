@@ -4,8 +4,9 @@ Each Function calls the library's hand-written kernels on the current torch stre
 
 - ``empirical_score(ctx, lig_ids, xyz, weights, tables)``: per-pose empirical score
   S(x; w, T) (pxd_score_adjoint_multi_dev, over one context or several in one launch).
-  Forward runs the value kernel; backward recomputes the pose inside the adjoint kernel
-  (no activations are stored besides the inputs) and returns dL/dx, dL/dw and dL/dT.
+  Forward runs the adjoint kernel once (scores, features, dS/dx, sum_p dS_p/dT); the
+  backward scales those by dL/dS, re-running the kernel only for the table gradient
+  when the per-pose output weights differ.
 - ``ligand_pose(ctx, lig, xyz_ref, centers, quats, torsions)``: torsion-tree forward
   kinematics (pxd_ligand_pose_dev) with its backward (pxd_ligand_pose_backward_dev):
   atom gradients become centre, quaternion and torsion gradients.
@@ -34,37 +35,66 @@ def _stream():
 
 
 class _EmpiricalScore(torch.autograd.Function):
+    """Forward runs the adjoint kernel once with unit output weights: scores, the
+    per-pose features, dS/dx and (when the tables need a gradient) sum_p dS_p/dT. The
+    backward scales those: dx = g_p dS_p/dx, dw from sum_p g_p features_p, and dT = g_0
+    sum_p dS_p/dT when every g_p is equal (the usual summed or averaged score); other g
+    re-run the adjoint kernel for dT."""
+
     @staticmethod
     def forward(fctx, xyz, weights, tables, pctxs, which, ctx_ids, lig_ids, rec_tors):
         P, A, _ = xyz.shape
+        dev = xyz.device
         x = xyz.detach().to(torch.float32).contiguous()
         w = weights.detach().to(torch.float64).contiguous()
         t = None if tables is None else tables.detach().to(torch.float32).contiguous()
-        score = torch.empty(P, dtype=torch.float64, device=xyz.device)
-        native.score_adjoint_multi_dev(pctxs, which, P, A, _ptr(ctx_ids), _ptr(lig_ids), _ptr(x), _ptr(rec_tors),
-                                       _ptr(w), _ptr(t), None, _ptr(score), None, None, None, None, _stream())
-        empty = torch.empty(0, device=xyz.device)
+        score = torch.empty(P, dtype=torch.float64, device=dev)
+        need_x, need_w, need_t = fctx.needs_input_grad[0], fctx.needs_input_grad[1], \
+            tables is not None and fctx.needs_input_grad[2]
+        empty = torch.empty(0, device=dev)
+        if need_x or need_w or need_t:
+            ones = torch.ones(P, dtype=torch.float64, device=dev)
+            feats = torch.empty((P, abi.NUM_SCORE_FEATURES), dtype=torch.float64, device=dev)
+            dx = torch.empty_like(x)
+            dt = torch.zeros(abi.PAIR_TYPES * abi.PAIR_BINS, dtype=torch.float64, device=dev) if need_t else None
+            native.score_adjoint_multi_dev(pctxs, which, P, A, _ptr(ctx_ids), _ptr(lig_ids), _ptr(x), _ptr(rec_tors),
+                                           _ptr(w), _ptr(t), _ptr(ones), _ptr(score), _ptr(feats), _ptr(dx), None,
+                                           _ptr(dt), _stream())
+        else:
+            feats = dx = dt = None
+            native.score_adjoint_multi_dev(pctxs, which, P, A, _ptr(ctx_ids), _ptr(lig_ids), _ptr(x), _ptr(rec_tors),
+                                           _ptr(w), _ptr(t), None, _ptr(score), None, None, None, None, _stream())
         fctx.save_for_backward(x, w, t if t is not None else empty, lig_ids,
-                               ctx_ids if ctx_ids is not None else empty, rec_tors if rec_tors is not None else empty)
+                               ctx_ids if ctx_ids is not None else empty, rec_tors if rec_tors is not None else empty,
+                               feats if feats is not None else empty, dx if dx is not None else empty,
+                               dt if dt is not None else empty)
         fctx.meta = (pctxs, which, tables is not None, xyz.dtype, weights.dtype,
                      None if tables is None else tables.dtype)
         return score
 
     @staticmethod
     def backward(fctx, grad_score):
-        x, w, t, lig_ids, ctx_ids, rec_tors = fctx.saved_tensors
+        x, w, t, lig_ids, ctx_ids, rec_tors, feats, dx, dt = fctx.saved_tensors
         pctxs, which, has_tab, xdt, wdt, tdt = fctx.meta
         P, A, _ = x.shape
         g = grad_score.detach().to(torch.float64).contiguous()
-        dx = torch.empty_like(x)
-        dw = torch.zeros(abi.NUM_SF_WEIGHTS, dtype=torch.float64, device=x.device)
-        dt = torch.zeros(abi.PAIR_TYPES * abi.PAIR_BINS, dtype=torch.float64, device=x.device) if has_tab else None
-        native.score_adjoint_multi_dev(pctxs, which, P, A, _ptr(ctx_ids if ctx_ids.numel() else None), _ptr(lig_ids),
-                                       _ptr(x), _ptr(rec_tors if rec_tors.numel() else None), _ptr(w),
-                                       _ptr(t if has_tab else None), _ptr(g), None, None, _ptr(dx), _ptr(dw),
-                                       _ptr(dt), _stream())
-        gt = dt.view(abi.PAIR_TYPES, abi.PAIR_BINS).to(tdt) if has_tab else None
-        return dx.to(xdt), dw.to(wdt), gt, None, None, None, None, None
+        gx = gw = gt = None
+        if fctx.needs_input_grad[0]:
+            gx = (dx * g.to(torch.float32)[:, None, None]).to(xdt)
+        if fctx.needs_input_grad[1]:
+            gw = abi.weights_grad(w, (feats * g[:, None]).sum(0)).to(wdt)
+        if has_tab and fctx.needs_input_grad[2]:
+            if bool((g == g[0]).all()):
+                gt = (dt * g[0]).view(abi.PAIR_TYPES, abi.PAIR_BINS).to(tdt)
+            else:
+                d2 = torch.zeros(abi.PAIR_TYPES * abi.PAIR_BINS, dtype=torch.float64, device=x.device)
+                scratch = torch.empty_like(x)
+                native.score_adjoint_multi_dev(pctxs, which, P, A, _ptr(ctx_ids if ctx_ids.numel() else None),
+                                               _ptr(lig_ids), _ptr(x), _ptr(rec_tors if rec_tors.numel() else None),
+                                               _ptr(w), _ptr(t), _ptr(g), None, None, _ptr(scratch), None, _ptr(d2),
+                                               _stream())
+                gt = d2.view(abi.PAIR_TYPES, abi.PAIR_BINS).to(tdt)
+        return gx, gw, gt, None, None, None, None, None
 
 
 def empirical_score(pctx, lig_ids, xyz, weights, tables=None, which=0, rec_tors=None, ctx_ids=None):

@@ -98,3 +98,17 @@ def test_adjoint_matches_h1e4_differences(system):
         tm[k] -= h
         fd = g * (score(s, x, tab=tp) - score(s, x, tab=tm)) / (2 * h)
         assert abs(fd - gt[k]) <= 1e-8 * max(1.0, abs(fd)), (k, fd, gt[k])
+
+
+def test_host_weight_gradient_matches_the_oracle(system):
+    """abi.weights_grad (the autograd backward's weight gradient from summed features)
+    equals the port's po_combine_grad, on numpy and torch inputs."""
+    import ctypes as C
+    f = np.random.default_rng(4).normal(size=abi.NUM_SCORE_FEATURES)
+    ref = np.zeros(abi.NUM_SF_WEIGHTS)
+    p = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    O.port_lib().po_combine_grad(p(system["w"]), p(f), 1.0, p(ref))
+    np.testing.assert_allclose(abi.weights_grad(system["w"], f), ref, rtol=1e-14, atol=1e-14)
+    torch = pytest.importorskip("torch")
+    got = abi.weights_grad(torch.tensor(system["w"]), torch.tensor(f)).numpy()
+    np.testing.assert_allclose(got, ref, rtol=1e-14, atol=1e-14)
