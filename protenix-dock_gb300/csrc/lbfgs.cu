@@ -29,6 +29,7 @@ struct LbfgsArgs {
     int D_pad;         // padded vector length
     float* hist;       // per warp: S [m][D_pad], Y [m][D_pad]
     size_t hist_stride;
+    int hist_smem;     // 1: the history lives in the warp's shared memory instead
 };
 
 constexpr int kWarpsPerBlock = 4;
@@ -43,7 +44,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
     const int Dp = a.D_pad;
-    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + 10 * Dp + 4 * a.c.m;
+    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + 10 * Dp + 4 * a.c.m +
+                         (a.hist_smem ? 2 * a.c.m * Dp : 0);
     float* base = smem + wib * per_warp;
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
@@ -61,7 +63,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
     v.ro = reinterpret_cast<double*>(vb + 10 * Dp);
     v.al = v.ro + a.c.m;
     const size_t gw = static_cast<size_t>(blockIdx.x) * kWarpsPerBlock + wib;
-    v.S = a.hist + gw * a.hist_stride;
+    v.S = a.hist_smem ? vb + 10 * Dp + 4 * a.c.m : a.hist + gw * a.hist_stride;
     v.Y = v.S + static_cast<size_t>(a.c.m) * Dp;
     const int R = a.env.rec.n_rotors;
     Closure c;
@@ -166,10 +168,11 @@ static int padded(int D) { return (D + kWarp - 1) / kWarp * kWarp; }
 
 using LbfgsKernelFn = void (*)(LbfgsArgs);
 
-// Register / occupancy variant of lbfgs_kernel: 0 = unconstrained registers, else the
-// minimum resident blocks per SM.
-static LbfgsKernelFn variant_fn(int min_blocks) {
-    switch (min_blocks) {
+// Variant of lbfgs_kernel: the low byte is the minimum resident blocks per SM (register
+// cap; 0 = unconstrained), kHistSmem marks the history in shared memory.
+constexpr int kHistSmem = 256;
+static LbfgsKernelFn variant_fn(int variant) {
+    switch (variant & 255) {
         case 4: return lbfgs_kernel<4>;
         case 5: return lbfgs_kernel<5>;
         case 6: return lbfgs_kernel<6>;
@@ -181,15 +184,27 @@ static LbfgsKernelFn variant_fn(int min_blocks) {
 static int class_bound(int cap) { return std::min(256, (cap + 31) / 32 * 32); }
 
 // The variant of a size class: the autotuner's choice for the class (pxd_lbfgs_autotune_dev),
-// else PXD_LBFGS_MIN_BLOCKS, else the default.
-static LbfgsKernelFn lbfgs_variant(const pxd_context* ctx, int cap) {
+// else PXD_LBFGS_MIN_BLOCKS (| kHistSmem when PXD_LBFGS_HIST_SMEM=1), else the default.
+static int lbfgs_variant_id(const pxd_context* ctx, int cap) {
     auto it = ctx->lbfgs_tuned.find(class_bound(cap));
-    if (it != ctx->lbfgs_tuned.end()) return variant_fn(it->second);
+    if (it != ctx->lbfgs_tuned.end()) return it->second;
     static int choice = [] {
         const char* v = std::getenv("PXD_LBFGS_MIN_BLOCKS");
-        return v ? std::atoi(v) : kDefaultMinBlocks;
+        const char* h = std::getenv("PXD_LBFGS_HIST_SMEM");
+        return (v ? std::atoi(v) : kDefaultMinBlocks) | (h && std::atoi(h) ? kHistSmem : 0);
     }();
-    return variant_fn(choice);
+    return choice;
+}
+static LbfgsKernelFn lbfgs_variant(const pxd_context* ctx, int cap) {
+    return variant_fn(lbfgs_variant_id(ctx, cap));
+}
+
+// Dynamic shared memory of one lbfgs_kernel block for ligands of up to `cap` atoms.
+static size_t lbfgs_block_smem(const pxd_context* ctx, int cap, int history, bool hist_smem) {
+    const int dp = padded(3 * cap + ctx->rec.n_rotors);
+    const int per_warp = pose_bufs_floats(cap, ctx->rec.n_local) + 10 * dp + 4 * history +
+                         (hist_smem ? 2 * history * dp : 0);
+    return sizeof(float) * kWarpsPerBlock * per_warp;
 }
 
 int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_ids,
@@ -354,6 +369,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     base.n_poses = n_poses;
     base.order = nullptr;
     base.count_dev = nullptr;
+    base.hist_smem = 0;
     fill_consts(base, p);
     base.n_local = ctx->rec.n_local;
     // the classes that registered ligands fall in (capped at the caller's max_atoms)
@@ -369,7 +385,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     const bool classes = caps.size() > 1 && n_poses >= 1024;
     if (!classes) caps.assign(1, max_atoms);
     struct Plan {
-        int cap, dp, blocks;
+        int cap, dp, blocks, hist_smem;
         size_t smem, stride;
         LbfgsKernelFn kern;
     };
@@ -379,10 +395,10 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
         Plan q;
         q.cap = cap;
         q.kern = lbfgs_variant(ctx, cap);
+        q.hist_smem = (lbfgs_variant_id(ctx, cap) & kHistSmem) ? 1 : 0;
         const LbfgsKernelFn kern = q.kern;
         q.dp = padded(3 * cap + ctx->rec.n_rotors);
-        const int per_warp = pose_bufs_floats(cap, base.n_local) + 10 * q.dp + 4 * p.history;
-        q.smem = sizeof(float) * kWarpsPerBlock * per_warp;
+        q.smem = lbfgs_block_smem(ctx, cap, p.history, q.hist_smem);
         rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   static_cast<int>(q.smem)),
                         "lbfgs smem attribute");
@@ -454,6 +470,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
         a.D_pad = plan[k].dp;
         a.hist = hist + hist_off[k];
         a.hist_stride = plan[k].stride;
+        a.hist_smem = plan[k].hist_smem;
         a.counter = counters + k;
         cudaStream_t ks = s;
         if (classes) {
@@ -683,7 +700,7 @@ extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* 
     }
     pxd_lbfgs_params p = *params;
     p.max_iter = std::min(p.max_iter, probe_iters);
-    static const int kVariants[4] = {4, 5, 6, 0};
+    static const int kVariants[8] = {4, 5, 6, 0, 4 | kHistSmem, 5 | kHistSmem, 6 | kHistSmem, 0 | kHistSmem};
     int n_report = 0;
     for (auto& [bound, rows] : by_class) {
         const int m = static_cast<int>(rows.size());
@@ -715,7 +732,11 @@ extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* 
         double best_rate = -1.0;
         int best = kDefaultMinBlocks;
         std::vector<int> nev(m);
+        int smem_limit = 0;
+        cudaDeviceGetAttribute(&smem_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
         for (int v : kVariants) {
+            if ((v & kHistSmem) && lbfgs_block_smem(ctx, cap, p.history, true) > static_cast<size_t>(smem_limit))
+                continue;  // the history does not fit beside the pose buffers
             ctx->lbfgs_tuned[bound] = v;
             cudaMemcpyAsync(d_x, d_x0, sizeof(float) * m * cap * 3, cudaMemcpyDeviceToDevice, s);
             cudaMemcpyAsync(d_t, d_t0, sizeof(float) * m * std::max(R, 1), cudaMemcpyDeviceToDevice, s);
