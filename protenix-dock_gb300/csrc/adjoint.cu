@@ -267,7 +267,7 @@ static int launch_adjoint(pxd_context* const* ctxs, int32_t n_ctx, int32_t which
     int blocks = (n_poses + kAdjWarps - 1) / kAdjWarps;
     if (blocks > ctx->n_sm * per_sm) blocks = ctx->n_sm * per_sm;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-    AdjArgs a;
+    AdjArgs a{};
     a.one = table[0];
     a.ctxs = nullptr;
     a.ctx_ids = ctx_ids;

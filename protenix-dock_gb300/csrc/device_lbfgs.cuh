@@ -49,6 +49,29 @@ __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double
     return (lo + hi) / 2.0;
 }
 
+// The two ends of the line search's bracket (step, value, directional derivative,
+// gradient) as named scalars selected by index 0 / 1: no dynamically indexed local arrays.
+struct Bracket {
+    double br0 = 0.0, br1 = 0.0, bf0 = 0.0, bf1 = 0.0, bgtd0 = 0.0, bgtd1 = 0.0;
+    float *bg0, *bg1;
+    __device__ double br(int i) const { return i ? br1 : br0; }
+    __device__ double bf(int i) const { return i ? bf1 : bf0; }
+    __device__ double bgtd(int i) const { return i ? bgtd1 : bgtd0; }
+    __device__ float* bg(int i) const { return i ? bg1 : bg0; }
+    __device__ void set_br(int i, double x) {
+        if (i) br1 = x;
+        else br0 = x;
+    }
+    __device__ void set_bf(int i, double x) {
+        if (i) bf1 = x;
+        else bf0 = x;
+    }
+    __device__ void set_bgtd(int i, double x) {
+        if (i) bgtd1 = x;
+        else bgtd0 = x;
+    }
+};
+
 // strong_wolfe (optimizer.cpp:235-427); g holds the current gradient on entry and the
 // accepted one on exit.
 static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_io, const float* d,
@@ -58,8 +81,9 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
     const double f = f_io;
     float* g_new = v.gnew;
     float* g_prev = v.gprev;
-    float* bg[2] = {v.bg0, v.bg1};
-    double br[2] = {0.0, 0.0}, bf[2] = {0.0, 0.0}, bgtd[2] = {0.0, 0.0};
+    Bracket B;
+    B.bg0 = v.bg0;
+    B.bg1 = v.bg1;
     double f_new = closure_eval(c, t, d, g_new);
     if (isnan(f_new)) {
         f_io = f_new;
@@ -77,23 +101,23 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
     int ls_iter = 0;
     while (ls_iter < p.ls_max) {
         if ((f_new > f + p.c1 * t * gtd) || (ls_iter > 1 && f_new >= f_prev)) {
-            br[0] = t_prev; br[1] = t; bf[0] = f_prev; bf[1] = f_new;
-            vcopy(bg[0], g_prev, D, lane);
-            vcopy(bg[1], g_new, D, lane);
-            bgtd[0] = gtd_prev; bgtd[1] = gtd_new;
+            B.br0 = t_prev; B.br1 = t; B.bf0 = f_prev; B.bf1 = f_new;
+            vcopy(B.bg0, g_prev, D, lane);
+            vcopy(B.bg1, g_new, D, lane);
+            B.bgtd0 = gtd_prev; B.bgtd1 = gtd_new;
             break;
         }
         if (fabs(gtd_new) <= -p.c2 * gtd) {
-            br[0] = t; bf[0] = f_new;
-            vcopy(bg[0], g_new, D, lane);
+            B.br0 = t; B.bf0 = f_new;
+            vcopy(B.bg0, g_new, D, lane);
             done = true;
             break;
         }
         if (gtd_new >= 0.0) {
-            br[0] = t_prev; br[1] = t; bf[0] = f_prev; bf[1] = f_new;
-            vcopy(bg[0], g_prev, D, lane);
-            vcopy(bg[1], g_new, D, lane);
-            bgtd[0] = gtd_prev; bgtd[1] = gtd_new;
+            B.br0 = t_prev; B.br1 = t; B.bf0 = f_prev; B.bf1 = f_new;
+            vcopy(B.bg0, g_prev, D, lane);
+            vcopy(B.bg1, g_new, D, lane);
+            B.bgtd0 = gtd_prev; B.bgtd1 = gtd_new;
             break;
         }
         const double min_step = t + 0.01 * (t - t_prev);
@@ -110,30 +134,30 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
     }
     double d_norm = 0.0;
     if (ls_iter == p.ls_max) {
-        br[0] = 0.0; br[1] = t; bf[0] = f; bf[1] = f_new;
-        vcopy(bg[0], g, D, lane);
-        vcopy(bg[1], g_new, D, lane);
+        B.br0 = 0.0; B.br1 = t; B.bf0 = f; B.bf1 = f_new;
+        vcopy(B.bg0, g, D, lane);
+        vcopy(B.bg1, g_new, D, lane);
     } else {
         d_norm = vabsmax(d, D, lane);
     }
     bool insuf = false;
     int lo = 0, hi = 1;
-    if (!done && bf[0] > bf[1]) {
+    if (!done && B.bf0 > B.bf1) {
         lo = 1;
         hi = 0;
     }
     while (!done && ls_iter < p.ls_max) {
         double min_step, max_step;
-        if (br[0] > br[1]) {
-            min_step = br[1];
-            max_step = br[0];
+        if (B.br0 > B.br1) {
+            min_step = B.br1;
+            max_step = B.br0;
         } else {
-            min_step = br[0];
-            max_step = br[1];
+            min_step = B.br0;
+            max_step = B.br1;
         }
         double eps = max_step - min_step;
         if (eps * d_norm < p.ls_tol_change) break;
-        t = cubic_interpolate(br[0], bf[0], bgtd[0], br[1], bf[1], bgtd[1], min_step, max_step);
+        t = cubic_interpolate(B.br0, B.bf0, B.bgtd0, B.br1, B.bf1, B.bgtd1, min_step, max_step);
         eps *= 0.1;
         if (fmin(max_step - t, t - min_step) < eps) {
             if (insuf || t >= max_step || t <= min_step) {
@@ -151,12 +175,12 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
         f_new = closure_eval(c, t, d, g_new);
         gtd_new = vdot(g_new, d, D, lane);
         ++ls_iter;
-        if (f_new > (f + p.c1 * t * gtd) || f_new >= bf[lo]) {
-            br[hi] = t;
-            bf[hi] = f_new;
-            vcopy(bg[hi], g_new, D, lane);
-            bgtd[hi] = gtd_new;
-            if (bf[0] > bf[1]) {
+        if (f_new > (f + p.c1 * t * gtd) || f_new >= B.bf(lo)) {
+            B.set_br(hi, t);
+            B.set_bf(hi, f_new);
+            vcopy(B.bg(hi), g_new, D, lane);
+            B.set_bgtd(hi, gtd_new);
+            if (B.bf0 > B.bf1) {
                 lo = 1;
                 hi = 0;
             } else {
@@ -166,21 +190,21 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
         } else {
             if (fabs(gtd_new) <= -p.c2 * gtd) {
                 done = true;
-            } else if (gtd_new * (br[hi] - br[lo]) >= 0.0) {
-                br[hi] = br[lo];
-                bf[hi] = bf[lo];
-                vcopy(bg[hi], bg[lo], D, lane);
-                bgtd[hi] = bgtd[lo];
+            } else if (gtd_new * (B.br(hi) - B.br(lo)) >= 0.0) {
+                B.set_br(hi, B.br(lo));
+                B.set_bf(hi, B.bf(lo));
+                vcopy(B.bg(hi), B.bg(lo), D, lane);
+                B.set_bgtd(hi, B.bgtd(lo));
             }
-            br[lo] = t;
-            bf[lo] = f_new;
-            vcopy(bg[lo], g_new, D, lane);
-            bgtd[lo] = gtd_new;
+            B.set_br(lo, t);
+            B.set_bf(lo, f_new);
+            vcopy(B.bg(lo), g_new, D, lane);
+            B.set_bgtd(lo, gtd_new);
         }
     }
-    t_io = br[lo];
-    f_io = bf[lo];
-    vcopy(g, bg[lo], D, lane);
+    t_io = B.br(lo);
+    f_io = B.bf(lo);
+    vcopy(g, B.bg(lo), D, lane);
 }
 
 // lbfgs_step::apply (optimizer.cpp:429-560) on the pose held in v.x; returns status.

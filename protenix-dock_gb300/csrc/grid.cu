@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
 
 int launch_grid_build(pxd_context* ctx, const float4* atoms, const float4* atoms_lo, const float2* se,
                       int n_atoms, const int* slot_type, int n_slots, float4* maps) {
-    GridArgs a;
+    GridArgs a{};
     a.atoms = atoms;
     a.atoms_lo = atoms_lo;
     a.se = se;

@@ -39,7 +39,7 @@ constexpr int kDefaultMinBlocks = 4;  // measured best on GB300 for the 42-atom 
 // variants are chosen per launch (lbfgs_variant).
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinBlocks : 1)
-    lbfgs_kernel(const LbfgsArgs a) {
+    lbfgs_kernel(const __grid_constant__ LbfgsArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
             }
             continue;
         }
-        const DevLigand L = a.ligands[lid];
+        const DevLigand& L = a.ligands[lid];
         const int N = L.n_atoms;
         const int D = 3 * N + R;
         const float* px = a.xyz + static_cast<size_t>(pose) * a.stride_atoms * 3;
@@ -213,7 +213,7 @@ int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_id
     if (n_poses <= 0) return PXD_OK;
     int rc = sync_ligand_table(ctx);
     if (rc) return rc;
-    ScoreArgs a;
+    ScoreArgs a{};
     a.env = make_env(ctx);
     a.ligands = ctx->d_ligands;
     a.lig_ids = lig_ids;
@@ -355,7 +355,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     if (n_poses <= 0) return PXD_OK;
     int rc = sync_ligand_table(ctx);
     if (rc) return rc;
-    LbfgsArgs base;
+    LbfgsArgs base{};
     base.env = make_env(ctx);
     base.ligands = ctx->d_ligands;
     base.lig_ids = lig_ids;
@@ -429,7 +429,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     float* hist = static_cast<float*>(ctx->scratch);
     int* counters = classes ? reinterpret_cast<int*>(static_cast<char*>(ctx->scratch) + hist_bytes) : ctx->d_counter;
     if (classes) {
-        ClassArgs ca;
+        ClassArgs ca{};
         ca.lig_ids = lig_ids;
         ca.ligands = ctx->d_ligands;
         ca.n_ligands = base.n_ligands;
@@ -537,7 +537,7 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     unsigned char* base = nullptr;
     rc = static_scratch(ctx, &base);
     if (rc) return rc;
-    LbfgsArgs a;
+    LbfgsArgs a{};
     a.env = make_env(ctx);
     a.ligands = ctx->d_ligands;
     a.lig_ids = lig_ids;
@@ -641,7 +641,7 @@ extern "C" int pxd_score_grad_multi_dev(pxd_context* const* ctxs, int32_t n_ctx,
     cudaMemcpyAsync(base, envs.data(), sizeof(EvalEnv) * n_ctx, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(base + e_bytes, tabs.data(), sizeof(void*) * n_ctx, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(base + e_bytes + t_bytes, n_ligs.data(), sizeof(int) * n_ctx, cudaMemcpyHostToDevice, s);
-    ScoreMultiArgs a;
+    ScoreMultiArgs a{};
     a.envs = reinterpret_cast<const EvalEnv*>(base);
     a.tabs = reinterpret_cast<const DevLigand* const*>(base + e_bytes);
     a.n_ligs = reinterpret_cast<const int*>(base + e_bytes + t_bytes);

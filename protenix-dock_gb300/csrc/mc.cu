@@ -238,7 +238,7 @@ __device__ void atomic_min_double(double* p, double v) {
     }
 }
 
-__global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const McArgs a) {
+__global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_constant__ McArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
@@ -533,7 +533,7 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     if (n_walkers == 0) return PXD_OK;
     int rc = sync_ligand_table(ctx);
     if (rc) return rc;
-    McArgs a;
+    McArgs a{};
     a.env.rec = ctx->rec;
     a.env.grid = ctx->grid;
     a.senv.rs = ctx->rec_score;

@@ -522,7 +522,7 @@ int pxd_score_dev(pxd_context* ctx, int32_t which, int32_t n_poses, int32_t max_
     if (n_poses == 0) return PXD_OK;
     int rc = sync_ligand_table(ctx);
     if (rc) return rc;
-    EsArgs a;
+    EsArgs a{};
     a.env.rs = ctx->rec_score;
     a.env.sf = ctx->d_sf[which];
     a.rec = ctx->rec;
