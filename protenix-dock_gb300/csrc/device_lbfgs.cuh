@@ -20,6 +20,34 @@ struct Vecs {
     double *ro, *al;
 };
 
+// D_pad-long vectors in a warp's optimiser slice: x, g, gp, d and the line search's g_new,
+// g_prev and two bracket gradients. The history update's y / two-loop q and s share the
+// space of g_prev and g_new: those are live only inside strong_wolfe and the final
+// evaluation, q and s only between line searches. Eight vectors instead of ten keep four
+// blocks' slices inside a smaller shared-memory carve-out, which leaves more L1 for the
+// history slab, the map gathers and the topology records.
+constexpr int kOptVecs = 8;
+
+// Carves the vectors from vb (kOptVecs * Dp floats) and the FP64 two-loop scalars ro, al
+// (2 * m doubles) after them.
+__device__ __forceinline__ Vecs carve_vecs(float* vb, int Dp, int m) {
+    Vecs v;
+    v.x = vb;
+    v.g = vb + Dp;
+    v.gp = vb + 2 * Dp;
+    v.d = vb + 3 * Dp;
+    v.gnew = vb + 4 * Dp;
+    v.gprev = vb + 5 * Dp;
+    v.bg0 = vb + 6 * Dp;
+    v.bg1 = vb + 7 * Dp;
+    v.q = v.gprev;
+    v.sv = v.gnew;
+    v.ro = reinterpret_cast<double*>(vb + kOptVecs * Dp);
+    v.al = v.ro + m;
+    v.S = v.Y = nullptr;
+    return v;
+}
+
 struct Closure {
     const EvalEnv* env;
     const DevLigand* L;

@@ -44,26 +44,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
     const int Dp = a.D_pad;
-    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + 10 * Dp + 4 * a.c.m +
+    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + kOptVecs * Dp + 4 * a.c.m +
                          (a.hist_smem ? 2 * a.c.m * Dp : 0);
     float* base = smem + wib * per_warp;
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
-    Vecs v;
-    v.x = vb;
-    v.g = vb + Dp;
-    v.gp = vb + 2 * Dp;
-    v.d = vb + 3 * Dp;
-    v.q = vb + 4 * Dp;
-    v.sv = vb + 5 * Dp;
-    v.gnew = vb + 6 * Dp;
-    v.gprev = vb + 7 * Dp;
-    v.bg0 = vb + 8 * Dp;
-    v.bg1 = vb + 9 * Dp;
-    v.ro = reinterpret_cast<double*>(vb + 10 * Dp);
-    v.al = v.ro + a.c.m;
+    Vecs v = carve_vecs(vb, Dp, a.c.m);
     const size_t gw = static_cast<size_t>(blockIdx.x) * kWarpsPerBlock + wib;
-    v.S = a.hist_smem ? vb + 10 * Dp + 4 * a.c.m : a.hist + gw * a.hist_stride;
+    v.S = a.hist_smem ? vb + kOptVecs * Dp + 4 * a.c.m : a.hist + gw * a.hist_stride;
     v.Y = v.S + static_cast<size_t>(a.c.m) * Dp;
     const int R = a.env.rec.n_rotors;
     Closure c;
@@ -202,7 +190,7 @@ static LbfgsKernelFn lbfgs_variant(const pxd_context* ctx, int cap) {
 // Dynamic shared memory of one lbfgs_kernel block for ligands of up to `cap` atoms.
 static size_t lbfgs_block_smem(const pxd_context* ctx, int cap, int history, bool hist_smem) {
     const int dp = padded(3 * cap + ctx->rec.n_rotors);
-    const int per_warp = pose_bufs_floats(cap, ctx->rec.n_local) + 10 * dp + 4 * history +
+    const int per_warp = pose_bufs_floats(cap, ctx->rec.n_local) + kOptVecs * dp + 4 * history +
                          (hist_smem ? 2 * history * dp : 0);
     return sizeof(float) * kWarpsPerBlock * per_warp;
 }
@@ -566,7 +554,7 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.c.reset = p.reset_threshold;
     a.n_local = ctx->rec.n_local;
     a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
-    const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + 10 * a.D_pad + 4 * p.history;
+    const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + kOptVecs * a.D_pad + 4 * p.history;
     const size_t smem = sizeof(float) * kWarpsPerBlock * per_warp;
     const LbfgsKernelFn kern = lbfgs_variant(ctx, max_atoms);
     rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

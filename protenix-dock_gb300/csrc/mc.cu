@@ -143,7 +143,7 @@ struct McArgs {
 };
 
 __host__ __device__ inline int mc_warp_floats(int max_atoms, int n_local, int Dp, int m) {
-    return pose_bufs_floats(max_atoms, n_local) + 10 * Dp + 4 * m + 2 * Dp + 4 * max_atoms +
+    return pose_bufs_floats(max_atoms, n_local) + kOptVecs * Dp + 4 * m + 2 * Dp + 4 * max_atoms +
            static_cast<int>(sizeof(KinShared) / sizeof(float)) + 64 + 16;
 }
 
@@ -247,20 +247,8 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     float* base = smem + static_cast<size_t>(wib) * mc_warp_floats(a.max_atoms, a.n_local, Dp, m);
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
-    Vecs v;
-    v.x = vb;
-    v.g = vb + Dp;
-    v.gp = vb + 2 * Dp;
-    v.d = vb + 3 * Dp;
-    v.q = vb + 4 * Dp;
-    v.sv = vb + 5 * Dp;
-    v.gnew = vb + 6 * Dp;
-    v.gprev = vb + 7 * Dp;
-    v.bg0 = vb + 8 * Dp;
-    v.bg1 = vb + 9 * Dp;
-    v.ro = reinterpret_cast<double*>(vb + 10 * Dp);
-    v.al = v.ro + m;
-    float* best_x = vb + 10 * Dp + 4 * m;
+    Vecs v = carve_vecs(vb, Dp, m);
+    float* best_x = vb + kOptVecs * Dp + 4 * m;
     float* tmp_x = best_x + Dp;
     float4* kc = reinterpret_cast<float4*>(tmp_x + Dp);
     KinShared& ks = *reinterpret_cast<KinShared*>(kc + a.max_atoms);
