@@ -161,6 +161,7 @@ using LbfgsKernelFn = void (*)(LbfgsArgs);
 constexpr int kHistSmem = 256;
 static LbfgsKernelFn variant_fn(int variant) {
     switch (variant & 255) {
+        case 3: return lbfgs_kernel<3>;
         case 4: return lbfgs_kernel<4>;
         case 5: return lbfgs_kernel<5>;
         case 6: return lbfgs_kernel<6>;
@@ -688,7 +689,8 @@ extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* 
     }
     pxd_lbfgs_params p = *params;
     p.max_iter = std::min(p.max_iter, probe_iters);
-    static const int kVariants[8] = {4, 5, 6, 0, 4 | kHistSmem, 5 | kHistSmem, 6 | kHistSmem, 0 | kHistSmem};
+    static const int kVariants[10] = {4, 5, 6, 3, 0, 4 | kHistSmem, 5 | kHistSmem, 6 | kHistSmem, 3 | kHistSmem,
+                                      0 | kHistSmem};
     int n_report = 0;
     for (auto& [bound, rows] : by_class) {
         const int m = static_cast<int>(rows.size());
