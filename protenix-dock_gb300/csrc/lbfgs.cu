@@ -385,15 +385,24 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
         q.cap = cap;
         q.kern = lbfgs_variant(ctx, cap);
         q.hist_smem = (lbfgs_variant_id(ctx, cap) & kHistSmem) ? 1 : 0;
-        const LbfgsKernelFn kern = q.kern;
         q.dp = padded(3 * cap + ctx->rec.n_rotors);
         q.smem = lbfgs_block_smem(ctx, cap, p.history, q.hist_smem);
+        q.stride = q.hist_smem ? 0 : static_cast<size_t>(2) * p.history * q.dp;
+        plan.push_back(q);
+    }
+    // classes may share a kernel variant with different slices: its dynamic shared-memory
+    // limit is the largest of theirs, set before any occupancy query or launch
+    std::map<LbfgsKernelFn, size_t> smem_of;
+    for (const Plan& q : plan) smem_of[q.kern] = std::max(smem_of[q.kern], q.smem);
+    for (const auto& [kern, bytes] : smem_of) {
         rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  static_cast<int>(q.smem)),
+                                                  static_cast<int>(bytes)),
                         "lbfgs smem attribute");
         if (rc) return rc;
+    }
+    for (Plan& q : plan) {
         int per_sm = 0;
-        rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpsPerBlock * kWarp,
+        rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, q.kern, kWarpsPerBlock * kWarp,
                                                                           q.smem),
                         "lbfgs occupancy");
         if (rc) return rc;
@@ -401,8 +410,6 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
         q.blocks = per_sm * ctx->n_sm;
         const int need = (n_poses + kWarpsPerBlock - 1) / kWarpsPerBlock;
         if (q.blocks > need) q.blocks = need;
-        q.stride = static_cast<size_t>(2) * p.history * q.dp;
-        plan.push_back(q);
     }
     // the class launches run concurrently, each on its own history slab
     std::vector<size_t> hist_off(plan.size());
