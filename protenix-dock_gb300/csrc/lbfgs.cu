@@ -292,7 +292,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp) score_multi_kernel(con
 // Size classes of the batched launch: poses are grouped by their ligand's atom count so
 // that each persistent launch sizes its per-warp shared memory (and so its residency)
 // for its own class instead of the largest ligand of the batch.
-constexpr int kSizeClasses = 8;
 constexpr int kClassBound[kSizeClasses] = {32, 64, 96, 128, 160, 192, 224, 256};
 
 struct ClassArgs {
@@ -321,6 +320,65 @@ __global__ void size_class_kernel(const ClassArgs a) {
     }
     const int pos = atomicAdd(&a.counts[c], 1);
     a.lists[static_cast<size_t>(c) * a.n_poses + pos] = i;
+}
+
+std::vector<int> size_class_caps(const pxd_context* ctx, int max_atoms, int n_items) {
+    std::vector<int> caps;
+    for (int k = 0; k < kSizeClasses; ++k) {
+        const int cap = std::min(kClassBound[k], max_atoms);
+        bool used = false;
+        for (auto& e : ctx->ligands) used = used || (e.n_atoms <= cap && (k == 0 || e.n_atoms > kClassBound[k - 1]));
+        if (used && (caps.empty() || caps.back() != cap)) caps.push_back(cap);
+        if (cap == max_atoms) break;
+    }
+    if (caps.empty() || caps.back() != max_atoms) caps.push_back(max_atoms);  // oversize / invalid ids
+    if (caps.size() > 1 && n_items < 1024) caps.assign(1, max_atoms);
+    return caps;
+}
+
+size_t size_class_ints(size_t n_cls, int n_items) { return 2 * n_cls + n_cls * static_cast<size_t>(n_items); }
+
+int launch_size_classes(pxd_context* ctx, int n_items, const int* lig_ids, const std::vector<int>& caps,
+                        int* scratch, cudaStream_t s) {
+    const size_t n_cls = caps.size();
+    ClassArgs ca{};
+    ca.lig_ids = lig_ids;
+    ca.ligands = ctx->d_ligands;
+    ca.n_ligands = static_cast<int>(ctx->ligands.size());
+    ca.n_poses = n_items;
+    ca.n_classes = static_cast<int>(n_cls);
+    for (size_t k = 0; k < n_cls; ++k) ca.bound[k] = caps[k];
+    ca.counts = scratch + n_cls;
+    ca.lists = scratch + 2 * n_cls;
+    int rc = cuda_check(ctx, cudaMemsetAsync(scratch, 0, sizeof(int) * 2 * n_cls, s), "class counters");
+    if (rc) return rc;
+    size_class_kernel<<<(n_items + 255) / 256, 256, 0, s>>>(ca);
+    return cuda_check(ctx, cudaGetLastError(), "size_class_kernel launch");
+}
+
+int class_fork(pxd_context* ctx, size_t n_cls, cudaStream_t s) {
+    for (size_t k = 0; k <= n_cls; ++k) {
+        if (k < n_cls && !ctx->class_streams[k]) {
+            int rc = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->class_streams[k], cudaStreamNonBlocking),
+                                "class stream");
+            if (rc) return rc;
+        }
+        if (!ctx->class_events[k]) {
+            int rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->class_events[k], cudaEventDisableTiming),
+                                "class event");
+            if (rc) return rc;
+        }
+    }
+    int rc = cuda_check(ctx, cudaEventRecord(ctx->class_events[n_cls], s), "fork");
+    for (size_t k = 0; k < n_cls && !rc; ++k)
+        rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->class_streams[k], ctx->class_events[n_cls], 0), "fork wait");
+    return rc;
+}
+
+int class_join(pxd_context* ctx, size_t k, cudaStream_t s) {
+    int rc = cuda_check(ctx, cudaEventRecord(ctx->class_events[k], ctx->class_streams[k]), "join record");
+    if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(s, ctx->class_events[k], 0), "join wait");
+    return rc;
 }
 
 static void fill_consts(LbfgsArgs& a, const pxd_lbfgs_params& p) {
@@ -361,18 +419,8 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     base.hist_smem = 0;
     fill_consts(base, p);
     base.n_local = ctx->rec.n_local;
-    // the classes that registered ligands fall in (capped at the caller's max_atoms)
-    std::vector<int> caps;
-    for (int k = 0; k < kSizeClasses; ++k) {
-        const int cap = std::min(kClassBound[k], max_atoms);
-        bool used = false;
-        for (auto& e : ctx->ligands) used = used || (e.n_atoms <= cap && (k == 0 || e.n_atoms > kClassBound[k - 1]));
-        if (used && (caps.empty() || caps.back() != cap)) caps.push_back(cap);
-        if (cap == max_atoms) break;
-    }
-    if (caps.empty() || caps.back() != max_atoms) caps.push_back(max_atoms);  // oversize / invalid ids
-    const bool classes = caps.size() > 1 && n_poses >= 1024;
-    if (!classes) caps.assign(1, max_atoms);
+    const std::vector<int> caps = size_class_caps(ctx, max_atoms, n_poses);
+    const bool classes = caps.size() > 1;
     struct Plan {
         int cap, dp, blocks, hist_smem;
         size_t smem, stride;
@@ -419,47 +467,19 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     }
     const size_t hist_bytes = (sizeof(float) * hist_floats + 255) / 256 * 256;
     const size_t n_cls = plan.size();
-    const size_t class_bytes = classes ? sizeof(int) * (2 * n_cls + n_cls * static_cast<size_t>(n_poses)) : 0;
+    const size_t class_bytes = classes ? sizeof(int) * size_class_ints(n_cls, n_poses) : 0;
     rc = ensure_scratch(ctx, hist_bytes + class_bytes);
     if (rc) return rc;
     float* hist = static_cast<float*>(ctx->scratch);
     int* counters = classes ? reinterpret_cast<int*>(static_cast<char*>(ctx->scratch) + hist_bytes) : ctx->d_counter;
     if (classes) {
-        ClassArgs ca{};
-        ca.lig_ids = lig_ids;
-        ca.ligands = ctx->d_ligands;
-        ca.n_ligands = base.n_ligands;
-        ca.n_poses = n_poses;
-        ca.n_classes = static_cast<int>(n_cls);
-        for (size_t k = 0; k < n_cls; ++k) ca.bound[k] = plan[k].cap;
-        ca.counts = counters + n_cls;
-        ca.lists = counters + 2 * n_cls;
-        rc = cuda_check(ctx, cudaMemsetAsync(counters, 0, sizeof(int) * 2 * n_cls, s), "class counters");
-        if (rc) return rc;
-        size_class_kernel<<<(n_poses + 255) / 256, 256, 0, s>>>(ca);
-        rc = cuda_check(ctx, cudaGetLastError(), "size_class_kernel launch");
-        if (rc) return rc;
+        // class k runs on class stream k after the classification; s waits for all of them
+        rc = launch_size_classes(ctx, n_poses, lig_ids, caps, counters, s);
+        if (!rc) rc = class_fork(ctx, n_cls, s);
     } else {
         rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), s), "counter reset");
-        if (rc) return rc;
     }
-    // fork: class k runs on side stream k after the classification; join back on s
-    if (classes) {
-        for (size_t k = 0; k <= n_cls; ++k) {
-            if (k < n_cls && !ctx->class_streams[k]) {
-                rc = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->class_streams[k], cudaStreamNonBlocking),
-                                "class stream");
-                if (rc) return rc;
-            }
-            if (!ctx->class_events[k]) {
-                rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->class_events[k], cudaEventDisableTiming),
-                                "class event");
-                if (rc) return rc;
-            }
-        }
-        rc = cuda_check(ctx, cudaEventRecord(ctx->class_events[n_cls], s), "fork");
-        if (rc) return rc;
-    }
+    if (rc) return rc;
     for (size_t k = 0; k < n_cls; ++k) {
         LbfgsArgs a = base;
         a.max_atoms = plan[k].cap;
@@ -473,17 +493,11 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
             a.count_dev = counters + n_cls + k;
             a.order = counters + 2 * n_cls + k * static_cast<size_t>(n_poses);
             ks = ctx->class_streams[k];
-            rc = cuda_check(ctx, cudaStreamWaitEvent(ks, ctx->class_events[n_cls], 0), "fork wait");
-            if (rc) return rc;
         }
         plan[k].kern<<<plan[k].blocks, kWarpsPerBlock * kWarp, plan[k].smem, ks>>>(a);
         rc = cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
+        if (!rc && classes) rc = class_join(ctx, k, s);
         if (rc) return rc;
-        if (classes) {
-            rc = cuda_check(ctx, cudaEventRecord(ctx->class_events[k], ks), "join record");
-            if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(s, ctx->class_events[k], 0), "join wait");
-            if (rc) return rc;
-        }
     }
     return PXD_OK;
 }

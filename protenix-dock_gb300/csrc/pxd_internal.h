@@ -214,6 +214,24 @@ int ensure_scratch(pxd_context* ctx, size_t bytes);
 int sync_ligand_table(pxd_context* ctx);
 int refresh_ligand_slots(pxd_context* ctx);
 
+// Size classes of a batch (lbfgs.cu): poses are sorted on the device by the atom count of
+// their ligand into classes of capacity 32, 64, ..., 256 atoms, and each class runs its own
+// persistent launch, with per-warp slices sized for its capacity, concurrently on the
+// context's class streams.
+constexpr int kSizeClasses = 8;
+// Capacities (ascending, the last = max_atoms) of the classes that the context's ligands
+// fall in; one class when there is only one or the batch is smaller than 1,024 items.
+std::vector<int> size_class_caps(const pxd_context* ctx, int max_atoms, int n_items);
+// Ints of class scratch for n_cls classes over n_items: counters [n_cls], counts [n_cls],
+// lists [n_cls][n_items].
+size_t size_class_ints(size_t n_cls, int n_items);
+// Zeroes the counters and counts and lists every item under its class, on stream s.
+int launch_size_classes(pxd_context* ctx, int n_items, const int* lig_ids, const std::vector<int>& caps,
+                        int* scratch, cudaStream_t s);
+// Fork: the class streams wait for what s has queued. Join: s waits for class k's stream.
+int class_fork(pxd_context* ctx, size_t n_cls, cudaStream_t s);
+int class_join(pxd_context* ctx, size_t k, cudaStream_t s);
+
 // kernels (launchers), one per translation unit
 int launch_grid_build(pxd_context* ctx, const float4* atoms_xyzq, const float4* atoms_lo,
                       const float2* atoms_se, int n_atoms, const int* slot_types, int n_slots,

@@ -144,3 +144,43 @@ def test_bad_parameters_rejected(mc):
     p = native.mc_params(c["hi"], c["lo"])
     with pytest.raises(native.NativeError):
         c["ctx"].mc_search(p, c["lid"], c["lig"].poses[0][None], [1])
+
+
+def test_mixed_ligand_launch_matches_single_ligand_launches(golden):
+    """Walkers of three ligands of 24, 54 and 81 atoms in one launch of 1,056 walkers
+    (per-warp slices sized for the largest) end bit for bit where one launch per ligand
+    (slices of its own size) ends."""
+    rec = model.Receptor.from_json(synth.make_receptor(seed=2, n_heavy=500, cube=24.0, cavity=8.0))
+    ligs = [model.Ligand.from_json(synth.make_ligand(seed=s, n_heavy=h, n_rot=r, n_n=1, n_o=2))
+            for s, h, r in ((21, 12, 2), (22, 28, 5), (23, 44, 7))]
+    box = model.make_box((0.0, 0.0, 0.0), (16.0, 16.0, 16.0), 0.5)
+    types = sorted(set(int(t) for l in ligs for t in l.vdw_type))
+    pose_sf, _ = model.load_scoring_function(os.path.join(golden, "scoring_function.json"))
+    ctx = native.Context(0)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, types)
+    ctx.set_slope(1e6)
+    ctx.set_scoring_function(0, pose_sf)
+    lids = [ctx.add_ligand(l) for l in ligs]
+    assert [l.n_atoms <= b for l, b in zip(ligs, (32, 64, 96))] == [True] * 3
+    assert ligs[0].n_atoms > 0 and ligs[1].n_atoms > 32 and ligs[2].n_atoms > 64
+    lo = np.array(box.init_xyz)
+    hi = lo + (np.array(box.npoints) - 1) * box.spacing
+    p = native.mc_params(lo, hi, seed=11, max_nsteps=2, relax_nsteps=5, full_nsteps=20)
+    per = 352
+    maxN = max(l.n_atoms for l in ligs)
+    n = per * len(ligs)
+    starts = np.zeros((n, maxN, 3))
+    ids = np.repeat(np.array(lids, np.int32), per)
+    wid = np.tile(np.arange(1, per + 1, dtype=np.int32), len(ligs))
+    for k, l in enumerate(ligs):
+        starts[k * per:(k + 1) * per, : l.n_atoms] = l.poses[0]
+    mixed = ctx.mc_search_multi(p, ids, starts, wid, np.ones(n, np.int32))
+    for k, (l, lid) in enumerate(zip(ligs, lids)):
+        rows = slice(k * per, (k + 1) * per)
+        single = ctx.mc_search(p, lid, starts[rows, : l.n_atoms], wid[rows])
+        for key in ("energy", "pscore", "nevals", "status"):
+            assert np.array_equal(mixed[key][rows], single[key]), key
+        assert np.array_equal(mixed["xyz"][rows, : l.n_atoms], single["xyz"])
+        assert np.sum(single["status"] == 0) >= per // 2
+    ctx.close()
