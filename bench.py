@@ -1031,8 +1031,10 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": config_dict(lig, box),
         "e2e": {"value": e2e_value, "unit": UNIT,
-                "h2d_bytes_per_step": N_POSES * (N * 3 * 4 + 4),
-                "d2h_bytes_per_step": N_POSES * (N * 3 * 4 + 8 + 4 + 4)},
+                # pxd_lbfgs copies the caller's FP64 coordinates both ways (narrowed to FP32
+                # on the device) and returns energy (FP64), evaluations and status per pose
+                "h2d_bytes_per_step": N_POSES * N * 3 * 8,
+                "d2h_bytes_per_step": N_POSES * (N * 3 * 8 + 8 + 4 + 4)},
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,

@@ -34,6 +34,31 @@ int cuda_check(pxd_context* ctx, cudaError_t e, const char* what) {
                      std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+template <class From, class To>
+__global__ void convert_kernel(const From* __restrict__ in, To* __restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+        out[i] = static_cast<To>(in[i]);
+}
+
+__global__ void fill_kernel(int* out, int v, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v;
+}
+
+// Element-wise type conversion of n values on stream s (grid-stride, at most 8 blocks per SM).
+template <class From, class To>
+void convert_on_device(const From* in, To* out, size_t n, int n_sm, cudaStream_t s) {
+    if (n == 0) return;
+    const size_t blocks = std::min<size_t>((n + 255) / 256, static_cast<size_t>(n_sm) * 8);
+    convert_kernel<From, To><<<static_cast<unsigned>(blocks), 256, 0, s>>>(in, out, n);
+}
+
+void fill_on_device(int* out, int v, int n, int n_sm, cudaStream_t s) {
+    if (n <= 0) return;
+    const int blocks = std::min((n + 255) / 256, n_sm * 8);
+    fill_kernel<<<blocks, 256, 0, s>>>(out, v, n);
+}
+
 int ensure_scratch(pxd_context* ctx, size_t bytes) {
     if (bytes <= ctx->scratch_bytes) return PXD_OK;
     if (ctx->scratch) {
@@ -1054,46 +1079,60 @@ int pxd_score_grad(pxd_context* ctx, int32_t lig, int32_t n_poses, const double*
     return PXD_OK;
 }
 
+// The host-buffer optimiser calls: the caller's FP64 arrays are copied as they are and
+// narrowed to FP32 (widened back) on the device, next to the kernel, instead of in loops
+// over the whole batch on one host core. static_cast rounds to nearest on both sides, so the
+// values are those of a host conversion.
+static int lbfgs_host(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses, int32_t max_atoms, int32_t lig,
+                      const int32_t* ligand_ids, double* xyz, double* tors, double* energy, int32_t* nevals,
+                      int32_t* status) {
+    const int R = ctx->rec.n_rotors;
+    const size_t nx = static_cast<size_t>(n_poses) * max_atoms * 3, nt = static_cast<size_t>(n_poses) * R;
+    int rc = PXD_OK;
+    Staging st{ctx, {}};
+    double* dx64 = st.alloc<double>(nx, &rc);
+    double* dt64 = rc ? nullptr : st.alloc<double>(nt, &rc);
+    float* dx = rc ? nullptr : st.alloc<float>(nx, &rc);
+    float* dt = rc ? nullptr : st.alloc<float>(nt, &rc);
+    double* de = rc ? nullptr : st.alloc<double>(n_poses, &rc);
+    int* dn = rc ? nullptr : st.alloc<int>(n_poses, &rc);
+    int* ds = rc ? nullptr : st.alloc<int>(n_poses, &rc);
+    int* di = rc ? nullptr : st.alloc<int>(n_poses, &rc);
+    if (rc) return rc;
+    cudaStream_t s = ctx->stream;
+    rc = cuda_check(ctx, cudaMemcpyAsync(dx64, xyz, nx * sizeof(double), cudaMemcpyHostToDevice, s), "poses in");
+    if (!rc && nt)
+        rc = cuda_check(ctx, cudaMemcpyAsync(dt64, tors, nt * sizeof(double), cudaMemcpyHostToDevice, s), "torsions in");
+    if (!rc && ligand_ids)
+        rc = cuda_check(ctx, cudaMemcpyAsync(di, ligand_ids, n_poses * sizeof(int), cudaMemcpyHostToDevice, s), "ids in");
+    if (rc) return rc;
+    convert_on_device(dx64, dx, nx, ctx->n_sm, s);
+    convert_on_device(dt64, dt, nt, ctx->n_sm, s);
+    if (!ligand_ids) fill_on_device(di, lig, n_poses, ctx->n_sm, s);
+    rc = cuda_check(ctx, cudaGetLastError(), "conversion kernels");
+    if (!rc) rc = pxd_lbfgs_dev(ctx, p, n_poses, max_atoms, di, dx, dt, de, dn, ds, s);
+    if (rc) return rc;
+    convert_on_device(dx, dx64, nx, ctx->n_sm, s);
+    convert_on_device(dt, dt64, nt, ctx->n_sm, s);
+    rc = cuda_check(ctx, cudaGetLastError(), "conversion kernels");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(xyz, dx64, nx * sizeof(double), cudaMemcpyDeviceToHost, s), "poses out");
+    if (!rc && nt)
+        rc = cuda_check(ctx, cudaMemcpyAsync(tors, dt64, nt * sizeof(double), cudaMemcpyDeviceToHost, s), "torsions out");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(energy, de, n_poses * sizeof(double), cudaMemcpyDeviceToHost, s), "energies out");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(nevals, dn, n_poses * sizeof(int), cudaMemcpyDeviceToHost, s), "evaluations out");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(status, ds, n_poses * sizeof(int), cudaMemcpyDeviceToHost, s), "status out");
+    if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(s), "lbfgs");
+    return rc;
+}
+
 int pxd_lbfgs(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t lig, int32_t n_poses, double* xyz,
               double* tors, double* energy, int32_t* nevals, int32_t* status) {
     int rc = check_ready(ctx);
     if (rc) return rc;
     if (lig < 0 || lig >= static_cast<int>(ctx->ligands.size()) || n_poses < 0)
         return set_error(ctx, PXD_ERR_INVALID, "ligand id");
-    const int N = ctx->ligands[lig].n_atoms, R = ctx->rec.n_rotors;
-    const size_t nx = static_cast<size_t>(n_poses) * N * 3, nt = static_cast<size_t>(n_poses) * R;
-    std::vector<float> hx(nx), ht(nt);
-    for (size_t i = 0; i < nx; ++i) hx[i] = static_cast<float>(xyz[i]);
-    for (size_t i = 0; i < nt; ++i) ht[i] = static_cast<float>(tors[i]);
-    std::vector<int> ids(n_poses, lig);
-    Staging st{ctx, {}};
-    float* dx = st.alloc<float>(nx, &rc);
-    if (rc) return rc;
-    float* dt = st.alloc<float>(nt, &rc);
-    if (rc) return rc;
-    double* de = st.alloc<double>(n_poses, &rc);
-    if (rc) return rc;
-    int* dn = st.alloc<int>(n_poses, &rc);
-    if (rc) return rc;
-    int* ds = st.alloc<int>(n_poses, &rc);
-    if (rc) return rc;
-    int* di = st.alloc<int>(n_poses, &rc);
-    if (rc) return rc;
-    cudaMemcpyAsync(dx, hx.data(), nx * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    if (nt) cudaMemcpyAsync(dt, ht.data(), nt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(di, ids.data(), n_poses * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
-    rc = pxd_lbfgs_dev(ctx, p, n_poses, N, di, dx, dt, de, dn, ds, ctx->stream);
-    if (rc) return rc;
-    cudaMemcpyAsync(hx.data(), dx, nx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    if (nt) cudaMemcpyAsync(ht.data(), dt, nt * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(energy, de, n_poses * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(nevals, dn, n_poses * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(status, ds, n_poses * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "lbfgs");
-    if (rc) return rc;
-    for (size_t i = 0; i < nx; ++i) xyz[i] = hx[i];
-    for (size_t i = 0; i < nt; ++i) tors[i] = ht[i];
-    return PXD_OK;
+    if (n_poses == 0) return PXD_OK;
+    return lbfgs_host(ctx, p, n_poses, ctx->ligands[lig].n_atoms, lig, nullptr, xyz, tors, energy, nevals, status);
 }
 
 int pxd_lbfgs_multi(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses, int32_t max_atoms,
@@ -1104,39 +1143,7 @@ int pxd_lbfgs_multi(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses
     if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS || (n_poses > 0 && !ligand_ids))
         return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");
     if (n_poses == 0) return PXD_OK;
-    const int R = ctx->rec.n_rotors;
-    const size_t nx = static_cast<size_t>(n_poses) * max_atoms * 3, nt = static_cast<size_t>(n_poses) * R;
-    std::vector<float> hx(nx), ht(nt);
-    for (size_t i = 0; i < nx; ++i) hx[i] = static_cast<float>(xyz[i]);
-    for (size_t i = 0; i < nt; ++i) ht[i] = static_cast<float>(tors[i]);
-    Staging st{ctx, {}};
-    float* dx = st.alloc<float>(nx, &rc);
-    if (rc) return rc;
-    float* dt = st.alloc<float>(nt, &rc);
-    if (rc) return rc;
-    double* de = st.alloc<double>(n_poses, &rc);
-    if (rc) return rc;
-    int* dn = st.alloc<int>(n_poses, &rc);
-    if (rc) return rc;
-    int* ds = st.alloc<int>(n_poses, &rc);
-    if (rc) return rc;
-    int* di = st.alloc<int>(n_poses, &rc);
-    if (rc) return rc;
-    cudaMemcpyAsync(dx, hx.data(), nx * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    if (nt) cudaMemcpyAsync(dt, ht.data(), nt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(di, ligand_ids, n_poses * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
-    rc = pxd_lbfgs_dev(ctx, p, n_poses, max_atoms, di, dx, dt, de, dn, ds, ctx->stream);
-    if (rc) return rc;
-    cudaMemcpyAsync(hx.data(), dx, nx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    if (nt) cudaMemcpyAsync(ht.data(), dt, nt * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(energy, de, n_poses * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(nevals, dn, n_poses * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(status, ds, n_poses * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "lbfgs");
-    if (rc) return rc;
-    for (size_t i = 0; i < nx; ++i) xyz[i] = hx[i];
-    for (size_t i = 0; i < nt; ++i) tors[i] = ht[i];
-    return PXD_OK;
+    return lbfgs_host(ctx, p, n_poses, max_atoms, -1, ligand_ids, xyz, tors, energy, nevals, status);
 }
 
 int pxd_ligand_kinematics(pxd_context* ctx, int32_t lig, int32_t n_poses, const double* xyz_in,
