@@ -340,17 +340,26 @@ int pxd_lbfgs(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t ligand_i
               int32_t* nevals, int32_t* status);
 
 /* Autotuner of the batched optimiser (no reference counterpart). For every size class
- * (ligands of <= 32, 64, ... 256 atoms) present in the batch, runs each register /
- * occupancy variant of the optimiser kernel (resident blocks per SM: 4, 5, 6, unbounded)
- * on up to `sample` of the class's poses with max_iter capped at probe_iters, times them
- * with CUDA events, and keeps the variant with the most score+gradient evaluations per
- * second for this context's later pxd_lbfgs* calls. Probes run on copies: the caller's
- * poses are not modified. report [8][2] (may be NULL) receives (class bound, chosen
- * variant), -1 after the last class. Synchronous. */
+ * (ligands of <= 32, 64, ... 256 atoms) present in the batch, runs each variant of the
+ * optimiser kernel -- resident blocks per SM 3, 4, 5, 6 or unbounded (the register
+ * budget), each with the L-BFGS history in global memory or, where it fits, in shared
+ * memory (+ PXD_LBFGS_HIST_SMEM) -- on up to `sample` of the class's poses with max_iter
+ * capped at probe_iters, times them with CUDA events, and keeps the variant with the most
+ * score+gradient evaluations per second for this context's later pxd_lbfgs* calls.
+ * Probes run on copies: the caller's poses are not modified. report [8][2] (may be NULL)
+ * receives (class bound, chosen variant), -1 after the last class. Synchronous. */
 int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t n_poses,
                            int32_t max_atoms, const int32_t* ligand_ids_dev, const float* xyz_dev,
                            const float* tors_dev, int32_t sample, int32_t probe_iters,
                            int32_t* report, void* stream);
+
+/* Sets the optimiser variant of one size class (class_bound 32, 64, ... 256) for this
+ * context's later pxd_lbfgs* calls, as the autotuner would: variant = resident blocks per
+ * SM (3, 4, 5, 6, or 0 for unbounded registers), + PXD_LBFGS_HIST_SMEM for the history in
+ * shared memory; -1 restores the default. Lets a caller reuse a saved tuning. Every
+ * variant computes the same arithmetic; register budgets may contract it differently. */
+#define PXD_LBFGS_HIST_SMEM 256
+int pxd_lbfgs_set_variant(pxd_context* ctx, int32_t class_bound, int32_t variant);
 
 /* Host-buffer version over poses of several ligands in one launch (the engine's
  * optimize over a whole ligand index): ligand_ids [n], xyz [n][max_atoms][3] and

@@ -158,7 +158,7 @@ using LbfgsKernelFn = void (*)(LbfgsArgs);
 
 // Variant of lbfgs_kernel: the low byte is the minimum resident blocks per SM (register
 // cap; 0 = unconstrained), kHistSmem marks the history in shared memory.
-constexpr int kHistSmem = 256;
+constexpr int kHistSmem = PXD_LBFGS_HIST_SMEM;
 static LbfgsKernelFn variant_fn(int variant) {
     switch (variant & 255) {
         case 3: return lbfgs_kernel<3>;
@@ -682,6 +682,21 @@ extern "C" int pxd_score_grad_multi_dev(pxd_context* const* ctxs, int32_t n_ctx,
 }
 
 // ------------------------------------------------------------------ autotuner
+extern "C" int pxd_lbfgs_set_variant(pxd_context* ctx, int32_t class_bound, int32_t variant) {
+    if (!ctx) return PXD_ERR_INVALID;
+    if (class_bound < 32 || class_bound > 256 || class_bound % 32)
+        return set_error(ctx, PXD_ERR_INVALID, "class bound must be 32, 64, ... 256");
+    if (variant == -1) {
+        ctx->lbfgs_tuned.erase(class_bound);
+        return PXD_OK;
+    }
+    const int blocks = variant & ~kHistSmem;
+    if (variant < 0 || !(blocks == 0 || (blocks >= 3 && blocks <= 6)))
+        return set_error(ctx, PXD_ERR_INVALID, "variant: 0 or 3..6 resident blocks, + PXD_LBFGS_HIST_SMEM");
+    ctx->lbfgs_tuned[class_bound] = variant;
+    return PXD_OK;
+}
+
 extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* params, int32_t n_poses,
                                       int32_t max_atoms, const int32_t* ids, const float* xyz, const float* tors,
                                       int32_t sample, int32_t probe_iters, int32_t* report, void* stream) {

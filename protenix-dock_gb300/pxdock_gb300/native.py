@@ -89,11 +89,15 @@ def load(auto_build=False):
     lib.pxd_score_hvp_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 13
     lib.pxd_lbfgs_autotune_dev.argtypes = [vp, C.POINTER(abi.LbfgsParams), C.c_int32, C.c_int32, vp, vp, vp,
                                            C.c_int32, C.c_int32, abi.i32p, vp]
+    lib.pxd_lbfgs_set_variant.argtypes = [vp, C.c_int32, C.c_int32]
     lib.pxd_ligand_pose_dir_multi_dev.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [vp] * 10
     lib.pxd_ligand_pose_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 6
     lib.pxd_ligand_pose_backward_dev.argtypes = [vp, C.c_int32, C.c_int32] + [vp] * 8
     _lib = lib
     return lib
+
+
+LBFGS_HIST_SMEM = 256  # PXD_LBFGS_HIST_SMEM: a variant's history-in-shared-memory flag
 
 
 def _p(a, t=C.c_double):
@@ -290,6 +294,10 @@ class Context:
         self._check(self.lib.pxd_lbfgs_autotune_dev(self.h, C.byref(params), n_poses, max_atoms, ids_ptr, xyz_ptr,
                                                     tors_ptr, sample, probe_iters, _p(rep, C.c_int32), stream))
         return {int(rep[2 * k]): int(rep[2 * k + 1]) for k in range(8) if rep[2 * k] >= 0}
+
+    def lbfgs_set_variant(self, class_bound, variant):
+        """pxd_lbfgs_set_variant: pins the optimiser variant of one size class (-1: default)."""
+        self._check(self.lib.pxd_lbfgs_set_variant(self.h, class_bound, variant))
 
     def lbfgs_dev_noalloc(self, params, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
                           nevals_ptr, status_ptr, stream=None):

@@ -64,6 +64,19 @@ def test_size_classes_match_single_ligand_launches():
         assert np.array_equal(mixed[0][rows, : l.n_atoms], single[0])
         for a, b in zip(mixed[1:], single[1:]):
             assert np.array_equal(a[rows], b)
+    # the history in shared memory instead of the global slab changes where S and Y live,
+    # not the arithmetic: the same launch, bit for bit
+    for b in (32, 64, 96):
+        ctx.lbfgs_set_variant(b, 4 | native.LBFGS_HIST_SMEM)
+    smem_hist = run(xyz, lig_ids, maxN)
+    for a, b in zip(smem_hist, mixed):
+        assert np.array_equal(a, b)
+    for b in (32, 64, 96):
+        ctx.lbfgs_set_variant(b, -1)
+    with pytest.raises(native.NativeError):
+        ctx.lbfgs_set_variant(48, 4)
+    with pytest.raises(native.NativeError):
+        ctx.lbfgs_set_variant(64, 7)
     # the autotuner picks a variant per size class from timed probes on copies; the
     # caller's poses are untouched and the tuned launch optimises to the same results
     x = torch.from_numpy(np.ascontiguousarray(xyz, np.float32)).to(dev)
