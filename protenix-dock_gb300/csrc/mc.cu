@@ -137,6 +137,7 @@ struct McArgs {
     double blo[3], bhi[3];  // the box as given, for the random centre draws
     uint32_t seed;
     int n_local, D_pad;
+    int warps_per_block;  // kMcWarps, or 1 when there are too few walkers to fill the SMs
     float* hist;
     size_t hist_stride;
     MtState* rng;
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     KinShared& ks = *reinterpret_cast<KinShared*>(kc + a.max_atoms);
     float* tq = reinterpret_cast<float*>(&ks + 1);          // [64] torsions of a move
     double* bc = reinterpret_cast<double*>(tq + 64);         // [8] broadcast slots
-    const size_t gw = static_cast<size_t>(blockIdx.x) * kMcWarps + wib;
+    const size_t gw = static_cast<size_t>(blockIdx.x) * a.warps_per_block + wib;
     v.S = a.hist + gw * a.hist_stride;
     v.Y = v.S + static_cast<size_t>(m) * Dp;
     MtState* rng = a.rng + gw;
@@ -556,20 +557,24 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     a.seed = p->seed;
     a.n_local = ctx->rec.n_local;
     a.D_pad = (3 * max_atoms + ctx->rec.n_rotors + kWarp - 1) / kWarp * kWarp;
-    const size_t smem = sizeof(float) * kMcWarps * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history);
+    // Fewer walkers than 4 per SM (a single docking search): one warp per block, so each
+    // walker has an SM's L1, shared-memory pipe and issue slots to itself.
+    a.warps_per_block = n_walkers < kMcWarps * ctx->n_sm ? 1 : kMcWarps;
+    const int wpb = a.warps_per_block;
+    const size_t smem = sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history);
     rc = cuda_check(ctx, cudaFuncSetAttribute(mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(smem)),
                     "mc smem attribute");
     if (rc) return rc;
     int per_sm = 0;
-    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel, kMcWarps * kWarp, smem),
+    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel, wpb * kWarp, smem),
                     "mc occupancy");
     if (rc) return rc;
     if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
     int blocks = per_sm * ctx->n_sm;
-    const int need = (n_walkers + kMcWarps - 1) / kMcWarps;
+    const int need = (n_walkers + wpb - 1) / wpb;
     if (blocks > need) blocks = need;
-    const size_t warps = static_cast<size_t>(blocks) * kMcWarps;
+    const size_t warps = static_cast<size_t>(blocks) * wpb;
     a.hist_stride = static_cast<size_t>(2) * p->lbfgs.history * a.D_pad;
     const size_t hist_bytes = sizeof(float) * a.hist_stride * warps;
     const size_t rng_off = (hist_bytes + 255) / 256 * 256;
@@ -582,7 +587,7 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(int), s), "counter reset");
     if (rc) return rc;
-    mc_kernel<<<blocks, kMcWarps * kWarp, smem, s>>>(a);
+    mc_kernel<<<blocks, wpb * kWarp, smem, s>>>(a);
     return cuda_check(ctx, cudaGetLastError(), "mc_kernel launch");
 }
 
