@@ -89,12 +89,12 @@ class KernelBackend:
         """(H_q u, d(u.g)/dw [36], d(u.g)/dT [32*256]) at q. Every product is linear in u,
         so u is divided by its largest row norm N (FP64) before the FP32 kernels and the
         results are multiplied by N in FP64: adjoints that grow over many unrolled steps
-        stay within FP32 range inside the kernels."""
+        stay within FP32 range inside the kernels. N stays on the device (a 0-d tensor), so
+        the backward pass queues its launches without waiting for the GPU."""
         q = q.to(torch.float32).contiguous()
         w, t = w.to(torch.float64).contiguous(), t.to(torch.float32).contiguous()
-        N = float(u.detach().to(torch.float64).norm(dim=1).max())
-        if not np.isfinite(N) or N == 0.0:
-            N = 1.0
+        N = u.detach().to(torch.float64).norm(dim=1).max()
+        N = torch.where(torch.isfinite(N) & (N > 0), N, torch.ones_like(N))
         u = (u.to(torch.float64) / N).to(torch.float32).contiguous()
         xd = torch.empty_like(x)
         native.ligand_pose_dir_multi_dev(self.ctxs, self.P, self.A, self.D, _p(self.ctx_ids), _p(self.lig_ids),
