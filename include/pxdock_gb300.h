@@ -356,8 +356,9 @@ int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* params, int
 /* Sets the optimiser variant of one size class (class_bound 32, 64, ... 256) for this
  * context's later pxd_lbfgs* calls, as the autotuner would: variant = resident blocks per
  * SM (3, 4, 5, 6, or 0 for unbounded registers), + PXD_LBFGS_HIST_SMEM for the history in
- * shared memory; -1 restores the default. Lets a caller reuse a saved tuning. Every
- * variant computes the same arithmetic; register budgets may contract it differently. */
+ * shared memory (ignored for launches whose slices would not fit it); -1 restores the
+ * default. Lets a caller reuse a saved tuning. Every variant computes the same arithmetic;
+ * register budgets may contract it differently. */
 #define PXD_LBFGS_HIST_SMEM 256
 int pxd_lbfgs_set_variant(pxd_context* ctx, int32_t class_bound, int32_t variant);
 

@@ -428,11 +428,18 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     };
     std::vector<Plan> plan;
     size_t hist_floats = 0;
+    int smem_limit = 0;
+    rc = cuda_check(ctx, cudaDeviceGetAttribute(&smem_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device),
+                    "shared memory limit");
+    if (rc) return rc;
     for (int cap : caps) {
         Plan q;
         q.cap = cap;
         q.kern = lbfgs_variant(ctx, cap);
         q.hist_smem = (lbfgs_variant_id(ctx, cap) & kHistSmem) ? 1 : 0;
+        // a pinned shared-memory history that does not fit this class falls back to the slab
+        if (q.hist_smem && lbfgs_block_smem(ctx, cap, p.history, true) > static_cast<size_t>(smem_limit))
+            q.hist_smem = 0;
         q.dp = padded(3 * cap + ctx->rec.n_rotors);
         q.smem = lbfgs_block_smem(ctx, cap, p.history, q.hist_smem);
         q.stride = q.hist_smem ? 0 : static_cast<size_t>(2) * p.history * q.dp;

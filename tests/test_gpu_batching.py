@@ -32,14 +32,14 @@ def test_size_classes_match_single_ligand_launches():
     p = native.lbfgs_params(max_iter=60, history=8, tolerance_grad=1e-3)
     tors = torch.zeros(1, device=dev)
 
-    def run(xyz, lig_ids, N):
+    def run(xyz, lig_ids, N, params=None):
         n = len(lig_ids)
         x = torch.from_numpy(np.ascontiguousarray(xyz, np.float32)).to(dev)
         d_ids = torch.from_numpy(np.asarray(lig_ids, np.int32)).to(dev)
         e = torch.zeros(n, dtype=torch.float64, device=dev)
         nev = torch.zeros(n, dtype=torch.int32, device=dev)
         st = torch.full((n,), -1, dtype=torch.int32, device=dev)
-        ctx.lbfgs_dev(p, n, N, d_ids.data_ptr(), x.data_ptr(), tors.data_ptr(), e.data_ptr(), nev.data_ptr(),
+        ctx.lbfgs_dev(params or p, n, N, d_ids.data_ptr(), x.data_ptr(), tors.data_ptr(), e.data_ptr(), nev.data_ptr(),
                       st.data_ptr())
         torch.cuda.synchronize()
         return x.cpu().numpy(), e.cpu().numpy(), nev.cpu().numpy(), st.cpu().numpy()
@@ -73,6 +73,17 @@ def test_size_classes_match_single_ligand_launches():
         assert np.array_equal(a, b)
     for b in (32, 64, 96):
         ctx.lbfgs_set_variant(b, -1)
+    # at history 100 the shared-memory history of the largest class does not fit: the
+    # pinned variant falls back to the global slab, and the launch is the default one
+    p100 = native.lbfgs_params(max_iter=20, history=100, tolerance_grad=1e-3)
+    big = starts[2].astype(np.float32)
+    ids_big = np.full(per, ids[2], np.int32)
+    plain = run(big, ids_big, ligs[2].n_atoms, p100)
+    ctx.lbfgs_set_variant(96, 4 | native.LBFGS_HIST_SMEM)
+    pinned = run(big, ids_big, ligs[2].n_atoms, p100)
+    ctx.lbfgs_set_variant(96, -1)
+    for a, b in zip(pinned, plain):
+        assert np.array_equal(a, b)
     with pytest.raises(native.NativeError):
         ctx.lbfgs_set_variant(48, 4)
     with pytest.raises(native.NativeError):
