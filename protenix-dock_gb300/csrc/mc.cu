@@ -566,17 +566,19 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
                                               static_cast<int>(smem)),
                     "mc smem attribute");
     if (rc) return rc;
-    // One-warp blocks leave most SMs with a single block: ask for the smallest shared-memory
-    // carve-out that holds it (percent of the SM's shared memory), so the rest serves as L1;
-    // full launches keep the driver's choice.
+    // One-warp blocks leave the SMs nearly empty: ask for the smallest shared-memory carve-out
+    // (percent of the SM's shared memory) that still holds the blocks each SM must run at
+    // once for every walker to start together, so the rest serves as L1; full launches keep
+    // the driver's choice.
     int carveout = cudaSharedmemCarveoutDefault;
     if (wpb == 1) {
         int sm_smem = 0;
         rc = cuda_check(ctx, cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device),
                         "shared memory per SM");
         if (rc) return rc;
-        const size_t need = smem + 1024;  // the block plus the driver's reserved kilobyte
-        carveout = std::min(100, static_cast<int>((100 * need + sm_smem - 1) / sm_smem) + 1);
+        const size_t per_sm_blocks = (static_cast<size_t>(n_walkers) + ctx->n_sm - 1) / ctx->n_sm;
+        const size_t need = per_sm_blocks * (smem + 1024);  // each block plus the driver's reserved kilobyte
+        carveout = static_cast<int>(std::min<size_t>(100, (100 * need + sm_smem - 1) / sm_smem + 1));
     }
     rc = cuda_check(ctx, cudaFuncSetAttribute(mc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carveout),
                     "mc carve-out");
