@@ -190,6 +190,12 @@ class Context:
     def __del__(self):
         self.close()
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def _check(self, rc):
         if rc != 0:
             raise NativeError(rc, self.lib.pxd_last_error(self.h).decode())
