@@ -152,8 +152,21 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_baseline(rec, lig, box, poses, target_s=15.0, use_ref=False):
-    """The reference algorithm on the host cores over a bounded sample of poses."""
+def ncu_warp_instructions_per_eval():
+    """Warp instructions per score+gradient evaluation of the batched kernel, from the
+    committed ncu summary (smsp__inst_executed.sum / evaluations of the captured launch)."""
+    path = os.path.join(REPO, "profiles", "lbfgs_kernel_ncu.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("warp_instructions_per_eval:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def cpu_baseline(rec, lig, box, poses, target_s=15.0, use_ref=False, keep=None):
+    """The reference algorithm on the host cores over a bounded sample of poses. With
+    `keep` (a dict), the port's results on the sample are stored in keep["port"]."""
     import oracle
     from pxdock_gb300 import abi
 
@@ -166,11 +179,13 @@ def cpu_baseline(rec, lig, box, poses, target_s=15.0, use_ref=False):
     n = max(threads, 16)
     while True:
         t0 = time.perf_counter()
-        port.lbfgs_batch(p, np.zeros((n, 0)), poses[:n], threads)
+        res = port.lbfgs_batch(p, np.zeros((n, 0)), poses[:n], threads)
         dt = time.perf_counter() - t0
         if dt >= target_s or n >= len(poses):
             break
         n = min(len(poses), int(n * max(2.0, target_s / max(dt, 1e-3) * 1.1)))
+    if keep is not None:
+        keep["port"] = res
     return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d of the %d poses, FP64 C port of the reference optimiser, %d threads, "
                       "%.1f s" % (n, N_POSES, threads, dt)}
@@ -1002,6 +1017,7 @@ def main():
     evals_total = evals_step * args.steps
     st = status.cpu().numpy()
     e_final = energy.cpu().numpy()
+    gpu_out = {"xyz": xyz.cpu().numpy(), "energy": e_final, "nevals": nevals.cpu().numpy(), "status": st}
     t_dev = sum(kernel_ms) / 1000.0
     if dist:
         tt = torch.tensor([t_dev], device=dev)
@@ -1021,10 +1037,15 @@ def main():
     for i in range(n_plain):
         ctx.lbfgs(p, lid, poses[i:i + 1])
     plain_value = n_plain / (time.perf_counter() - t1)
-    peak, peak_kind = measured_peak()
+    hbm_peak, peak_kind = measured_peak()
+    # the maps of the bench ligand (8 x 8.5 MB) stay L2-resident, so the bandwidth that
+    # bounds the gathers is L2's: measured here, random 16-byte gathers over 64 MiB
+    l2_peak = native.gather_bandwidth(local, 64 << 20, 10)
     bytes_per_eval = (256 + 24) * N
     achieved = evals_step * bytes_per_eval / (np.mean(kernel_ms) / 1000.0) / 1e9
     tpe = ncu_traffic_per_eval()
+    wipe = ncu_warp_instructions_per_eval()
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": float(np.mean(kernel_ms)), "higher_is_better": True,
@@ -1036,8 +1057,11 @@ def main():
                 "h2d_bytes_per_step": N_POSES * N * 3 * 8,
                 "d2h_bytes_per_step": N_POSES * (N * 3 * 8 + 8 + 4 + 4)},
         "gpu_launches": args.steps,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind,
+        "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak, "unit": "GB/s",
+                     "frac": achieved / l2_peak,
+                     "peak_kind": "measured in this run: random 16-byte gathers over 64 MiB "
+                                  "(pxd_gather_bandwidth)",
+                     "hbm_peak": hbm_peak, "hbm_frac": achieved / hbm_peak, "hbm_peak_kind": peak_kind,
                      "traffic": None if tpe is None else tpe * evals_step,
                      "algorithmic_bytes_per_eval": bytes_per_eval},
         "plain_gpu": {"value": plain_value, "unit": UNIT, "poses": n_plain,
@@ -1051,8 +1075,27 @@ def main():
     clocks = clk.summary()
     if clocks:
         line["clocks"] = clocks
+    if wipe is not None:
+        # instruction issue: warp instructions per evaluation (ncu) x evaluations/s against
+        # the SMs' four schedulers at the SM clock sampled during the timed region
+        mhz = clocks["sm_mhz"] if clocks else 2070.0
+        rate = wipe * evals_step / (np.mean(kernel_ms) / 1000.0)
+        peak_issue = n_sm * 4 * mhz * 1e6
+        line["issue"] = {"warp_instructions_per_eval": wipe, "achieved": rate, "peak": peak_issue,
+                         "unit": "warp instructions/s", "frac": rate / peak_issue,
+                         "sm_mhz": mhz, "sms": n_sm}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(rec, lig, box, poses)
+        import oracle
+
+        keep = {}
+        line["cpu_baseline"] = cpu_baseline(rec, lig, box, poses, keep=keep)
+        port = keep["port"]
+        k = len(port["energy"])
+        # outcomes of the GPU (the last timed step) and the port on the same k starts
+        gpu_k = {key: v[:k] for key, v in gpu_out.items()}
+        line["parity"] = oracle.compare_outcomes(gpu_k, port)
+        line["parity"]["what"] = ("GPU (run) against the FP64 port of the reference optimiser "
+                                  "(ref) on the cpu_baseline sample: the first %d starts" % k)
     del out
     if rank == 0:
         print(json.dumps(line))

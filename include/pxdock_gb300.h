@@ -616,6 +616,14 @@ int pxd_mc_search_multi(pxd_context* ctx, const pxd_mc_params* params, int32_t n
 int pxd_rng_draws(pxd_context* ctx, uint32_t seed, int32_t n, const int32_t* kinds,
                   const int32_t* ints, double* out);
 
+/* Measurement probe (no reference counterpart): the bandwidth of random 16-byte gathers
+ * -- the access pattern of the map lookups inside receptor_cache::get (grid.cpp:273-303)
+ * as the kernels make it -- over a working set of working_set_bytes (rounded down to a
+ * power of two) on `device`, in GB/s of bytes loaded, median of `reps` timed launches.
+ * Below the L2 size it gives the L2 gather roofline of the batched kernels whose maps
+ * stay L2-resident. Allocates and frees its own buffers. */
+int pxd_gather_bandwidth(int32_t device, int64_t working_set_bytes, int32_t reps, double* gbs);
+
 /* ------------------------------------------------------------ engine facade */
 
 /* bytedock::ReusableEngine (engine/include/bytedock/core/entrance.h:30-74) over this

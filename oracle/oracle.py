@@ -23,7 +23,9 @@ from pxdock_gb300 import abi  # noqa: E402
 
 PORT_LIB = os.path.join(HERE, "lib", "libpxd_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "liboracle_ref.so")
-REF_ENGINE = "/root/reference/engine"
+# the reference engine's source tree (engine/ of the reference checkout); the Makefile
+# reads the same variable
+REF_ENGINE = os.environ.get("REF_ENGINE", "/root/reference/engine")
 
 f64p = abi.f64p
 i32p = abi.i32p
@@ -462,3 +464,44 @@ class RefSystem:
             raise RuntimeError(self.lib.ref_last_error().decode())
         return dict(xyz=xyz.reshape(-1, 3), torsions=tors[: self.n_tors], energy=e[0],
                     pscore=ps[0], nevals=nev.value)
+
+
+# ------------------------------------------------------------------ optimiser outcomes
+# Optimiser outcomes of two runs over the same starting poses, for
+# tests/test_gpu_headline.py and bench.py's CPU-baseline leg: evaluations per pose,
+# status counts, final-energy quartiles and the fraction of poses that end within
+# 0.05 A RMSD (lbfgs_step::apply, optimizer.cpp:429-560, on both sides).
+
+OUTCOME_STATUS = ("converged", "not_converged", "nan", "bad_input")
+
+
+def pose_rmsd(a, b):
+    """Per-pose RMSD of [P][N][3] coordinate arrays."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.sqrt(np.mean(np.sum((a - b) ** 2, axis=-1), axis=-1))
+
+
+def outcome_summary(run):
+    """Population figures of one run (dict with energy, nevals, status)."""
+    st = np.asarray(run["status"])
+    e = np.asarray(run["energy"], np.float64)
+    return {
+        "evals_per_pose": float(np.mean(run["nevals"])),
+        "status": {n: int((st == k).sum()) for k, n in enumerate(OUTCOME_STATUS)},
+        "energy_quartiles": [float(v) for v in np.percentile(e, [25, 50, 75])],
+    }
+
+
+def compare_outcomes(run, ref, tol_rmsd=0.05):
+    """Figures of `run` against `ref` over the same starts (both dicts with xyz, energy,
+    nevals, status)."""
+    d = pose_rmsd(run["xyz"], ref["xyz"])
+    return {
+        "poses": int(len(d)),
+        "within_rmsd": float(np.mean(d <= tol_rmsd)),
+        "tol_rmsd": tol_rmsd,
+        "run": outcome_summary(run),
+        "ref": outcome_summary(ref),
+    }
+

@@ -388,27 +388,28 @@ int pxd_score_adjoint(pxd_context* ctx, int32_t which, int32_t lig, int32_t n_po
     double* d_dt = st.alloc<double>(kTabN, &rc);
     if (rc) return rc;
     cudaStream_t s = ctx->stream;
-    cudaMemcpyAsync(d_x, hx.data(), nx * 4, cudaMemcpyHostToDevice, s);
-    if (!ht.empty()) cudaMemcpyAsync(d_t, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_ids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_w, weights, kNumW * 8, cudaMemcpyHostToDevice, s);
-    if (tables) cudaMemcpyAsync(d_tab, htabf.data(), kTabN * 4, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_g, hg.data(), hg.size() * 8, cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(d_dw, 0, kNumW * 8, s);
-    cudaMemsetAsync(d_dt, 0, kTabN * 8, s);
+    queue_copy(ctx, &rc, d_x, hx.data(), nx * 4, cudaMemcpyHostToDevice, s);
+    if (!ht.empty()) queue_copy(ctx, &rc, d_t, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice, s);
+    queue_copy(ctx, &rc, d_ids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, s);
+    queue_copy(ctx, &rc, d_w, weights, kNumW * 8, cudaMemcpyHostToDevice, s);
+    if (tables) queue_copy(ctx, &rc, d_tab, htabf.data(), kTabN * 4, cudaMemcpyHostToDevice, s);
+    queue_copy(ctx, &rc, d_g, hg.data(), hg.size() * 8, cudaMemcpyHostToDevice, s);
+    if (!rc) rc = cuda_check(ctx, cudaMemsetAsync(d_dw, 0, kNumW * 8, s), "weight gradient clear");
+    if (!rc) rc = cuda_check(ctx, cudaMemsetAsync(d_dt, 0, kTabN * 8, s), "table gradient clear");
+    if (rc) return rc;
     rc = pxd_score_adjoint_dev(ctx, which, n_poses, N, d_ids, d_x, d_t, d_w, d_tab, grad ? d_g : nullptr, d_s, d_f,
                                grad ? d_dx : nullptr, grad ? d_dw : nullptr, grad ? d_dt : nullptr, s);
     if (rc) return rc;
     std::vector<double> os(n_poses), of(static_cast<size_t>(n_poses) * kNumF), odw(kNumW), odt(kTabN);
     std::vector<float> odx(grad ? nx : 0);
-    cudaMemcpyAsync(os.data(), d_s, os.size() * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(of.data(), d_f, of.size() * 8, cudaMemcpyDeviceToHost, s);
+    queue_copy(ctx, &rc, os.data(), d_s, os.size() * 8, cudaMemcpyDeviceToHost, s);
+    queue_copy(ctx, &rc, of.data(), d_f, of.size() * 8, cudaMemcpyDeviceToHost, s);
     if (grad) {
-        cudaMemcpyAsync(odx.data(), d_dx, nx * 4, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(odw.data(), d_dw, kNumW * 8, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(odt.data(), d_dt, kTabN * 8, cudaMemcpyDeviceToHost, s);
+        queue_copy(ctx, &rc, odx.data(), d_dx, nx * 4, cudaMemcpyDeviceToHost, s);
+        queue_copy(ctx, &rc, odw.data(), d_dw, kNumW * 8, cudaMemcpyDeviceToHost, s);
+        queue_copy(ctx, &rc, odt.data(), d_dt, kTabN * 8, cudaMemcpyDeviceToHost, s);
     }
-    rc = cuda_check(ctx, cudaStreamSynchronize(s), "score adjoint");
+    rc = sync_copies(ctx, rc, s, "score adjoint");
     if (rc) return rc;
     if (score) std::copy(os.begin(), os.end(), score);
     if (features) std::copy(of.begin(), of.end(), features);

@@ -1063,16 +1063,17 @@ int pxd_score_grad(pxd_context* ctx, int32_t lig, int32_t n_poses, const double*
     if (rc) return rc;
     int* di = st.alloc<int>(n_poses, &rc);
     if (rc) return rc;
-    cudaMemcpyAsync(dx, hx.data(), nx * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    if (nt) cudaMemcpyAsync(dt, ht.data(), nt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(di, ids.data(), n_poses * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    queue_copy(ctx, &rc, dx, hx.data(), nx * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (nt) queue_copy(ctx, &rc, dt, ht.data(), nt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    queue_copy(ctx, &rc, di, ids.data(), n_poses * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    if (rc) return rc;
     rc = pxd_score_grad_dev(ctx, n_poses, N, di, dx, dt, de, dg, dtg, ctx->stream);
     if (rc) return rc;
     std::vector<float> hg(nx), htg(nt);
-    cudaMemcpyAsync(energy, de, n_poses * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(hg.data(), dg, nx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    if (nt) cudaMemcpyAsync(htg.data(), dtg, nt * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "score_grad");
+    queue_copy(ctx, &rc, energy, de, n_poses * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    queue_copy(ctx, &rc, hg.data(), dg, nx * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (nt) queue_copy(ctx, &rc, htg.data(), dtg, nt * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    rc = sync_copies(ctx, rc, ctx->stream, "score_grad");
     if (rc) return rc;
     for (size_t i = 0; i < nx; ++i) lig_grad[i] = hg[i];
     for (size_t i = 0; i < nt; ++i) tors_grad[i] = htg[i];
@@ -1173,13 +1174,23 @@ int pxd_ligand_kinematics(pxd_context* ctx, int32_t lig, int32_t n_poses, const 
     if (rc) return rc;
     float* dout = st.alloc<float>(ho.size(), &rc);
     if (rc) return rc;
-    cudaMemcpyAsync(dx, hx.data(), hx.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(dc, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(dr, hr.data(), hr.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
-    if (!ht.empty()) cudaMemcpyAsync(dt, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    rc = cuda_check(ctx, cudaMemcpyAsync(dx, hx.data(), hx.size() * 4, cudaMemcpyHostToDevice, ctx->stream),
+                    "ligand kinematics: coordinates to the device");
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpyAsync(dc, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, ctx->stream),
+                        "ligand kinematics: centres to the device");
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpyAsync(dr, hr.data(), hr.size() * 4, cudaMemcpyHostToDevice, ctx->stream),
+                        "ligand kinematics: rotations to the device");
+    if (!rc && !ht.empty())
+        rc = cuda_check(ctx, cudaMemcpyAsync(dt, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice, ctx->stream),
+                        "ligand kinematics: torsions to the device");
+    if (rc) return rc;
     rc = launch_ligand_kinematics(ctx, lig, n_poses, dx, dc, dr, dt, dout, ctx->stream);
     if (rc) return rc;
-    cudaMemcpyAsync(ho.data(), dout, ho.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    rc = cuda_check(ctx, cudaMemcpyAsync(ho.data(), dout, ho.size() * 4, cudaMemcpyDeviceToHost, ctx->stream),
+                    "ligand kinematics: coordinates to the host");
+    if (rc) return rc;
     rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ligand kinematics");
     if (rc) return rc;
     for (size_t i = 0; i < ho.size(); ++i) xyz_out[i] = ho[i];
@@ -1217,16 +1228,17 @@ int pxd_ligand_backward(pxd_context* ctx, int32_t lig, int32_t n_poses, const do
     if (rc) return rc;
     float* dtt = st.alloc<float>(static_cast<size_t>(n_poses) * T, &rc);
     if (rc) return rc;
-    cudaMemcpyAsync(dx, hx.data(), nx * 4, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(dg, hg.data(), nx * 4, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(dc, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    queue_copy(ctx, &rc, dx, hx.data(), nx * 4, cudaMemcpyHostToDevice, ctx->stream);
+    queue_copy(ctx, &rc, dg, hg.data(), nx * 4, cudaMemcpyHostToDevice, ctx->stream);
+    queue_copy(ctx, &rc, dc, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (rc) return rc;
     rc = launch_ligand_backward(ctx, lig, n_poses, dx, dc, dg, doc, dot, dtt, ctx->stream);
     if (rc) return rc;
     std::vector<float> oc(hc.size()), oq(hc.size()), ot(static_cast<size_t>(n_poses) * T);
-    cudaMemcpyAsync(oc.data(), doc, oc.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
-    cudaMemcpyAsync(oq.data(), dot, oq.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
-    if (!ot.empty()) cudaMemcpyAsync(ot.data(), dtt, ot.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ligand backward");
+    queue_copy(ctx, &rc, oc.data(), doc, oc.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    queue_copy(ctx, &rc, oq.data(), dot, oq.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (!ot.empty()) queue_copy(ctx, &rc, ot.data(), dtt, ot.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    rc = sync_copies(ctx, rc, ctx->stream, "ligand backward");
     if (rc) return rc;
     for (size_t i = 0; i < oc.size(); ++i) {
         center_grad[i] = oc[i];
@@ -1247,11 +1259,12 @@ int pxd_receptor_kinematics(pxd_context* ctx, int32_t n_poses, const double* tor
     if (rc) return rc;
     float* dout = st.alloc<float>(ho.size(), &rc);
     if (rc) return rc;
-    if (!ht.empty()) cudaMemcpyAsync(dt, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (!ht.empty()) queue_copy(ctx, &rc, dt, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (rc) return rc;
     rc = launch_receptor_kinematics(ctx, n_poses, dt, dout, ctx->stream);
     if (rc) return rc;
-    cudaMemcpyAsync(ho.data(), dout, ho.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "receptor kinematics");
+    queue_copy(ctx, &rc, ho.data(), dout, ho.size() * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    rc = sync_copies(ctx, rc, ctx->stream, "receptor kinematics");
     if (rc) return rc;
     for (size_t i = 0; i < ho.size(); ++i) xyz_out[i] = ho[i];
     return PXD_OK;

@@ -157,8 +157,12 @@ int launch_receptor_kinematics(pxd_context* ctx, int n_poses, const float* tors,
     const size_t b0 = sizeof(float4) * M, b1 = sizeof(int) * M;
     int rc = cuda_check(ctx, cudaMallocAsync(&mem, b0 + b1, s), "receptor kinematics tables");
     if (rc) return rc;
-    cudaMemcpyAsync(mem, xyz0.data(), b0, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(static_cast<char*>(mem) + b0, rotor.data(), b1, cudaMemcpyHostToDevice, s);
+    queue_copy(ctx, &rc, mem, xyz0.data(), b0, cudaMemcpyHostToDevice, s);
+    queue_copy(ctx, &rc, static_cast<char*>(mem) + b0, rotor.data(), b1, cudaMemcpyHostToDevice, s);
+    if (rc) {
+        cudaFreeAsync(mem, s);
+        return rc;
+    }
     RecKinArgs a{n_poses, M, ctx->rec.n_rotors, static_cast<float4*>(mem),
                  reinterpret_cast<int*>(static_cast<char*>(mem) + b0), ctx->rec.rotor_origin,
                  ctx->rec.rotor_axis, tors, out};

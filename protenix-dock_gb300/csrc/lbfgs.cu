@@ -381,6 +381,23 @@ int class_join(pxd_context* ctx, size_t k, cudaStream_t s) {
     return rc;
 }
 
+// Raises a kernel variant's dynamic shared-memory limit to at least `bytes`, never
+// lowering it. The limit is a process-wide property of the kernel on the current device:
+// a launcher on another thread that set a larger limit for its own launch must not see it
+// lowered between its attribute call and its launch.
+static int raise_smem_limit(pxd_context* ctx, LbfgsKernelFn kern, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> limit;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = limit[{ctx->device, reinterpret_cast<const void*>(kern)}];
+    if (bytes <= cur) return PXD_OK;
+    const int rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        static_cast<int>(bytes)),
+                              "lbfgs smem attribute");
+    if (!rc) cur = bytes;
+    return rc;
+}
+
 static void fill_consts(LbfgsArgs& a, const pxd_lbfgs_params& p) {
     a.c.max_iter = p.max_iter;
     a.c.max_eval = p.max_eval;
@@ -450,9 +467,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     std::map<LbfgsKernelFn, size_t> smem_of;
     for (const Plan& q : plan) smem_of[q.kern] = std::max(smem_of[q.kern], q.smem);
     for (const auto& [kern, bytes] : smem_of) {
-        rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  static_cast<int>(bytes)),
-                        "lbfgs smem attribute");
+        rc = raise_smem_limit(ctx, kern, bytes);
         if (rc) return rc;
     }
     for (Plan& q : plan) {
@@ -569,26 +584,12 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.stride_atoms = max_atoms;
     a.order = nullptr;
     a.count_dev = nullptr;
-    a.c.max_iter = p.max_iter;
-    a.c.max_eval = p.max_eval;
-    a.c.m = p.history;
-    a.c.ls_max = p.ls_max;
-    a.c.lr = p.lr;
-    a.c.tol_grad = p.tolerance_grad;
-    a.c.tol_change = p.tolerance_change;
-    a.c.c1 = p.ls_c1;
-    a.c.c2 = p.ls_c2;
-    a.c.ls_tol_change = p.ls_tolerance_change;
-    a.c.gtd_threshold = p.ls_gtd_threshold;
-    a.c.reset = p.reset_threshold;
+    fill_consts(a, p);
     a.n_local = ctx->rec.n_local;
     a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
-    const int per_warp = pose_bufs_floats(max_atoms, a.n_local) + kOptVecs * a.D_pad + 4 * p.history;
-    const size_t smem = sizeof(float) * kWarpsPerBlock * per_warp;
+    const size_t smem = lbfgs_block_smem(ctx, max_atoms, p.history, false);
     const LbfgsKernelFn kern = lbfgs_variant(ctx, max_atoms);
-    rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(smem)),
-                    "lbfgs smem attribute");
+    rc = raise_smem_limit(ctx, kern, smem);
     if (rc) return rc;
     int per_sm = 0;
     rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern,
@@ -655,9 +656,20 @@ extern "C" int pxd_score_grad_multi_dev(pxd_context* const* ctxs, int32_t n_ctx,
     int rc = cuda_check(ctx, cudaMallocAsync(&mem, e_bytes + t_bytes + sizeof(int) * n_ctx, s), "context tables");
     if (rc) return rc;
     char* base = static_cast<char*>(mem);
-    cudaMemcpyAsync(base, envs.data(), sizeof(EvalEnv) * n_ctx, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(base + e_bytes, tabs.data(), sizeof(void*) * n_ctx, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(base + e_bytes + t_bytes, n_ligs.data(), sizeof(int) * n_ctx, cudaMemcpyHostToDevice, s);
+    rc = cuda_check(ctx, cudaMemcpyAsync(base, envs.data(), sizeof(EvalEnv) * n_ctx, cudaMemcpyHostToDevice, s),
+                    "context table copy");
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpyAsync(base + e_bytes, tabs.data(), sizeof(void*) * n_ctx,
+                                             cudaMemcpyHostToDevice, s),
+                        "ligand table pointer copy");
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpyAsync(base + e_bytes + t_bytes, n_ligs.data(), sizeof(int) * n_ctx,
+                                             cudaMemcpyHostToDevice, s),
+                        "ligand count copy");
+    if (rc) {
+        cudaFreeAsync(mem, s);
+        return rc;
+    }
     ScoreMultiArgs a{};
     a.envs = reinterpret_cast<const EvalEnv*>(base);
     a.tabs = reinterpret_cast<const DevLigand* const*>(base + e_bytes);
@@ -750,15 +762,18 @@ extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* 
         int* d_n = rc ? nullptr : st.alloc<int>(m, &rc);
         int* d_s = rc ? nullptr : st.alloc<int>(m, &rc);
         if (rc) return rc;
-        cudaMemcpyAsync(d_ids, rid.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s);
-        for (int k = 0; k < m; ++k) {  // gather the sampled rows at the class's stride
-            cudaMemcpy2DAsync(d_x0 + static_cast<size_t>(k) * cap * 3, sizeof(float) * cap * 3,
-                              xyz + static_cast<size_t>(rows[k]) * max_atoms * 3, sizeof(float) * max_atoms * 3,
-                              sizeof(float) * cap * 3, 1, cudaMemcpyDeviceToDevice, s);
+        queue_copy(ctx, &rc, d_ids, rid.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s, "autotune ids");
+        for (int k = 0; k < m && !rc; ++k) {  // gather the sampled rows at the class's stride
+            rc = cuda_check(ctx, cudaMemcpy2DAsync(d_x0 + static_cast<size_t>(k) * cap * 3, sizeof(float) * cap * 3,
+                                                   xyz + static_cast<size_t>(rows[k]) * max_atoms * 3,
+                                                   sizeof(float) * max_atoms * 3, sizeof(float) * cap * 3, 1,
+                                                   cudaMemcpyDeviceToDevice, s),
+                            "autotune pose gather");
             if (R > 0)
-                cudaMemcpyAsync(d_t0 + static_cast<size_t>(k) * R, tors + static_cast<size_t>(rows[k]) * R,
-                                sizeof(float) * R, cudaMemcpyDeviceToDevice, s);
+                queue_copy(ctx, &rc, d_t0 + static_cast<size_t>(k) * R, tors + static_cast<size_t>(rows[k]) * R,
+                           sizeof(float) * R, cudaMemcpyDeviceToDevice, s, "autotune torsion gather");
         }
+        if (rc) return rc;
         cudaEvent_t a, b;
         cudaEventCreate(&a);
         cudaEventCreate(&b);
@@ -771,8 +786,11 @@ extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* 
             if ((v & kHistSmem) && lbfgs_block_smem(ctx, cap, p.history, true) > static_cast<size_t>(smem_limit))
                 continue;  // the history does not fit beside the pose buffers
             ctx->lbfgs_tuned[bound] = v;
-            cudaMemcpyAsync(d_x, d_x0, sizeof(float) * m * cap * 3, cudaMemcpyDeviceToDevice, s);
-            cudaMemcpyAsync(d_t, d_t0, sizeof(float) * m * std::max(R, 1), cudaMemcpyDeviceToDevice, s);
+            queue_copy(ctx, &rc, d_x, d_x0, sizeof(float) * m * cap * 3, cudaMemcpyDeviceToDevice, s,
+                       "autotune pose restore");
+            queue_copy(ctx, &rc, d_t, d_t0, sizeof(float) * m * std::max(R, 1), cudaMemcpyDeviceToDevice, s,
+                       "autotune torsion restore");
+            if (rc) break;
             cudaEventRecord(a, s);
             rc = launch_lbfgs(ctx, p, m, cap, d_ids, d_x, d_t, d_e, d_n, d_s, s);
             cudaEventRecord(b, s);

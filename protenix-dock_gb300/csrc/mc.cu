@@ -636,28 +636,36 @@ int pxd_mc_search(pxd_context* ctx, const pxd_mc_params* p, int32_t lig, int32_t
     int* d_first = d_w + n;
     int* d_nev = d_first + n;
     int* d_st = d_nev + n;
-    cudaMemcpyAsync(d_start, hx.data(), 4 * nx, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_ids, ids.data(), 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_w, walker_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_first, first_pose, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_gm, gm.data(), 8 * gm.size(), cudaMemcpyHostToDevice, ctx->stream);
-    rc = pxd_mc_search_dev(ctx, p, n, N, d_ids, d_w, d_first, d_start, d_out, d_tors, d_e, d_ps, d_nev, d_st, d_gm,
+    queue_copy(ctx, &rc, d_start, hx.data(), 4 * nx, cudaMemcpyHostToDevice, ctx->stream, "search starts");
+    queue_copy(ctx, &rc, d_ids, ids.data(), 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream,
+               "search ligand ids");
+    queue_copy(ctx, &rc, d_w, walker_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream,
+               "search walker ids");
+    queue_copy(ctx, &rc, d_first, first_pose, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream,
+               "search first-pose flags");
+    queue_copy(ctx, &rc, d_gm, gm.data(), 8 * gm.size(), cudaMemcpyHostToDevice, ctx->stream, "search radii");
+    if (!rc) rc = pxd_mc_search_dev(ctx, p, n, N, d_ids, d_w, d_first, d_start, d_out, d_tors, d_e, d_ps, d_nev, d_st, d_gm,
                            ctx->stream);
     std::vector<float> ho(nx), ht(nt);
     if (!rc) {
-        cudaMemcpyAsync(ho.data(), d_out, 4 * nx, cudaMemcpyDeviceToHost, ctx->stream);
-        if (nt) cudaMemcpyAsync(ht.data(), d_tors, 4 * nt, cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_e, d_e, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_ps, d_ps, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_nev, d_nev, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_st, d_st, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
+        queue_copy(ctx, &rc, ho.data(), d_out, 4 * nx, cudaMemcpyDeviceToHost, ctx->stream, "search poses");
+        if (nt) queue_copy(ctx, &rc, ht.data(), d_tors, 4 * nt, cudaMemcpyDeviceToHost, ctx->stream, "search torsions");
+        queue_copy(ctx, &rc, out_e, d_e, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search energies");
+        queue_copy(ctx, &rc, out_ps, d_ps, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search pose scores");
+        queue_copy(ctx, &rc, out_nev, d_nev, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search evaluations");
+        queue_copy(ctx, &rc, out_st, d_st, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search status");
     }
     cudaFreeAsync(mem, ctx->stream);
-    if (rc) return rc;
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "search");
+    rc = sync_copies(ctx, rc, ctx->stream, "search");
     if (rc) return rc;
     int err = 0;
-    cudaMemcpy(&err, ctx->d_counter + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    rc = cuda_check(ctx, cudaMemcpy(&err, ctx->d_counter + 1, sizeof(int), cudaMemcpyDeviceToHost),
+                    "search start flag");
+    if (rc) return rc;
     for (size_t i = 0; i < nx; ++i) out_xyz[i] = ho[i];
     for (size_t i = 0; i < nt; ++i) out_tors[i] = ht[i];
     if (err) return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a random start found no pose inside the box");
@@ -698,29 +706,37 @@ int pxd_mc_search_multi(pxd_context* ctx, const pxd_mc_params* p, int32_t n, int
     int* d_first = d_w + n;
     int* d_nev = d_first + n;
     int* d_st = d_nev + n;
-    cudaMemcpyAsync(d_start, hx.data(), 4 * nx, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_ids, ligand_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_w, walker_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_first, first_pose, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_gm, gm.data(), 8 * gm.size(), cudaMemcpyHostToDevice, ctx->stream);
-    rc = pxd_mc_search_dev(ctx, p, n, max_atoms, d_ids, d_w, d_first, d_start, d_out, d_tors, d_e, d_ps, d_nev,
+    queue_copy(ctx, &rc, d_start, hx.data(), 4 * nx, cudaMemcpyHostToDevice, ctx->stream, "search starts");
+    queue_copy(ctx, &rc, d_ids, ligand_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream,
+               "search ligand ids");
+    queue_copy(ctx, &rc, d_w, walker_ids, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream,
+               "search walker ids");
+    queue_copy(ctx, &rc, d_first, first_pose, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream,
+               "search first-pose flags");
+    queue_copy(ctx, &rc, d_gm, gm.data(), 8 * gm.size(), cudaMemcpyHostToDevice, ctx->stream, "search minima");
+    if (!rc) rc = pxd_mc_search_dev(ctx, p, n, max_atoms, d_ids, d_w, d_first, d_start, d_out, d_tors, d_e, d_ps, d_nev,
                            d_st, d_gm, ctx->stream);
     std::vector<float> ho(nx), ht(nt);
     if (!rc) {
-        cudaMemcpyAsync(ho.data(), d_out, 4 * nx, cudaMemcpyDeviceToHost, ctx->stream);
-        if (nt) cudaMemcpyAsync(ht.data(), d_tors, 4 * nt, cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_e, d_e, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_ps, d_ps, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_nev, d_nev, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(out_st, d_st, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(gm.data(), d_gm, 8 * gm.size(), cudaMemcpyDeviceToHost, ctx->stream);
+        queue_copy(ctx, &rc, ho.data(), d_out, 4 * nx, cudaMemcpyDeviceToHost, ctx->stream, "search poses");
+        if (nt) queue_copy(ctx, &rc, ht.data(), d_tors, 4 * nt, cudaMemcpyDeviceToHost, ctx->stream, "search torsions");
+        queue_copy(ctx, &rc, out_e, d_e, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search energies");
+        queue_copy(ctx, &rc, out_ps, d_ps, 8 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search pose scores");
+        queue_copy(ctx, &rc, out_nev, d_nev, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search evaluations");
+        queue_copy(ctx, &rc, out_st, d_st, 4 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, ctx->stream,
+                   "search status");
+        queue_copy(ctx, &rc, gm.data(), d_gm, 8 * gm.size(), cudaMemcpyDeviceToHost, ctx->stream, "search minima");
     }
     cudaFreeAsync(mem, ctx->stream);
-    if (rc) return rc;
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "search");
+    rc = sync_copies(ctx, rc, ctx->stream, "search");
     if (rc) return rc;
     int err = 0;
-    cudaMemcpy(&err, ctx->d_counter + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    rc = cuda_check(ctx, cudaMemcpy(&err, ctx->d_counter + 1, sizeof(int), cudaMemcpyDeviceToHost),
+                    "search start flag");
+    if (rc) return rc;
     for (size_t i = 0; i < nx; ++i) out_xyz[i] = ho[i];
     for (size_t i = 0; i < nt; ++i) out_tors[i] = ht[i];
     if (global_min)
@@ -746,14 +762,15 @@ int pxd_rng_draws(pxd_context* ctx, uint32_t seed, int32_t n, const int32_t* kin
     int* d_k = reinterpret_cast<int*>(d_out + total);
     int* d_i = d_k + n;
     MtState* d_s = reinterpret_cast<MtState*>(reinterpret_cast<char*>(d_i + n) + (16 - ((8 * total + 8 * n) % 16)) % 16);
-    cudaMemcpyAsync(d_k, kinds, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_i, ints, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream);
-    rng_draws_kernel<<<1, 32, 0, ctx->stream>>>(seed, n, d_k, d_i, d_out, d_s);
-    rc = cuda_check(ctx, cudaGetLastError(), "rng_draws_kernel launch");
-    if (!rc) cudaMemcpyAsync(out, d_out, 8 * static_cast<size_t>(total), cudaMemcpyDeviceToHost, ctx->stream);
+    queue_copy(ctx, &rc, d_k, kinds, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream, "draw kinds");
+    queue_copy(ctx, &rc, d_i, ints, 4 * static_cast<size_t>(n), cudaMemcpyHostToDevice, ctx->stream, "draw bounds");
+    if (!rc) {
+        rng_draws_kernel<<<1, 32, 0, ctx->stream>>>(seed, n, d_k, d_i, d_out, d_s);
+        rc = cuda_check(ctx, cudaGetLastError(), "rng_draws_kernel launch");
+    }
+    queue_copy(ctx, &rc, out, d_out, 8 * static_cast<size_t>(total), cudaMemcpyDeviceToHost, ctx->stream, "draws");
     cudaFreeAsync(mem, ctx->stream);
-    if (rc) return rc;
-    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "rng draws");
+    return sync_copies(ctx, rc, ctx->stream, "rng draws");
 }
 
 }  // extern "C"

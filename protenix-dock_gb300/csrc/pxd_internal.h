@@ -265,6 +265,23 @@ void gbsa_properties(const pxd_score_lists* l, int n, std::vector<double>& radiu
                      std::vector<double>& screen);
 
 // Host-buffer wrappers stage their arrays in stream-ordered device allocations.
+// Queues one asynchronous copy unless an earlier step failed (*rc != 0), keeping the first
+// failure in *rc and in the context's error string. Zero-byte copies are skipped.
+inline void queue_copy(pxd_context* ctx, int* rc, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind,
+                       cudaStream_t s, const char* what = "copy") {
+    if (*rc || bytes == 0) return;
+    *rc = cuda_check(ctx, cudaMemcpyAsync(dst, src, bytes, kind, s), what);
+}
+
+// Waits for the work queued on s, so that no host buffer is released while a copy into it
+// is in flight, and returns the first failure: rc (a copy that failed to queue) before the
+// stream's own.
+inline int sync_copies(pxd_context* ctx, int rc, cudaStream_t s, const char* what) {
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (rc) return rc;
+    return cuda_check(ctx, e, what);
+}
+
 struct Staging {
     pxd_context* ctx;
     std::vector<void*> dev;

@@ -439,17 +439,22 @@ static int gbsa_system(pxd_context* ctx, int n, const std::vector<double>& x, co
     if (rc) return rc;
     double* d = static_cast<double*>(mem);
     GbArgs a{n, d, d + 3 * n, d + 4 * n, d + 5 * n, d + 6 * n, d + 7 * n};
-    cudaMemcpyAsync(d, x.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d + 3 * n, q.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d + 4 * n, radius.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d + 5 * n, screen.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
+    queue_copy(ctx, &rc, d, x.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream, "gbsa coordinates");
+    queue_copy(ctx, &rc, d + 3 * n, q.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream, "gbsa charges");
+    queue_copy(ctx, &rc, d + 4 * n, radius.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream,
+               "gbsa radii");
+    queue_copy(ctx, &rc, d + 5 * n, screen.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream,
+               "gbsa screening");
     const int threads = 128, blocks = (n + threads - 1) / threads;
-    gb_born_kernel<<<blocks, threads, 0, ctx->stream>>>(a);
-    gb_energy_kernel<<<blocks, threads, 0, ctx->stream>>>(a);
+    if (!rc) {
+        gb_born_kernel<<<blocks, threads, 0, ctx->stream>>>(a);
+        gb_energy_kernel<<<blocks, threads, 0, ctx->stream>>>(a);
+        rc = cuda_check(ctx, cudaGetLastError(), "gbsa kernels launch");
+    }
     std::vector<double> part(n);
-    cudaMemcpyAsync(part.data(), a.partial, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+    queue_copy(ctx, &rc, part.data(), a.partial, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream, "gbsa sums");
     cudaFreeAsync(mem, ctx->stream);
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "gbsa");
+    rc = sync_copies(ctx, rc, ctx->stream, "gbsa");
     if (rc) return rc;
     double s = 0.0;
     for (int i = 0; i < n; ++i) s += part[i];
@@ -626,18 +631,17 @@ int pxd_score(pxd_context* ctx, int32_t which, int32_t lig, int32_t n_poses, con
     float* d_x = reinterpret_cast<float*>(d_t + static_cast<size_t>(n_poses) * PXD_NUM_TERMS);
     float* d_r = d_x + nx;
     int* d_i = reinterpret_cast<int*>(d_r + nt + 1);
-    cudaMemcpyAsync(d_x, hx.data(), 4 * nx, cudaMemcpyHostToDevice, ctx->stream);
-    if (nt) cudaMemcpyAsync(d_r, ht.data(), 4 * nt, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(d_i, ids.data(), 4 * static_cast<size_t>(n_poses), cudaMemcpyHostToDevice, ctx->stream);
-    rc = pxd_score_dev(ctx, which, n_poses, N, d_i, d_x, d_r, d_s, d_t, ctx->stream);
+    queue_copy(ctx, &rc, d_x, hx.data(), 4 * nx, cudaMemcpyHostToDevice, ctx->stream, "score coordinates");
+    if (nt) queue_copy(ctx, &rc, d_r, ht.data(), 4 * nt, cudaMemcpyHostToDevice, ctx->stream, "score torsions");
+    queue_copy(ctx, &rc, d_i, ids.data(), 4 * static_cast<size_t>(n_poses), cudaMemcpyHostToDevice, ctx->stream,
+               "score ligand ids");
+    if (!rc) rc = pxd_score_dev(ctx, which, n_poses, N, d_i, d_x, d_r, d_s, d_t, ctx->stream);
     std::vector<double> ht2(static_cast<size_t>(n_poses) * PXD_NUM_TERMS);
-    if (!rc) {
-        cudaMemcpyAsync(score, d_s, 8 * static_cast<size_t>(n_poses), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(ht2.data(), d_t, 8 * ht2.size(), cudaMemcpyDeviceToHost, ctx->stream);
-    }
+    queue_copy(ctx, &rc, score, d_s, 8 * static_cast<size_t>(n_poses), cudaMemcpyDeviceToHost, ctx->stream,
+               "scores");
+    queue_copy(ctx, &rc, ht2.data(), d_t, 8 * ht2.size(), cudaMemcpyDeviceToHost, ctx->stream, "score terms");
     cudaFreeAsync(mem, ctx->stream);
-    if (rc) return rc;
-    rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "score");
+    rc = sync_copies(ctx, rc, ctx->stream, "score");
     if (rc) return rc;
     const double gcoef = ctx->sf_host[which].coef[PXD_TERM_GBSA];
     for (int p = 0; p < n_poses; ++p) {

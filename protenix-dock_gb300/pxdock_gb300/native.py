@@ -79,6 +79,7 @@ def load(auto_build=False):
                                         abi.i32p, abi.i32p, abi.f64p, abi.f64p, abi.f64p, abi.f64p,
                                         abi.f64p, abi.i32p, abi.i32p, abi.f64p]
     lib.pxd_rng_draws.argtypes = [vp, C.c_uint32, C.c_int32, abi.i32p, abi.i32p, abi.f64p]
+    lib.pxd_gather_bandwidth.argtypes = [C.c_int32, C.c_int64, C.c_int32, abi.f64p]
     lib.pxd_sf_weights.argtypes = [C.POINTER(abi.SfParams), abi.f64p]
     lib.pxd_sf_weights.restype = None
     lib.pxd_score_adjoint_dev.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32] + [vp] * 12
@@ -509,3 +510,14 @@ def mc_params(box_lo, box_hi, **kw):
         else:
             setattr(p, k, v)
     return p
+
+
+def gather_bandwidth(device=0, working_set_bytes=64 << 20, reps=10):
+    """pxd_gather_bandwidth: GB/s of random 16-byte gathers over a working set on `device`
+    (below the L2 size: the L2 gather roofline of the batched kernels)."""
+    lib = load()
+    out = np.zeros(1)
+    rc = lib.pxd_gather_bandwidth(device, working_set_bytes, reps, _p(out))
+    if rc != 0:
+        raise NativeError(rc, "gather bandwidth probe failed")
+    return float(out[0])

@@ -1,8 +1,9 @@
 """The FP64 port against the reference engine compiled from its own sources.
 
 Runs only where oracle/_ref/liboracle_ref.so could be built (the reference checkout is
-present); elsewhere the committed golden fixtures (tests/golden/ref_*.npz) carry the
-reference's answers instead (test_oracle_golden.py).
+present); elsewhere the committed fixture tests/golden/ref_answers.npz (written by
+tests/golden/make_ref_answers.py) carries the reference's answers instead, and
+test_oracle_golden.py replays them on the port.
 """
 import json
 import math
