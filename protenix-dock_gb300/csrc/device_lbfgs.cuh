@@ -28,8 +28,17 @@ struct Vecs {
 // history slab, the map gathers and the topology records.
 constexpr int kOptVecs = 8;
 
+// Physical L-BFGS history slots of a warp: the m kept (s, y) pairs and one spare that
+// receives the next pair before its curvature test decides whether it is kept, so the
+// pair is written once, in the pass that forms it.
+__host__ __device__ constexpr int hist_slots(int m) { return m + 1; }
+
+// Floats of the FP64 two-loop scalars after the vectors: ro per physical slot (m + 1
+// doubles) and al per kept pair (m doubles), rounded up to 16 bytes.
+__host__ __device__ constexpr int opt_scalar_floats(int m) { return (2 * (2 * m + 1) + 3) / 4 * 4; }
+
 // Carves the vectors from vb (kOptVecs * Dp floats) and the FP64 two-loop scalars ro, al
-// (2 * m doubles) after them.
+// (opt_scalar_floats(m) floats) after them.
 __device__ __forceinline__ Vecs carve_vecs(float* vb, int Dp, int m) {
     Vecs v;
     v.x = vb;
@@ -43,7 +52,7 @@ __device__ __forceinline__ Vecs carve_vecs(float* vb, int Dp, int m) {
     v.q = v.gprev;
     v.sv = v.gnew;
     v.ro = reinterpret_cast<double*>(vb + kOptVecs * Dp);
-    v.al = v.ro + m;
+    v.al = v.ro + hist_slots(m);
     v.S = v.Y = nullptr;
     return v;
 }
@@ -124,26 +133,27 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
         return;
     }
     double t_prev = 0.0, f_prev = f, gtd_prev = gtd;
-    vcopy(g_prev, g, D, lane);
-    bool done = false;
+    // the previous trial's gradient: g itself until the first interpolation step
+    const float* gpv = g;
     int ls_iter = 0;
     while (ls_iter < p.ls_max) {
         if ((f_new > f + p.c1 * t * gtd) || (ls_iter > 1 && f_new >= f_prev)) {
             B.br0 = t_prev; B.br1 = t; B.bf0 = f_prev; B.bf1 = f_new;
-            vcopy(B.bg0, g_prev, D, lane);
+            vcopy(B.bg0, gpv, D, lane);
             vcopy(B.bg1, g_new, D, lane);
             B.bgtd0 = gtd_prev; B.bgtd1 = gtd_new;
             break;
         }
         if (fabs(gtd_new) <= -p.c2 * gtd) {
-            B.br0 = t; B.bf0 = f_new;
-            vcopy(B.bg0, g_new, D, lane);
-            done = true;
-            break;
+            // strong Wolfe holds at this trial: it is the accepted step
+            t_io = t;
+            f_io = f_new;
+            vcopy(g, g_new, D, lane);
+            return;
         }
         if (gtd_new >= 0.0) {
             B.br0 = t_prev; B.br1 = t; B.bf0 = f_prev; B.bf1 = f_new;
-            vcopy(B.bg0, g_prev, D, lane);
+            vcopy(B.bg0, gpv, D, lane);
             vcopy(B.bg1, g_new, D, lane);
             B.bgtd0 = gtd_prev; B.bgtd1 = gtd_new;
             break;
@@ -155,6 +165,7 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
         t_prev = tmp;
         f_prev = f_new;
         vcopy(g_prev, g_new, D, lane);
+        gpv = g_prev;
         gtd_prev = gtd_new;
         f_new = closure_eval(c, t, d, g_new);
         gtd_new = vdot(g_new, d, D, lane);
@@ -168,9 +179,9 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
     } else {
         d_norm = vabsmax(d, D, lane);
     }
-    bool insuf = false;
+    bool insuf = false, done = false;
     int lo = 0, hi = 1;
-    if (!done && B.bf0 > B.bf1) {
+    if (B.bf0 > B.bf1) {
         lo = 1;
         hi = 0;
     }
@@ -235,10 +246,32 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
     vcopy(g, B.bg(lo), D, lane);
 }
 
+// One step of a compensated dot product: the body of vdot, so that a dot accumulated
+// inside another pass gives vdot's result bit for bit.
+__device__ __forceinline__ void ds_dot_acc(DS& acc, float x, float y) {
+    const float p = x * y;
+    const float pe = fmaf(x, y, -p);
+    ds_add(acc, p);
+    acc.lo += pe;
+}
+
 // lbfgs_step::apply (optimizer.cpp:429-560) on the pose held in v.x; returns status.
+//
+// The vector work of an iteration runs in fused passes over the warp's elements, each
+// lane touching only its own elements (e = lane + 32 k), with the arithmetic of every
+// element as in the textbook order, so the iterates are those of separate passes:
+//   - the history update: y = g - g_prev and s = t d go straight into the spare history
+//     slot, with max|y|, y.s and y.y in the same pass;
+//   - the first loop: q -= al_k y_k fused with the next pair's s_{k-1} . q, then
+//     d = H_diag q with y_0 . d;
+//   - the second loop: d += (al_k - be_k) s_k fused with the next y_{k+1} . d, the last
+//     step with g . d for the line search.
+// Kept pairs sit in physical slots (base + j) % (m + 1), j = 0 .. count - 1 oldest first;
+// the spare slot (base + count) % (m + 1) receives the next pair.
 static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v, int D,
                           size_t Dp, int lane, double& energy) {
     const int m = p.m;
+    const int slots = hist_slots(m);
     const int max_eval = p.max_eval > 0 ? p.max_eval : p.max_iter * 5 / 4;
     c.x0 = v.x;
     c.nevals = 0;
@@ -246,74 +279,125 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
     energy = loss;
     if (vabsmax(v.g, D, lane) < p.tol_grad) return PXD_POSE_CONVERGED;
     int status = PXD_POSE_NOT_CONVERGED;
-    int head = 0, count = 0;
+    int base = 0, count = 0;
     double H_diag = 1.0, t = 0.0, prev_loss;
     int n_iter = 0;
-    bool updated = false, high = false;
+    bool updated = false;
     while (n_iter < p.max_iter && c.nevals < max_eval) {
         ++n_iter;
-        if (n_iter > 1) {
-            for (int e = lane; e < D; e += kWarp) v.q[e] = v.g[e] - v.gp[e];  // y
-            __syncwarp();
-            high = vabsmax(v.q, D, lane) > p.reset;
-        }
-        if (n_iter == 1 || high) {
-            for (int e = lane; e < D; e += kWarp) v.d[e] = -v.g[e];
-            __syncwarp();
-            head = count = 0;
-            H_diag = 1.0;
-        } else {
+        bool reset = n_iter == 1;
+        if (!reset) {
+            const int spare = (base + count) % slots;
+            float* ys_ = v.Y + spare * Dp;
+            float* ss_ = v.S + spare * Dp;
             const float tf = static_cast<float>(t);
-            for (int e = lane; e < D; e += kWarp) v.sv[e] = v.d[e] * tf;
-            __syncwarp();
-            const double ys = vdot(v.q, v.sv, D, lane);
-            if (ys > 1e-10) {
-                int slot;
-                if (count == m) {
-                    slot = head;
-                    head = (head + 1) % m;
-                } else {
-                    slot = (head + count) % m;
-                    ++count;
-                }
-                H_diag = ys / vdot(v.q, v.q, D, lane);
-                vcopy(v.Y + slot * Dp, v.q, D, lane);
-                vcopy(v.S + slot * Dp, v.sv, D, lane);
-                if (lane == 0) v.ro[slot] = 1.0 / ys;
-                __syncwarp();
+            float ymax = 0.f;
+            DS a_ys{0.f, 0.f}, a_yy{0.f, 0.f};
+            for (int e = lane; e < D; e += kWarp) {
+                const float y = v.g[e] - v.gp[e];
+                const float sv = v.d[e] * tf;
+                ys_[e] = y;
+                ss_[e] = sv;
+                ymax = fmaxf(ymax, fabsf(y));
+                ds_dot_acc(a_ys, y, sv);
+                ds_dot_acc(a_yy, y, y);
             }
-            for (int e = lane; e < D; e += kWarp) v.q[e] = -v.g[e];
+            reset = warp_max(ymax) > p.reset;
+            if (!reset) {
+                const double ys = ds_warp_sum(a_ys);
+                const double yy = ds_warp_sum(a_yy);
+                if (ys > 1e-10) {
+                    if (count == m)
+                        base = (base + 1) % slots;  // the oldest slot becomes the spare
+                    else
+                        ++count;
+                    H_diag = ys / yy;
+                    if (lane == 0) v.ro[spare] = 1.0 / ys;
+                }
+            }
             __syncwarp();
-            for (int k = count - 1; k > -1; --k) {
-                const int slot = (head + k) % m;
-                const double al = vdot(v.S + slot * Dp, v.q, D, lane) * v.ro[slot];
-                if (lane == 0) v.al[k] = al;
-                const float nal = static_cast<float>(-al);
-                const float* yy = v.Y + slot * Dp;
-                for (int e = lane; e < D; e += kWarp) v.q[e] = fmaf(yy[e], nal, v.q[e]);
-                __syncwarp();
+        }
+        double gtd;
+        if (reset || count == 0) {
+            // d = -H_diag g (H_diag = 1 after a reset), g_prev = g, g . d and |g|_1
+            if (reset) {
+                base = count = 0;
+                H_diag = 1.0;
             }
             const float hd = static_cast<float>(H_diag);
-            for (int e = lane; e < D; e += kWarp) v.d[e] = v.q[e] * hd;
+            DS acc{0.f, 0.f}, a_abs{0.f, 0.f};
+            for (int e = lane; e < D; e += kWarp) {
+                const float ge = v.g[e];
+                const float de = reset ? -ge : (-ge) * hd;
+                v.d[e] = de;
+                v.gp[e] = ge;
+                ds_dot_acc(acc, ge, de);
+                ds_add(a_abs, fabsf(ge));
+            }
             __syncwarp();
-            for (int k = 0; k < count; ++k) {
-                const int slot = (head + k) % m;
-                const double be = vdot(v.Y + slot * Dp, v.d, D, lane) * v.ro[slot];
-                const float w = static_cast<float>(v.al[k] - be);
-                const float* ss = v.S + slot * Dp;
-                for (int e = lane; e < D; e += kWarp) v.d[e] = fmaf(ss[e], w, v.d[e]);
+            gtd = ds_warp_sum(acc);
+            if (reset) {
+                const double inv = 1.0 / ds_warp_sum(a_abs);
+                t = fmin(1.0, inv) * p.lr * 0.1;
+            } else {
+                t = p.lr;
+            }
+        } else {
+            // first loop, newest to oldest: q = -g - sum al_k y_k
+            DS acc{0.f, 0.f};
+            {
+                const float* sk = v.S + ((base + count - 1) % slots) * Dp;
+                for (int e = lane; e < D; e += kWarp) {
+                    const float ge = v.g[e];
+                    v.q[e] = -ge;
+                    v.gp[e] = ge;
+                    ds_dot_acc(acc, sk[e], -ge);
+                }
+            }
+            for (int k = count - 1; k >= 0; --k) {
+                const int sl = (base + k) % slots;
+                const double al = ds_warp_sum(acc) * v.ro[sl];
+                if (lane == 0) v.al[k] = al;
+                const float nal = static_cast<float>(-al);
+                const float* yk = v.Y + sl * Dp;
+                acc = DS{0.f, 0.f};
+                if (k > 0) {
+                    const float* sn = v.S + ((base + k - 1) % slots) * Dp;
+                    for (int e = lane; e < D; e += kWarp) {
+                        const float qe = fmaf(yk[e], nal, v.q[e]);
+                        v.q[e] = qe;
+                        ds_dot_acc(acc, sn[e], qe);
+                    }
+                } else {
+                    // the last update, then d = H_diag q and the second loop's first dot
+                    const float hd = static_cast<float>(H_diag);
+                    for (int e = lane; e < D; e += kWarp) {
+                        const float de = fmaf(yk[e], nal, v.q[e]) * hd;
+                        v.d[e] = de;
+                        ds_dot_acc(acc, yk[e], de);
+                    }
+                }
                 __syncwarp();
             }
-        }
-        vcopy(v.gp, v.g, D, lane);
-        prev_loss = loss;
-        if (n_iter == 1 || high) {
-            const double inv = 1.0 / vabssum(v.g, D, lane);
-            t = fmin(1.0, inv) * p.lr * 0.1;
-        } else {
+            // second loop, oldest to newest: d += (al_k - be_k) s_k
+            for (int k = 0; k < count; ++k) {
+                const int sl = (base + k) % slots;
+                const double be = ds_warp_sum(acc) * v.ro[sl];
+                const float w = static_cast<float>(v.al[k] - be);
+                const float* sk = v.S + sl * Dp;
+                const float* nx = k + 1 < count ? v.Y + ((base + k + 1) % slots) * Dp : v.g;
+                acc = DS{0.f, 0.f};
+                for (int e = lane; e < D; e += kWarp) {
+                    const float de = fmaf(sk[e], w, v.d[e]);
+                    v.d[e] = de;
+                    ds_dot_acc(acc, nx[e], de);
+                }
+                __syncwarp();
+            }
+            gtd = ds_warp_sum(acc);  // g . d after the last step
             t = p.lr;
         }
-        const double gtd = vdot(v.g, v.d, D, lane);
+        prev_loss = loss;
         if (gtd > -p.tol_change) {
             status = PXD_POSE_CONVERGED;
             break;
@@ -324,16 +408,21 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
             status = PXD_POSE_NAN;
             break;
         }
+        // x += t d, with max|g| and max|t d| for the convergence tests
         const float tf = static_cast<float>(t);
-        for (int e = lane; e < D; e += kWarp) v.x[e] = fmaf(v.d[e], tf, v.x[e]);
+        float gmax = 0.f, smax = 0.f;
+        for (int e = lane; e < D; e += kWarp) {
+            const float de = v.d[e];
+            v.x[e] = fmaf(de, tf, v.x[e]);
+            gmax = fmaxf(gmax, fabsf(v.g[e]));
+            smax = fmaxf(smax, fabsf(de * tf));
+        }
         __syncwarp();
         updated = true;
-        if (vabsmax(v.g, D, lane) <= p.tol_grad) {
+        if (warp_max(gmax) <= p.tol_grad) {
             status = PXD_POSE_CONVERGED;
             break;
         }
-        float smax = 0.f;
-        for (int e = lane; e < D; e += kWarp) smax = fmaxf(smax, fabsf(v.d[e] * tf));
         if (warp_max(smax) <= p.tol_change) {
             status = PXD_POSE_CONVERGED;
             break;

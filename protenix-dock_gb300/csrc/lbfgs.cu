@@ -44,15 +44,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
     const int Dp = a.D_pad;
-    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + kOptVecs * Dp + 4 * a.c.m +
-                         (a.hist_smem ? 2 * a.c.m * Dp : 0);
+    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + kOptVecs * Dp + opt_scalar_floats(a.c.m) +
+                         (a.hist_smem ? 2 * hist_slots(a.c.m) * Dp : 0);
     float* base = smem + wib * per_warp;
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
     Vecs v = carve_vecs(vb, Dp, a.c.m);
     const size_t gw = static_cast<size_t>(blockIdx.x) * kWarpsPerBlock + wib;
-    v.S = a.hist_smem ? vb + kOptVecs * Dp + 4 * a.c.m : a.hist + gw * a.hist_stride;
-    v.Y = v.S + static_cast<size_t>(a.c.m) * Dp;
+    v.S = a.hist_smem ? vb + kOptVecs * Dp + opt_scalar_floats(a.c.m) : a.hist + gw * a.hist_stride;
+    v.Y = v.S + static_cast<size_t>(hist_slots(a.c.m)) * Dp;
     const int R = a.env.rec.n_rotors;
     Closure c;
     c.env = &a.env;
@@ -191,8 +191,8 @@ static LbfgsKernelFn lbfgs_variant(const pxd_context* ctx, int cap) {
 // Dynamic shared memory of one lbfgs_kernel block for ligands of up to `cap` atoms.
 static size_t lbfgs_block_smem(const pxd_context* ctx, int cap, int history, bool hist_smem) {
     const int dp = padded(3 * cap + ctx->rec.n_rotors);
-    const int per_warp = pose_bufs_floats(cap, ctx->rec.n_local) + kOptVecs * dp + 4 * history +
-                         (hist_smem ? 2 * history * dp : 0);
+    const int per_warp = pose_bufs_floats(cap, ctx->rec.n_local) + kOptVecs * dp + opt_scalar_floats(history) +
+                         (hist_smem ? 2 * hist_slots(history) * dp : 0);
     return sizeof(float) * kWarpsPerBlock * per_warp;
 }
 
@@ -459,7 +459,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
             q.hist_smem = 0;
         q.dp = padded(3 * cap + ctx->rec.n_rotors);
         q.smem = lbfgs_block_smem(ctx, cap, p.history, q.hist_smem);
-        q.stride = q.hist_smem ? 0 : static_cast<size_t>(2) * p.history * q.dp;
+        q.stride = q.hist_smem ? 0 : static_cast<size_t>(2) * hist_slots(p.history) * q.dp;
         plan.push_back(q);
     }
     // classes may share a kernel variant with different slices: its dynamic shared-memory
@@ -597,7 +597,7 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
                     "lbfgs occupancy");
     if (rc) return rc;
     if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
-    a.hist_stride = static_cast<size_t>(2) * p.history * a.D_pad;
+    a.hist_stride = static_cast<size_t>(2) * hist_slots(p.history) * a.D_pad;
     const size_t block_bytes = sizeof(float) * a.hist_stride * kWarpsPerBlock;
     const size_t fit = (kStaticScratchBytes - kStaticCounterBytes) / block_bytes;
     if (fit < 1)

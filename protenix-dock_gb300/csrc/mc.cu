@@ -144,7 +144,7 @@ struct McArgs {
 };
 
 __host__ __device__ inline int mc_warp_floats(int max_atoms, int n_local, int Dp, int m) {
-    return pose_bufs_floats(max_atoms, n_local) + kOptVecs * Dp + 4 * m + 2 * Dp + 4 * max_atoms +
+    return pose_bufs_floats(max_atoms, n_local) + kOptVecs * Dp + opt_scalar_floats(m) + 2 * Dp + 4 * max_atoms +
            static_cast<int>(sizeof(KinShared) / sizeof(float)) + 64 + 16;
 }
 
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
     Vecs v = carve_vecs(vb, Dp, m);
-    float* best_x = vb + kOptVecs * Dp + 4 * m;
+    float* best_x = vb + kOptVecs * Dp + opt_scalar_floats(m);
     float* tmp_x = best_x + Dp;
     float4* kc = reinterpret_cast<float4*>(tmp_x + Dp);
     KinShared& ks = *reinterpret_cast<KinShared*>(kc + a.max_atoms);
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     double* bc = reinterpret_cast<double*>(tq + 64);         // [8] broadcast slots
     const size_t gw = static_cast<size_t>(blockIdx.x) * a.warps_per_block + wib;
     v.S = a.hist + gw * a.hist_stride;
-    v.Y = v.S + static_cast<size_t>(m) * Dp;
+    v.Y = v.S + static_cast<size_t>(hist_slots(m)) * Dp;
     MtState* rng = a.rng + gw;
     const int R = a.env.rec.n_rotors;
     Closure c;
@@ -592,7 +592,7 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     const int need = (n_walkers + wpb - 1) / wpb;
     if (blocks > need) blocks = need;
     const size_t warps = static_cast<size_t>(blocks) * wpb;
-    a.hist_stride = static_cast<size_t>(2) * p->lbfgs.history * a.D_pad;
+    a.hist_stride = static_cast<size_t>(2) * hist_slots(p->lbfgs.history) * a.D_pad;
     const size_t hist_bytes = sizeof(float) * a.hist_stride * warps;
     const size_t rng_off = (hist_bytes + 255) / 256 * 256;
     rc = ensure_scratch(ctx, rng_off + sizeof(MtState) * warps);
