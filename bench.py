@@ -9,6 +9,10 @@ tolerance 1e-3 (the other constants as the reference optimiser).
 A step is one batched L-BFGS pass over all 65,536 poses. Start poses are restored and
 L2 is flushed (a 256 MiB write) between steps, outside the timed kernel.
 
+With --gpus N (N > 1), one process per GPU -- launched by torchrun, or spawned here when
+no launcher set WORLD_SIZE -- each optimises a cost-balanced share (pxdock_gb300.shard) of
+one set of N x 65,536 starts (weak scaling); the time is the maximum over ranks.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 --impl reference times the reference algorithm on the host cores (the FP64 C port of the
@@ -53,7 +57,7 @@ def workload(seed_poses=2, n_poses=N_POSES):
     return rec, lig, box, poses
 
 
-def config_dict(lig, box):
+def config_dict(lig, box, world=1):
     return {
         "workload": "batched L-BFGS pose optimisation: 1 ligand (%d atoms, %d torsions) x %d "
                     "poses, %dx%dx%d FP32 maps (%.0f A box @ %.3f A), m=%d, max_iter=%d, "
@@ -64,7 +68,9 @@ def config_dict(lig, box):
         "ligand_atoms": lig.n_atoms,
         "grid_points": int(np.prod(list(box.npoints))),
         "l2": "flushed between steps (256 MiB write); inputs ~100 MB < L2",
-        "parallelism": "replicas",
+        "parallelism": "replicas" if world == 1 else
+                       "replicas x%d: one process per GPU, each a cost-balanced share of one set of "
+                       "%d x %d starts, no collective on the data path" % (world, world, N_POSES),
     }
 
 
@@ -910,6 +916,27 @@ def run_evaluate(args):
     return 0
 
 
+def free_port():
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def spawn_ranks(n):
+    """--gpus N without an outer launcher: runs N ranks of this command, one per GPU, with
+    the torch.distributed environment a launcher would set (rendezvous on 127.0.0.1).
+    Rank 0 prints the JSON line; the exit status is the worst rank's."""
+    port = free_port()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), WORLD_SIZE=str(n), LOCAL_RANK=str(r), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + sys.argv[1:], env=env))
+    return max(p.wait() for p in procs)
+
+
 def main():
     global N_POSES
     ap = argparse.ArgumentParser()
@@ -933,6 +960,8 @@ def main():
                     help="poses per step (smaller only for profiling captures)")
     args = ap.parse_args()
     N_POSES = args.poses
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_ranks(args.gpus)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "screening":
@@ -966,7 +995,17 @@ def main():
 
         dist.init_process_group("nccl")
     native.load(auto_build=True)
-    rec, lig, box, poses = workload(seed_poses=2 + rank)
+    if world > 1:
+        # weak scaling over one workload: N x 65,536 starts (seed 2) in blocks of 65,536,
+        # split by the cost-balanced partition that every rank computes alike
+        from pxdock_gb300 import shard
+
+        rec, lig, box, all_poses = workload(seed_poses=2, n_poses=N_POSES * world)
+        mine = shard.rank_share([float(N_POSES)] * world, rank, world)
+        poses = np.concatenate([all_poses[b * N_POSES:(b + 1) * N_POSES] for b in mine])
+        del all_poses
+    else:
+        rec, lig, box, poses = workload(seed_poses=2)
     ctx = native.Context(local)
     ctx.set_receptor(rec)
     ctx.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)))
@@ -1030,7 +1069,12 @@ def main():
         t1 = time.perf_counter()
         out = ctx.lbfgs(p, lid, poses)
         e2e_times.append(time.perf_counter() - t1)
-    e2e_value = world * N_POSES / float(np.mean(e2e_times))
+    t_e2e = float(np.mean(e2e_times))
+    if dist:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = world * N_POSES / t_e2e
     # plain per-pose path: one call per pose
     n_plain = 64
     t1 = time.perf_counter()
@@ -1050,7 +1094,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": float(np.mean(kernel_ms)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": config_dict(lig, box),
+        "config": config_dict(lig, box, world),
         "e2e": {"value": e2e_value, "unit": UNIT,
                 # pxd_lbfgs copies the caller's FP64 coordinates both ways (narrowed to FP32
                 # on the device) and returns energy (FP64), evaluations and status per pose

@@ -13,8 +13,15 @@ walker (search) of every ligand in the index. Differences a caller can see:
     {E, dE/dx, dE/dy, dE/dz} file per map); the reference's Boost archives are not
     readable here;
   - output files are written in index-file order;
-  - the extra keyword `device` (default 0) picks the CUDA device.
+  - the extra keyword `device` (default 0) picks the CUDA device;
+  - optimize and search take the extra keywords `rank` and `world` (default 0 and 1, the
+    reference's single process): with world > 1, the call processes only this rank's
+    cost-balanced share of the index (pxdock_gb300.shard), so that one process per GPU
+    covers the index with every output file written once.
 """
+import os
+import tempfile
+
 import ctypes as C
 
 import numpy as np
@@ -109,13 +116,35 @@ class ReusableEngine:
         """The reference names this argument output_dir; it is the CSV file written."""
         self._call(self._lib.pxd_engine_evaluate, _b(ligand_index_file), _b(output_dir))
 
-    def optimize(self, ligand_index_file, output_dir, max_niters=240, slope=1e6):
-        self._call(self._lib.pxd_engine_optimize, _b(ligand_index_file), _b(output_dir), max_niters, slope)
+    def _sharded(self, ligand_index_file, rank, world, walkers, run):
+        """Runs run(index_file) on this rank's share of the index (world > 1) or on the
+        whole index (world == 1, the reference's behaviour)."""
+        if world == 1 and rank == 0:
+            return run(ligand_index_file)
+        if world < 1 or not 0 <= rank < world:
+            raise RuntimeError("rank %d outside a world of %d" % (rank, world))
+        from pxdock_gb300 import shard
+
+        fd, path = tempfile.mkstemp(prefix="pxd_rank%d_" % rank, suffix=".txt")
+        os.close(fd)
+        try:
+            if shard.rank_index(ligand_index_file, rank, world, path, walkers) > 0:
+                run(path)
+        finally:
+            os.unlink(path)
+
+    def optimize(self, ligand_index_file, output_dir, max_niters=240, slope=1e6, rank=0, world=1):
+        self._sharded(ligand_index_file, rank, world, None,
+                      lambda idx: self._call(self._lib.pxd_engine_optimize, _b(idx), _b(output_dir),
+                                             max_niters, slope))
 
     def search(self, ligand_index_file, output_dir, seed=0, exhaustiveness=256, max_nsteps=200,
-               relax_nsteps=40, num_modes=8, min_rmsd=0.5, mc_mmenergy_threshold=-1., slope=1e6):
-        self._call(self._lib.pxd_engine_search, _b(ligand_index_file), _b(output_dir), seed, exhaustiveness,
-                   max_nsteps, relax_nsteps, num_modes, min_rmsd, mc_mmenergy_threshold, slope)
+               relax_nsteps=40, num_modes=8, min_rmsd=0.5, mc_mmenergy_threshold=-1., slope=1e6, rank=0,
+               world=1):
+        self._sharded(ligand_index_file, rank, world, exhaustiveness,
+                      lambda idx: self._call(self._lib.pxd_engine_search, _b(idx), _b(output_dir), seed,
+                                             exhaustiveness, max_nsteps, relax_nsteps, num_modes, min_rmsd,
+                                             mc_mmenergy_threshold, slope))
 
 
 # ----------------------------------------------------- the engine's host-only parts

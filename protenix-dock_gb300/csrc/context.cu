@@ -163,6 +163,7 @@ bool topo_indices_ok(const TopoIn& t) {
 struct TopoOffsets {
     int n_bond_slots, n_angle_slots, n_dih_slots, n_pair_slots;
     size_t bond_ij, bond_p, angle_ijk, angle_p, dih_ijkl, dih_terms, dih_term, pair_ij, pair_p;
+    size_t bond_p64, angle_p64, dih_term64, pair_p64;
 };
 
 TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
@@ -171,45 +172,54 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
         auto order = schedule_rounds<2>(t.bonds, t.n_atoms);
         std::vector<int2> ij;
         std::vector<float2> p;
+        std::vector<double2> p64;
         for (int s : order) {
             if (s < 0) {
                 ij.push_back(make_int2(-1, -1));
                 p.push_back(make_float2(0.f, 0.f));
+                p64.push_back(make_double2(0.0, 0.0));
             } else {
                 const auto a = slot_atoms<2>(t.bonds, s);
                 const int b = s & ~kReversed;
                 ij.push_back(make_int2(a[0], a[1]));
                 p.push_back(make_float2(static_cast<float>(t.bond_k[b]), static_cast<float>(t.bond_r0[b])));
+                p64.push_back(make_double2(t.bond_k[b], t.bond_r0[b]));
             }
         }
         o.n_bond_slots = static_cast<int>(order.size());
         o.bond_ij = pk.put(ij);
         o.bond_p = pk.put(p);
+        o.bond_p64 = pk.put(p64);
     }
     {
         auto order = schedule_rounds<3>(t.angles, t.n_atoms);
         std::vector<int4> ijk;
         std::vector<float2> p;
+        std::vector<double2> p64;
         for (int s : order) {
             if (s < 0) {
                 ijk.push_back(make_int4(-1, -1, -1, -1));
                 p.push_back(make_float2(0.f, 0.f));
+                p64.push_back(make_double2(0.0, 0.0));
             } else {
                 const auto a = slot_atoms<3>(t.angles, s);
                 const int b = s & ~kReversed;
                 ijk.push_back(make_int4(a[0], a[1], a[2], 0));
                 p.push_back(make_float2(static_cast<float>(t.angle_k[b]), static_cast<float>(t.angle_t0[b])));
+                p64.push_back(make_double2(t.angle_k[b], t.angle_t0[b]));
             }
         }
         o.n_angle_slots = static_cast<int>(order.size());
         o.angle_ijk = pk.put(ijk);
         o.angle_p = pk.put(p);
+        o.angle_p64 = pk.put(p64);
     }
     {
         auto order = schedule_rounds<4>(t.dih, t.n_atoms);
         std::vector<int4> ijkl;
         std::vector<int2> tr;
         std::vector<float4> terms;
+        std::vector<double4> terms64;
         for (int s : order) {
             if (s < 0) {
                 ijkl.push_back(make_int4(-1, -1, -1, -1));
@@ -219,24 +229,29 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
                 const int b = s & ~kReversed;
                 ijkl.push_back(make_int4(a[0], a[1], a[2], a[3]));
                 tr.push_back(make_int2(static_cast<int>(terms.size()), static_cast<int>(t.dih_terms[b].size())));
-                for (auto& u : t.dih_terms[b])
+                for (auto& u : t.dih_terms[b]) {
                     terms.push_back(make_float4(static_cast<float>(u[0]), static_cast<float>(u[1]),
                                                 static_cast<float>(u[2]), 0.f));
+                    terms64.push_back(make_double4(u[0], u[1], u[2], 0.0));
+                }
             }
         }
         o.n_dih_slots = static_cast<int>(order.size());
         o.dih_ijkl = pk.put(ijkl);
         o.dih_terms = pk.put(tr);
         o.dih_term = pk.put(terms);
+        o.dih_term64 = pk.put(terms64);
     }
     {
         auto order = schedule_rounds<2>(t.pairs, t.n_atoms);
         std::vector<int2> ij;
         std::vector<float4> p;
+        std::vector<double4> p64;
         for (int s : order) {
             if (s < 0) {
                 ij.push_back(make_int2(-1, -1));
                 p.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+                p64.push_back(make_double4(0.0, 0.0, 0.0, 0.0));
                 continue;
             }
             const auto a = slot_atoms<2>(t.pairs, s);
@@ -248,10 +263,12 @@ TopoOffsets pack_topo(Packer& pk, const TopoIn& t) {
             ij.push_back(make_int2(i, j));
             p.push_back(make_float4(static_cast<float>(A), static_cast<float>(C),
                                     static_cast<float>(sm * sm), 0.f));
+            p64.push_back(make_double4(A, C, sm * sm, 0.0));
         }
         o.n_pair_slots = static_cast<int>(order.size());
         o.pair_ij = pk.put(ij);
         o.pair_p = pk.put(p);
+        o.pair_p64 = pk.put(p64);
     }
     return o;
 }
@@ -272,6 +289,10 @@ DevTopo topo_pointers(void* base, int n_atoms, const TopoOffsets& o) {
     d.dih_term = at<float4>(base, o.dih_term);
     d.pair_ij = at<int2>(base, o.pair_ij);
     d.pair_p = at<float4>(base, o.pair_p);
+    d.bond_p64 = at<double2>(base, o.bond_p64);
+    d.angle_p64 = at<double2>(base, o.angle_p64);
+    d.dih_term64 = at<double4>(base, o.dih_term64);
+    d.pair_p64 = at<double4>(base, o.pair_p64);
     return d;
 }
 
@@ -360,7 +381,12 @@ int upload_explicit(pxd_context* ctx, const std::vector<int>& atoms, const std::
     std::vector<float4> xq;
     std::vector<float2> se;
     std::vector<int> loc;
+    std::vector<double4> xq64;
+    std::vector<double2> se64;
     for (int a : atoms) {
+        xq64.push_back(make_double4(ctx->rec_xyz[3 * a], ctx->rec_xyz[3 * a + 1], ctx->rec_xyz[3 * a + 2],
+                                    ctx->rec_charge[a]));
+        se64.push_back(make_double2(ctx->rec_sigma[a], ctx->rec_epsilon[a]));
         xq.push_back(make_float4(static_cast<float>(ctx->rec_xyz[3 * a]),
                                  static_cast<float>(ctx->rec_xyz[3 * a + 1]),
                                  static_cast<float>(ctx->rec_xyz[3 * a + 2]),
@@ -372,6 +398,8 @@ int upload_explicit(pxd_context* ctx, const std::vector<int>& atoms, const std::
     offs[0] = pk.put(xq);
     offs[1] = pk.put(se);
     offs[2] = pk.put(loc);
+    offs[3] = pk.put(xq64);
+    offs[4] = pk.put(se64);
     int rc = cuda_check(ctx, cudaMalloc(mem, pk.bytes.size()), "receptor explicit list");
     if (rc) return rc;
     return cuda_check(ctx, cudaMemcpy(*mem, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice),
@@ -386,6 +414,8 @@ void point_explicit(pxd_context* ctx, bool with_maps) {
     ctx->rec.ex_xyzq = at<float4>(mem, o[0]);
     ctx->rec.ex_se = at<float2>(mem, o[1]);
     ctx->rec.ex_local = at<int>(mem, o[2]);
+    ctx->rec.ex_xyzq64 = at<double4>(mem, o[3]);
+    ctx->rec.ex_se64 = at<double2>(mem, o[4]);
 }
 
 int sync_ligand_table(pxd_context* ctx) {
@@ -613,7 +643,12 @@ int pxd_set_receptor(pxd_context* ctx, const pxd_receptor_desc* r) {
     const double e_const = constant_intra_energy(full, ctx->rec_xyz, ctx->is_mov);
     Packer pk;
     std::vector<float4> origin, axis, local_xyz0;
+    std::vector<double4> origin64, axis64, local64;
     for (int k = 0; k < r->n_rotors; ++k) {
+        origin64.push_back(make_double4(ctx->rotor_origin[3 * k], ctx->rotor_origin[3 * k + 1],
+                                        ctx->rotor_origin[3 * k + 2], 0.0));
+        axis64.push_back(make_double4(ctx->rotor_axis[3 * k], ctx->rotor_axis[3 * k + 1], ctx->rotor_axis[3 * k + 2],
+                                      0.0));
         origin.push_back(make_float4(static_cast<float>(ctx->rotor_origin[3 * k]),
                                      static_cast<float>(ctx->rotor_origin[3 * k + 1]),
                                      static_cast<float>(ctx->rotor_origin[3 * k + 2]), 0.f));
@@ -625,12 +660,17 @@ int pxd_set_receptor(pxd_context* ctx, const pxd_receptor_desc* r) {
         const int a = locals[l];
         if (l < n_mov) {
             const int k = ctx->mov_rotor[l];
+            local64.push_back(make_double4(ctx->rec_xyz[3 * a] - ctx->rotor_origin[3 * k],
+                                           ctx->rec_xyz[3 * a + 1] - ctx->rotor_origin[3 * k + 1],
+                                           ctx->rec_xyz[3 * a + 2] - ctx->rotor_origin[3 * k + 2], k));
             local_xyz0.push_back(make_float4(
                 static_cast<float>(ctx->rec_xyz[3 * a] - ctx->rotor_origin[3 * k]),
                 static_cast<float>(ctx->rec_xyz[3 * a + 1] - ctx->rotor_origin[3 * k + 1]),
                 static_cast<float>(ctx->rec_xyz[3 * a + 2] - ctx->rotor_origin[3 * k + 2]),
                 bits_as_float(k)));
         } else {
+            local64.push_back(make_double4(ctx->rec_xyz[3 * a], ctx->rec_xyz[3 * a + 1], ctx->rec_xyz[3 * a + 2],
+                                           -1.0));
             local_xyz0.push_back(make_float4(static_cast<float>(ctx->rec_xyz[3 * a]),
                                              static_cast<float>(ctx->rec_xyz[3 * a + 1]),
                                              static_cast<float>(ctx->rec_xyz[3 * a + 2]), 0.f));
@@ -640,6 +680,7 @@ int pxd_set_receptor(pxd_context* ctx, const pxd_receptor_desc* r) {
     const size_t o_axis = pk.put(axis);
     const size_t o_rmov = pk.put(ctx->rotor_mov_off);
     const size_t o_local = pk.put(local_xyz0);
+    const size_t o_origin64 = pk.put(origin64), o_axis64 = pk.put(axis64), o_local64 = pk.put(local64);
     TopoOffsets to = pack_topo(pk, sub);
     int rc = cuda_check(ctx, cudaMalloc(&ctx->rec_mem, pk.bytes.size()), "receptor allocation");
     if (rc) return rc;
@@ -654,6 +695,9 @@ int pxd_set_receptor(pxd_context* ctx, const pxd_receptor_desc* r) {
     d.rotor_axis = at<float4>(ctx->rec_mem, o_axis);
     d.rotor_mov = at<int>(ctx->rec_mem, o_rmov);
     d.local_xyz0 = at<float4>(ctx->rec_mem, o_local);
+    d.rotor_origin64 = at<double4>(ctx->rec_mem, o_origin64);
+    d.rotor_axis64 = at<double4>(ctx->rec_mem, o_axis64);
+    d.local_xyz064 = at<double4>(ctx->rec_mem, o_local64);
     d.intra = topo_pointers(ctx->rec_mem, n_local, to);
     d.e_const = e_const;
     // explicit pair lists: every atom (no maps) and the rotor atoms (maps present)
@@ -700,7 +744,9 @@ static int alloc_maps(pxd_context* ctx, const pxd_box* box, const std::vector<in
     ctx->n_slots = 1 + static_cast<int>(types.size());
     for (int t = 0; t < PXD_NUM_VDW_TYPES; ++t) ctx->type_slot[t] = -1;
     for (size_t k = 0; k < types.size(); ++k) ctx->type_slot[types[k]] = 1 + static_cast<int>(k);
-    int rc = cuda_check(ctx, cudaMalloc(&ctx->maps, sizeof(float4) * P * ctx->n_slots), "map allocation");
+    // float4 records of every slot, then the FP32 residuals of their FP64 energies
+    int rc = cuda_check(ctx, cudaMalloc(&ctx->maps, (sizeof(float4) + sizeof(float)) * P * ctx->n_slots),
+                        "map allocation");
     if (rc) return rc;
     DevGrid& g = ctx->grid;
     g.has_grid = 1;
@@ -724,6 +770,10 @@ static int alloc_maps(pxd_context* ctx, const pxd_box* box, const std::vector<in
     g.slope = static_cast<float>(ctx->slope);
     g.P = static_cast<int>(P);
     g.maps = ctx->maps;
+    g.e_lo = reinterpret_cast<const float*>(ctx->maps + P * ctx->n_slots);
+    g.init64 = make_double3(box->init_xyz[0], box->init_xyz[1], box->init_xyz[2]);
+    g.spacing64 = box->spacing;
+    g.slope64 = ctx->slope;
     return PXD_OK;
 }
 
@@ -756,8 +806,10 @@ int pxd_grid_build(pxd_context* ctx, const pxd_box* box, const int32_t* types, i
     // non-rotor receptor atoms (grid.cpp:119-123, 173)
     std::vector<float4> xq, xl;
     std::vector<float2> se;
+    std::vector<double2> se64;
     for (int a = 0; a < ctx->n_rec; ++a) {
         if (ctx->is_mov[a]) continue;
+        se64.push_back(make_double2(ctx->rec_sigma[a], ctx->rec_epsilon[a]));
         const double* x = &ctx->rec_xyz[3 * a];
         const float4 hi = make_float4(static_cast<float>(x[0]), static_cast<float>(x[1]), static_cast<float>(x[2]),
                                       static_cast<float>(ctx->rec_charge[a]));
@@ -770,14 +822,15 @@ int pxd_grid_build(pxd_context* ctx, const pxd_box* box, const int32_t* types, i
     for (size_t k = 0; k < tl.size(); ++k) slot_type[1 + k] = tl[k];
     Packer pk;
     const size_t o_xq = pk.put(xq), o_xl = pk.put(xl), o_se = pk.put(se), o_st = pk.put(slot_type);
+    const size_t o_se64 = pk.put(se64);
     void* mem = nullptr;
     rc = cuda_check(ctx, cudaMalloc(&mem, pk.bytes.size()), "grid atom upload");
     if (rc) return rc;
     rc = cuda_check(ctx, cudaMemcpy(mem, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice), "grid atom copy");
     if (!rc)
         rc = launch_grid_build(ctx, at<float4>(mem, o_xq), at<float4>(mem, o_xl), at<float2>(mem, o_se),
-                               static_cast<int>(xq.size()),
-                               at<int>(mem, o_st), ctx->n_slots, ctx->maps);
+                               at<double2>(mem, o_se64), static_cast<int>(xq.size()), at<int>(mem, o_st),
+                               ctx->n_slots, ctx->maps, const_cast<float*>(ctx->grid.e_lo));
     cudaFree(mem);
     if (rc) {
         pxd_grid_drop(ctx);
@@ -798,6 +851,7 @@ int pxd_grid_set_slope(pxd_context* ctx, double slope) {
     if (!ctx) return PXD_ERR_INVALID;
     ctx->slope = slope;
     ctx->grid.slope = static_cast<float>(slope);
+    ctx->grid.slope64 = slope;
     return PXD_OK;
 }
 
@@ -851,12 +905,19 @@ int pxd_grid_write_map(pxd_context* ctx, const pxd_box* box, int32_t map, const 
         for (int t = 0; t < PXD_NUM_VDW_TYPES; ++t) all.push_back(t);
         int rc = alloc_maps(ctx, box, all);
         if (rc) return rc;
-        cudaMemset(ctx->maps, 0, sizeof(float4) * ctx->grid.P * ctx->n_slots);
+        rc = cuda_check(ctx, cudaMemset(ctx->maps, 0, (sizeof(float4) + sizeof(float)) * ctx->grid.P * ctx->n_slots),
+                        "map clear");
+        if (rc) return rc;
     }
     const int slot = map == PXD_NUM_VDW_TYPES ? 0 : ctx->type_slot[map];
     int rc = cuda_check(ctx, cudaMemcpy(ctx->maps + static_cast<size_t>(slot) * ctx->grid.P, host_records,
                                         sizeof(float4) * ctx->grid.P, cudaMemcpyHostToDevice),
                         "map write");
+    if (rc) return rc;
+    // an installed FP32 record set carries no FP64 residual: its energies are the records'
+    rc = cuda_check(ctx, cudaMemset(const_cast<float*>(ctx->grid.e_lo) + static_cast<size_t>(slot) * ctx->grid.P, 0,
+                                    sizeof(float) * ctx->grid.P),
+                    "map residual clear");
     if (rc) return rc;
     if (ctx->has_receptor) point_explicit(ctx, true);
     rc = refresh_ligand_slots(ctx);
@@ -886,7 +947,11 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
     std::vector<float> q(N);
     std::vector<int> slots(N, -1), types(lig->vdw_type, lig->vdw_type + N);
     std::vector<float2> se(N);
+    std::vector<double> q64(N);
+    std::vector<double2> se64(N);
     for (int a = 0; a < N; ++a) {
+        q64[a] = lig->ff.charge[a];
+        se64[a] = make_double2(PXD_VDW_SIGMA[types[a]], PXD_VDW_EPSILON[types[a]]);
         q[a] = static_cast<float>(lig->ff.charge[a]);
         se[a] = make_float2(static_cast<float>(PXD_VDW_SIGMA[types[a]]), static_cast<float>(PXD_VDW_EPSILON[types[a]]));
         if (ctx->grid.has_grid) {
@@ -896,6 +961,7 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
         }
     }
     const size_t o_q = pk.put(q), o_slot = pk.put(slots), o_se = pk.put(se), o_type = pk.put(types);
+    const size_t o_q64 = pk.put(q64), o_se64 = pk.put(se64);
     // torsion tree
     const pxd_torsion_tree& tr = lig->tree;
     if (tr.n_frags > 0) {
@@ -954,6 +1020,8 @@ int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand
     d.charge = at<float>(e.mem, o_q);
     d.map_slot = at<int>(e.mem, o_slot);
     d.se = at<float2>(e.mem, o_se);
+    d.charge64 = at<double>(e.mem, o_q64);
+    d.se64 = at<double2>(e.mem, o_se64);
     d.type = at<int>(e.mem, o_type);
     d.n_frags = tr.n_frags;
     d.n_tors = tr.n_torsions;

@@ -71,19 +71,13 @@ __device__ __forceinline__ float warp_sum_f(float v) {
     return __shfl_sync(kFull, v, 0);
 }
 
-// Dot product of two D-vectors with exact FP32 products (fma) accumulated as a
+// One step of a dot product with the exact FP32 product (fma) accumulated as a
 // compensated pair: ~44 significant bits, on the FP32 pipe.
-// Out of line for the same reason as eval_pose: the optimiser takes ~20 of these.
-static __device__ __noinline__ double vdot(const float* a, const float* b, int D, int lane) {
-    DS acc{0.f, 0.f};
-    for (int e = lane; e < D; e += kWarp) {
-        const float x = a[e], y = b[e];
-        const float p = x * y;
-        const float pe = fmaf(x, y, -p);
-        ds_add(acc, p);
-        acc.lo += pe;
-    }
-    return ds_warp_sum(acc);
+__device__ __forceinline__ void ds_dot_acc(DS& acc, float x, float y) {
+    const float p = x * y;
+    const float pe = fmaf(x, y, -p);
+    ds_add(acc, p);
+    acc.lo += pe;
 }
 
 __device__ __forceinline__ double vabssum(const float* a, int D, int lane) {
@@ -170,11 +164,17 @@ __device__ __forceinline__ void sub_rec(float4* p, float3 g) {
     *p = v;
 }
 
+// Squared pair distances are floored at 1e-4 A^2 (r = 0.01 A) in the FP32 pair terms: below
+// r ~ 3e-3 A the 12th power overflows FP32 (the FP64 reference stays finite down to 1e-25 A),
+// and the inf energy / NaN gradient would end the optimisation as a NaN. Only such near-
+// coincident atoms see the floor; the reported FP64 energy (energy64.cuh) has none.
+constexpr float kPairR2Floor = 1e-4f;
+
 // One pre-combined pair (p = A, C, S2): energy into `en`, returns dE/dr_ij * r_ij / r
 // (the gradient of atom j; atom i takes its negative).
 __device__ __forceinline__ float3 pair_grad(float4 p, float4 xi, float4 xj, float& en) {
     const float3 rij = sub3(xyz(xj), xyz(xi));
-    const float r2 = dot3(rij, rij);
+    const float r2 = fmaxf(dot3(rij, rij), kPairR2Floor);
     const float rinv = rsqrtf(r2);
     const float rinv2 = rinv * rinv;
     const float x = p.z * rinv2;
@@ -255,8 +255,11 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
             const float nrkj_1 = __fdividef(1.f, sqrtf(nrkj2) + kEpsF);
             const float nrkj_2 = nrkj_1 * nrkj_1;
             const float nrkj = nrkj2 * nrkj_1;
-            const float a = -__fdividef(nrkj, dot3(m, m));
-            const float b = __fdividef(nrkj, dot3(n, n));
+            // + kEpsF: a collapsed dihedral (m or n = 0, possible in FP32 only for a pose
+            // flung ~1e11 A out of the box, where coordinates resolve to ~1e4 A) gives a zero
+            // gradient instead of 0 * inf = NaN; resolvable geometries are unaffected
+            const float a = -__fdividef(nrkj, dot3(m, m) + kEpsF);
+            const float b = __fdividef(nrkj, dot3(n, n) + kEpsF);
             const float3 gi = mul3(m, -a), gl = mul3(n, -b);
             const float pp = dot3(rij, rkj) * nrkj_2, qq = dot3(rkj, rkl) * nrkj_2;
             const float3 sv = sub3(mul3(gi, pp), mul3(gl, qq));
@@ -279,12 +282,21 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
         }
         __syncwarp();
     }
-    // 1-4 and all other pairs: Coulomb + LJ 12-6 (interaction.cpp:127-168, pair.h:25-60)
+    // 1-4 and all other pairs: Coulomb + LJ 12-6 (interaction.cpp:127-168, pair.h:25-60).
+    // The next round's record is loaded while this round computes, so its L1/L2 latency
+    // is not exposed at the round's barrier (the pair rounds are the most numerous).
+    int2 ij_n = lane < t.n_pair_slots ? __ldg(&t.pair_ij[lane]) : make_int2(-1, -1);
+    float4 p_n = lane < t.n_pair_slots ? __ldg(&t.pair_p[lane]) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int s = lane; s < t.n_pair_slots; s += kWarp) {
-        const int2 ij = __ldg(&t.pair_ij[s]);
+        const int2 ij = ij_n;
+        const float4 pp = p_n;
+        if (s + kWarp < t.n_pair_slots) {
+            ij_n = __ldg(&t.pair_ij[s + kWarp]);
+            p_n = __ldg(&t.pair_p[s + kWarp]);
+        }
         if (ij.x >= 0) {
             float en;
-            const float3 g = pair_grad(__ldg(&t.pair_p[s]), X[ij.x], X[ij.y], en);
+            const float3 g = pair_grad(pp, X[ij.x], X[ij.y], en);
             ds_add(e, en);
             sub_rec(&G0[ij.x], g);
             add_rec(&G1[ij.y], g);
@@ -385,11 +397,13 @@ struct EvalEnv {
 };
 
 // Energy and flat gradient [dE/dxyz (3N) | dE/dtorsion (R)] at x0 + t * d (d may be
-// null: evaluate at x0). Replaces binding_system_interactions::put_gradients as the
-// optimiser's closure calls it (optimizer.cpp:155-167).
+// null: evaluate at x0). With gdir, *gdot receives gradient . gdir (the line search's
+// directional derivative), accumulated while the flat gradient is written. Replaces
+// binding_system_interactions::put_gradients as the optimiser's closure calls it
+// (optimizer.cpp:155-167).
 __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLigand& L, const float* x0,
                                                 const float* d, float t, float* gout, const PoseBufs& b,
-                                                int lane) {
+                                                int lane, const float* gdir = nullptr, double* gdot = nullptr) {
     const int N = L.n_atoms;
     const int n3 = 3 * N;
     const DevReceptor& R = env.rec;
@@ -453,7 +467,7 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
                 const float3 xj = loc >= 0 ? xyz(b.loc_xyz[loc]) : xyz(rj);
                 const float2 sej = __ldg(&R.ex_se[j]);
                 const float3 rij = sub3(xj, xi);
-                const float r2 = dot3(rij, rij);
+                const float r2 = fmaxf(dot3(rij, rij), kPairR2Floor);
                 const float rinv = rsqrtf(r2);
                 const float rinv2 = rinv * rinv;
                 const float s = (sei.x + sej.x) * 0.5f;
@@ -484,7 +498,7 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
                 const float3 xj = loc >= 0 ? xyz(b.loc_xyz[loc]) : xyz(rj);
                 const float2 sej = __ldg(&R.ex_se[j]);
                 const float3 rij = sub3(xj, xi);
-                const float r2 = dot3(rij, rij);
+                const float r2 = fmaxf(dot3(rij, rij), kPairR2Floor);
                 const float rinv = rsqrtf(r2);
                 const float rinv2 = rinv * rinv;
                 const float s = (sei.x + sej.x) * 0.5f;
@@ -503,12 +517,21 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
     }
     __syncwarp();
     // flat gradient and the receptor-torsion chain rule (interaction.cpp:338-350)
+    DS gd{0.f, 0.f};
     for (int a = lane; a < N; a += kWarp) {
         const float4 g0 = b.lig_grad[a], g1 = b.lig_grad[b.lig_gs + a];
         const float4 g2 = b.lig_grad[2 * b.lig_gs + a], g3 = b.lig_grad[3 * b.lig_gs + a];
-        gout[3 * a] = (g0.x + g1.x) + (g2.x + g3.x);
-        gout[3 * a + 1] = (g0.y + g1.y) + (g2.y + g3.y);
-        gout[3 * a + 2] = (g0.z + g1.z) + (g2.z + g3.z);
+        const float gx = (g0.x + g1.x) + (g2.x + g3.x);
+        const float gy = (g0.y + g1.y) + (g2.y + g3.y);
+        const float gz = (g0.z + g1.z) + (g2.z + g3.z);
+        gout[3 * a] = gx;
+        gout[3 * a + 1] = gy;
+        gout[3 * a + 2] = gz;
+        if (gdir) {
+            ds_dot_acc(gd, gx, gdir[3 * a]);
+            ds_dot_acc(gd, gy, gdir[3 * a + 1]);
+            ds_dot_acc(gd, gz, gdir[3 * a + 2]);
+        }
     }
     for (int r = lane; r < R.n_rotors; r += kWarp) {
         float acc = 0.f;
@@ -521,8 +544,10 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
             acc += dot3(xyz(b.mov_jac[l]), g);
         }
         gout[n3 + r] = acc;
+        if (gdir) ds_dot_acc(gd, acc, gdir[n3 + r]);
     }
     __syncwarp();
+    if (gdir) *gdot = ds_warp_sum(gd);
     return ds_warp_sum(e) + R.e_const;
 }
 
@@ -530,8 +555,8 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
 // much code overflow the instruction cache (the top stall of the batched kernel).
 static __device__ __noinline__ double eval_pose(const EvalEnv& env, const DevLigand& L, const float* x0,
                                                 const float* d, float t, float* gout, const PoseBufs& b,
-                                                int lane) {
-    return eval_pose_body(env, L, x0, d, t, gout, b, lane);
+                                                int lane, double* gdot = nullptr) {
+    return eval_pose_body(env, L, x0, d, t, gout, b, lane, gdot ? d : nullptr, gdot);
 }
 
 // Shared-memory floats needed by PoseBufs for a ligand of up to n_atoms atoms.

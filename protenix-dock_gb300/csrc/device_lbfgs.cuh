@@ -6,6 +6,7 @@
 #pragma once
 
 #include "device_eval.cuh"
+#include "energy64.cuh"
 
 namespace pxd {
 
@@ -66,9 +67,10 @@ struct Closure {
     int nevals;
 };
 
-__device__ __forceinline__ double closure_eval(Closure& c, double t, const float* d, float* g) {
+__device__ __forceinline__ double closure_eval(Closure& c, double t, const float* d, float* g,
+                                               double* gdot = nullptr) {
     ++c.nevals;
-    return eval_pose(*c.env, *c.L, c.x0, d, static_cast<float>(t), g, *c.b, c.lane);
+    return eval_pose(*c.env, *c.L, c.x0, d, static_cast<float>(t), g, *c.b, c.lane, gdot);
 }
 
 __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double g1, double x2,
@@ -121,12 +123,12 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
     Bracket B;
     B.bg0 = v.bg0;
     B.bg1 = v.bg1;
-    double f_new = closure_eval(c, t, d, g_new);
+    double gtd_new = 0.0;
+    double f_new = closure_eval(c, t, d, g_new, &gtd_new);
     if (isnan(f_new)) {
         f_io = f_new;
         return;
     }
-    double gtd_new = vdot(g_new, d, D, lane);
     if (fabs(gtd_new) > p.gtd_threshold) {
         f_io = f_new;
         vcopy(g, g_new, D, lane);
@@ -167,8 +169,7 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
         vcopy(g_prev, g_new, D, lane);
         gpv = g_prev;
         gtd_prev = gtd_new;
-        f_new = closure_eval(c, t, d, g_new);
-        gtd_new = vdot(g_new, d, D, lane);
+        f_new = closure_eval(c, t, d, g_new, &gtd_new);
         ++ls_iter;
     }
     double d_norm = 0.0;
@@ -211,8 +212,7 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
         } else {
             insuf = false;
         }
-        f_new = closure_eval(c, t, d, g_new);
-        gtd_new = vdot(g_new, d, D, lane);
+        f_new = closure_eval(c, t, d, g_new, &gtd_new);
         ++ls_iter;
         if (f_new > (f + p.c1 * t * gtd) || f_new >= B.bf(lo)) {
             B.set_br(hi, t);
@@ -246,14 +246,6 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
     vcopy(g, B.bg(lo), D, lane);
 }
 
-// One step of a compensated dot product: the body of vdot, so that a dot accumulated
-// inside another pass gives vdot's result bit for bit.
-__device__ __forceinline__ void ds_dot_acc(DS& acc, float x, float y) {
-    const float p = x * y;
-    const float pe = fmaf(x, y, -p);
-    ds_add(acc, p);
-    acc.lo += pe;
-}
 
 // lbfgs_step::apply (optimizer.cpp:429-560) on the pose held in v.x; returns status.
 //
@@ -268,16 +260,21 @@ __device__ __forceinline__ void ds_dot_acc(DS& acc, float x, float y) {
 //     step with g . d for the line search.
 // Kept pairs sit in physical slots (base + j) % (m + 1), j = 0 .. count - 1 oldest first;
 // the spare slot (base + count) % (m + 1) receives the next pair.
+//
+// energy receives the FP64 objective at the returned pose (energy64), or, with
+// final_energy false (a caller that does not use it), the last FP32 loss.
 static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v, int D,
-                          size_t Dp, int lane, double& energy) {
+                          size_t Dp, int lane, double& energy, bool final_energy = true) {
     const int m = p.m;
     const int slots = hist_slots(m);
     const int max_eval = p.max_eval > 0 ? p.max_eval : p.max_iter * 5 / 4;
     c.x0 = v.x;
     c.nevals = 0;
     double loss = closure_eval(c, 0.0, nullptr, v.g);
-    energy = loss;
-    if (vabsmax(v.g, D, lane) < p.tol_grad) return PXD_POSE_CONVERGED;
+    if (vabsmax(v.g, D, lane) < p.tol_grad) {
+        energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : loss;
+        return PXD_POSE_CONVERGED;
+    }
     int status = PXD_POSE_NOT_CONVERGED;
     int base = 0, count = 0;
     double H_diag = 1.0, t = 0.0, prev_loss;
@@ -432,7 +429,10 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
             break;
         }
     }
-    if (updated) energy = closure_eval(c, 0.0, nullptr, v.gnew);
+    // the reported energy: the FP64 objective at the returned pose; an optimisation that
+    // moved counts it as its final evaluation, as the reference does (optimizer.cpp:552-556)
+    if (updated) ++c.nevals;
+    energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : loss;
     return status;
 }
 

@@ -11,6 +11,12 @@
 // The Coulomb map is summed in FP64 (see the loop).
 // The squared distance is floored at 1e-4 A^2 so that a grid point sitting on an atom
 // cannot overflow FP32, and records are clamped to +-1e30 before the FP32 store.
+//
+// The energy channel is also kept in FP64 for the final FP64 energy of a pose: every LJ
+// pair term above kFp64Term kcal/mol in magnitude is recomputed in FP64 from FP64 sigma,
+// epsilon and coordinates (an FP32 term carries ~1e-6 of its size, 100 kcal/mol on a
+// 1e8 clash), the smaller ones stay FP32 (each under 1e-9 kcal/mol of rounding), and the
+// record's energy is the FP64 sum rounded to FP32 with the remainder stored in e_lo.
 #include "device_eval.cuh"
 #include "../../include/pxdock_gb300_vdw.h"
 
@@ -21,18 +27,22 @@ constexpr int kGridTile = 256;
 constexpr float kR2Floor = 1e-4f;
 constexpr double kRecordCeil = 1e30;
 constexpr double kCoulombD = 332.0637141491396;  // kCoulombFactor, system.h:83
+constexpr float kFp64Term = 1e-3f;
 
 struct GridArgs {
     const float4* atoms;   // x, y, z, charge of every non-rotor receptor atom (FP32 hi part)
     const float4* atoms_lo;// x, y, z, charge residuals: value - hi, in FP32
     const float2* se;      // sigma, epsilon
+    const double2* se64;   // sigma, epsilon in FP64
     int n_atoms;
     int3 npts;
     double3 init;
     double spacing;
     const int* slot_type;  // [n_slots] ligand type, or -1 for the Coulomb map
     const float2* type_se; // [99] sigma, epsilon of the ligand types
+    const double2* type_se64;
     float4* maps;
+    float* e_lo;           // [n_slots][P] FP64 energy - FP32 record energy
     int P;
 };
 
@@ -44,11 +54,13 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
     __shared__ float4 s_xyzq[kGridTile];
     __shared__ float4 s_lo[kGridTile];
     __shared__ float2 s_se[kGridTile];
+    __shared__ double2 s_se64[kGridTile];
     const int p = blockIdx.x * kGridThreads + threadIdx.x;
     const int slot = blockIdx.y;
     const int type = a.slot_type[slot];
     const bool coul = type < 0;
     const float2 tse = coul ? make_float2(0.f, 0.f) : a.type_se[type];
+    const double2 tse64 = coul ? make_double2(0.0, 0.0) : a.type_se64[type];
     const int nz = a.npts.z, ny = a.npts.y;
     const int k = p % nz;
     const int j = (p / nz) % ny;
@@ -59,6 +71,7 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
     const float3 pl = make_float3(static_cast<float>(px - pt.x), static_cast<float>(py - pt.y),
                                   static_cast<float>(pz - pt.z));
     double E = 0.0, GX = 0.0, GY = 0.0, GZ = 0.0;
+    double E64 = 0.0;  // LJ terms recomputed in FP64
     for (int t0 = 0; t0 < a.n_atoms; t0 += kGridTile) {
         const int n = min(kGridTile, a.n_atoms - t0);
         __syncthreads();
@@ -66,6 +79,7 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
             s_xyzq[u] = a.atoms[t0 + u];
             s_lo[u] = a.atoms_lo[t0 + u];
             s_se[u] = a.se[t0 + u];
+            s_se64[u] = a.se64[t0 + u];
         }
         __syncthreads();
         float e = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
@@ -108,7 +122,20 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
                 const float u6 = x * x * x;
                 const float u12 = u6 * u6;
                 const float C = sqrtf(tse.y * se.y) * 4.f;
-                e = fmaf(C, u12 - u6, e);
+                const float ep = C * (u12 - u6);
+                if (fabsf(ep) > kFp64Term) {
+                    const double2 se64 = s_se64[u];
+                    const double dx = (static_cast<double>(at.x) - px) + static_cast<double>(lo.x);
+                    const double dy = (static_cast<double>(at.y) - py) + static_cast<double>(lo.y);
+                    const double dz = (static_cast<double>(at.z) - pz) + static_cast<double>(lo.z);
+                    const double r2d = fmax(dx * dx + dy * dy + dz * dz, static_cast<double>(kR2Floor));
+                    const double sd = (tse64.x + se64.x) * 0.5;
+                    const double xd = sd * sd / r2d;
+                    const double u6d = xd * xd * xd;
+                    E64 += sqrt(tse64.y * se64.y) * 4.0 * (u6d * u6d - u6d);
+                } else {
+                    e += ep;
+                }
                 // grad_point -= vec * de_dr_r, de_dr_r = C(-12 u12 + 6 u6) / r^2 (pair.h:42-60)
                 const float w = C * (12.f * u12 - 6.f * u6) * rinv2;
                 gx = fmaf(vx, w, gx);
@@ -122,17 +149,24 @@ __global__ void __launch_bounds__(kGridThreads) grid_build_kernel(const GridArgs
         }
     }
     if (p < a.P) {
-        a.maps[static_cast<size_t>(slot) * a.P + p] =
-            make_float4(clampf_rec(E), clampf_rec(GX), clampf_rec(GY), clampf_rec(GZ));
+        const double Ef = E + E64;
+        const float hi = clampf_rec(Ef);
+        a.maps[static_cast<size_t>(slot) * a.P + p] = make_float4(hi, clampf_rec(GX), clampf_rec(GY), clampf_rec(GZ));
+        const double rest = Ef - static_cast<double>(hi);
+        a.e_lo[static_cast<size_t>(slot) * a.P + p] =
+            fabs(Ef) < kRecordCeil ? static_cast<float>(rest) : 0.f;
     }
 }
 
 int launch_grid_build(pxd_context* ctx, const float4* atoms, const float4* atoms_lo, const float2* se,
-                      int n_atoms, const int* slot_type, int n_slots, float4* maps) {
+                      const double2* se64, int n_atoms, const int* slot_type, int n_slots, float4* maps,
+                      float* e_lo) {
     GridArgs a{};
     a.atoms = atoms;
     a.atoms_lo = atoms_lo;
     a.se = se;
+    a.se64 = se64;
+    a.e_lo = e_lo;
     a.n_atoms = n_atoms;
     a.npts = make_int3(ctx->box.npoints[0], ctx->box.npoints[1], ctx->box.npoints[2]);
     a.init = make_double3(ctx->box.init_xyz[0], ctx->box.init_xyz[1], ctx->box.init_xyz[2]);
@@ -141,18 +175,26 @@ int launch_grid_build(pxd_context* ctx, const float4* atoms, const float4* atoms
     a.maps = maps;
     a.P = ctx->grid.P;
     // ligand type table on the device (sigma, epsilon)
-    float2 table[PXD_NUM_VDW_TYPES];
-    for (int t = 0; t < PXD_NUM_VDW_TYPES; ++t)
-        table[t] = make_float2(static_cast<float>(PXD_VDW_SIGMA[t]),
-                               static_cast<float>(PXD_VDW_EPSILON[t]));
-    float2* d_table = nullptr;
+    struct Tables {
+        float2 f32[PXD_NUM_VDW_TYPES];
+        double2 f64[PXD_NUM_VDW_TYPES];
+    } table;
+    for (int t = 0; t < PXD_NUM_VDW_TYPES; ++t) {
+        table.f32[t] = make_float2(static_cast<float>(PXD_VDW_SIGMA[t]), static_cast<float>(PXD_VDW_EPSILON[t]));
+        table.f64[t] = make_double2(PXD_VDW_SIGMA[t], PXD_VDW_EPSILON[t]);
+    }
+    Tables* d_table = nullptr;
     int rc = cuda_check(ctx, cudaMallocAsync(&d_table, sizeof(table), ctx->stream), "type table");
     if (rc) return rc;
-    rc = cuda_check(ctx, cudaMemcpyAsync(d_table, table, sizeof(table), cudaMemcpyHostToDevice,
+    rc = cuda_check(ctx, cudaMemcpyAsync(d_table, &table, sizeof(table), cudaMemcpyHostToDevice,
                                          ctx->stream),
                     "type table copy");
-    if (rc) return rc;
-    a.type_se = d_table;
+    if (rc) {
+        cudaFreeAsync(d_table, ctx->stream);
+        return rc;
+    }
+    a.type_se = d_table->f32;
+    a.type_se64 = d_table->f64;
     dim3 grid((a.P + kGridThreads - 1) / kGridThreads, n_slots);
     grid_build_kernel<<<grid, kGridThreads, 0, ctx->stream>>>(a);
     rc = cuda_check(ctx, cudaGetLastError(), "grid_build_kernel launch");

@@ -112,7 +112,7 @@ struct ScoreArgs {
     int D_pad;
 };
 
-__global__ void __launch_bounds__(kWarpsPerBlock * kWarp) score_kernel(const ScoreArgs a) {
+__global__ void __launch_bounds__(kWarpsPerBlock * kWarp) score_kernel(const __grid_constant__ ScoreArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
@@ -135,11 +135,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp) score_kernel(const Sco
         for (int e = lane; e < 3 * N; e += kWarp) x[e] = px[e];
         for (int r = lane; r < R; r += kWarp) x[3 * N + r] = a.tors[static_cast<size_t>(pose) * R + r];
         __syncwarp();
-        const double e = eval_pose_body(a.env, L, x, nullptr, 0.f, g, b, lane);
+        eval_pose_body(a.env, L, x, nullptr, 0.f, g, b, lane);
         float* og = a.lig_grad + static_cast<size_t>(pose) * a.max_atoms * 3;
         for (int k = lane; k < 3 * N; k += kWarp) og[k] = g[k];
         for (int r = lane; r < R; r += kWarp)
             a.tors_grad[static_cast<size_t>(pose) * R + r] = g[3 * N + r];
+        // the energy is the FP64 objective, the gradient the FP32 one
+        const double e = energy64(a.env, a.ligands[lid], x, b, lane);
         if (lane == 0) a.energy[pose] = e;
         __syncwarp();
     }
@@ -279,11 +281,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp) score_multi_kernel(con
         for (int e = lane; e < 3 * N; e += kWarp) x[e] = px[e];
         for (int r = lane; r < R; r += kWarp) x[3 * N + r] = a.tors[static_cast<size_t>(pose) * a.tors_stride + r];
         __syncwarp();
-        const double e = eval_pose_body(env, L, x, nullptr, 0.f, g, b, lane);
+        eval_pose_body(env, L, x, nullptr, 0.f, g, b, lane);
         float* og = a.lig_grad + static_cast<size_t>(pose) * a.max_atoms * 3;
         for (int k = lane; k < 3 * a.max_atoms; k += kWarp) og[k] = k < 3 * N ? g[k] : 0.f;
         for (int r = lane; r < R; r += kWarp)
             a.tors_grad[static_cast<size_t>(pose) * a.tors_stride + r] = g[3 * N + r];
+        // the energy is the FP64 objective, the gradient the FP32 one (as score_kernel)
+        const double e = energy64(env, a.tabs[c][lid], x, b, lane);
         if (lane == 0) a.energy[pose] = e;
         __syncwarp();
     }

@@ -396,8 +396,8 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                         const double gm = *reinterpret_cast<volatile double*>(&a.gmin[lid]);
                         if (pre > gm + a.threshold) continue;
                     }
-                    double cdd_e = 0.0;
-                    lbfgs_pose(c, a.fast, v, D, Dp, lane, cdd_e);
+                    double cdd_e = 0.0;  // unused: the step is judged by its pose score
+                    lbfgs_pose(c, a.fast, v, D, Dp, lane, cdd_e, false);
                     total += c.nevals;
                     const double cdd_ps = mc_pscore(a, L, v.x, b, lane);
                     bool accept = step == 0 || cdd_ps < tmp_ps;

@@ -38,6 +38,11 @@ struct DevTopo {
     const float4* dih_term;   // k, periodicity, phase, -
     const int2* pair_ij;
     const float4* pair_p;     // A = 332.06 qi qj s_c, C = 4 sqrt(ei ej) s_v, S2 = ((si+sj)/2)^2
+    // the same parameters in FP64, slot for slot, for the final FP64 energy (energy64.cuh)
+    const double2* bond_p64;
+    const double2* angle_p64;
+    const double4* dih_term64;
+    const double4* pair_p64;
 };
 
 struct DevSf {
@@ -99,6 +104,8 @@ struct DevLigand {
     const float* charge;      // [N]
     const int* map_slot;      // [N] vdW map slot of the atom's type (-1: no map)
     const float2* se;         // [N] sigma, epsilon (explicit inter pairs)
+    const double* charge64;   // [N] FP64 copies for the final FP64 energy
+    const double2* se64;      // [N]
     const int* type;          // [N] ligand vdW type
     // torsion tree (forward kinematics, data.cpp:592-641)
     int n_frags, n_tors;
@@ -121,6 +128,12 @@ struct DevReceptor {
     const float4* rotor_axis;     // [R] unit
     const int* rotor_mov;         // [R+1] rotor atoms are local [rotor_mov[r], rotor_mov[r+1])
     const float4* local_xyz0;     // [n_local] input coordinates (rotor atoms: x0 - origin)
+    // FP64 copies for the final FP64 energy
+    const double4* ex_xyzq64;
+    const double2* ex_se64;
+    const double4* rotor_origin64;
+    const double4* rotor_axis64;
+    const double4* local_xyz064;  // w: rotor id as a double (rotor atoms)
     DevTopo intra;                // rotor-touching receptor terms over local atoms
     double e_const;               // energy of the receptor terms that touch no rotor atom
 };
@@ -136,6 +149,11 @@ struct DevGrid {
     float slope;
     int P;
     const float4* maps;
+    // the final FP64 energy: box geometry and slope in FP64, and per map point the FP64
+    // energy's residual below its FP32 record, E = maps[.].x + e_lo[.]
+    double3 init64;
+    double spacing64, slope64;
+    const float* e_lo;        // [n_slots][P]
 };
 
 // Flat DOF layout of a pose: [ligand xyz (3N) | receptor torsions (T_r)] (optimizer.cpp:56-76)
@@ -178,7 +196,7 @@ struct pxd_context {
     void* rec_ex_all = nullptr;           // explicit list with every receptor atom (no maps)
     void* rec_ex_mov = nullptr;           // explicit list with rotor atoms (maps present)
     int n_ex_all = 0, n_ex_mov = 0;
-    size_t ex_all_off[3] = {0, 0, 0}, ex_mov_off[3] = {0, 0, 0};
+    size_t ex_all_off[5] = {0, 0, 0, 0, 0}, ex_mov_off[5] = {0, 0, 0, 0, 0};
     // maps
     pxd::DevGrid grid{};
     pxd_box box{};
@@ -234,8 +252,8 @@ int class_join(pxd_context* ctx, size_t k, cudaStream_t s);
 
 // kernels (launchers), one per translation unit
 int launch_grid_build(pxd_context* ctx, const float4* atoms_xyzq, const float4* atoms_lo,
-                      const float2* atoms_se, int n_atoms, const int* slot_types, int n_slots,
-                      float4* maps);
+                      const float2* atoms_se, const double2* atoms_se64, int n_atoms, const int* slot_types,
+                      int n_slots, float4* maps, float* e_lo);
 int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_ids,
                  const float* xyz, const float* tors, double* energy, float* lig_grad,
                  float* tors_grad, cudaStream_t s);
