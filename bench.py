@@ -229,24 +229,20 @@ def run_reference(args):
 
 
 def screening_ligands(n, seed=3):
-    """Seeded ligands of uneven size: heavy atoms U{10..60}, rotatable bonds U{0..15},
-    C 70 % / N 12 % / O 15 % / Cl 3 % (a draw the generator cannot embed is redrawn)."""
+    """Seeded ligands of uneven size (pxdock_gb300.synth.screening_set: heavy atoms U{10..60},
+    rotatable bonds U{0..15}, C 70 % / N 12 % / O 15 % / Cl 3 %), built on all host cores.
+    Ligands the device path does not take (over 256 atoms, 32 torsions or 64 fragments) are
+    skipped like draws the generator cannot embed."""
     from pxdock_gb300 import model, synth
 
-    rng = np.random.default_rng(seed)
-    out, k = [], 0
-    while len(out) < n and k < 20 * n:
-        h, r = int(rng.integers(10, 61)), int(rng.integers(0, 16))
-        k += 1
-        try:
-            lj = synth.make_ligand(seed=1000 + k, n_heavy=h, n_rot=min(r, h // 3), n_n=max(1, round(0.12 * h)),
-                                   n_o=max(1, round(0.15 * h)), n_other=round(0.03 * h))
-        except RuntimeError:
-            continue
-        lig = model.Ligand.from_json(lj)
-        if lig.n_atoms <= 256 and lig.n_torsions <= 32 and lig.tree.n_frags <= 64:
-            out.append(lig)
-    return out
+    return [model.Ligand.from_json(lj) for lj in synth.screening_set(n, seed, cpu_threads(), _screening_accept)]
+
+
+def _screening_accept(lj):
+    from pxdock_gb300 import model
+
+    lig = model.Ligand.from_json(lj)
+    return lig.n_atoms <= 256 and lig.n_torsions <= 32 and lig.tree.n_frags <= 64
 
 
 def run_screening(args):

@@ -17,6 +17,7 @@ named shapes stand in for them:
 The JSON written here is read by the same parsers as real prepared inputs.
 """
 import math
+import os
 
 import numpy as np
 
@@ -41,14 +42,25 @@ def _blen(a, b):
     return BOND_LEN.get((a, b)) or BOND_LEN.get((b, a)) or 1.5
 
 
+# 3-vector cross product and norm with the values numpy's cross / linalg.norm give (the
+# same IEEE products and the same sqrt of the dot product), without their per-call
+# overhead, which dominated ligand generation.
+def _cross3(a, b):
+    return np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]])
+
+
+def _norm3(v):
+    return math.sqrt(v.dot(v))
+
+
 def _unit(v):
-    return v / np.linalg.norm(v)
+    return v / _norm3(v)
 
 
 def _perp(v, rng):
     while True:
-        w = np.cross(v, rng.normal(size=3))
-        n = np.linalg.norm(w)
+        w = _cross3(v, rng.normal(size=3))
+        n = _norm3(w)
         if n > 1e-3:
             return w / n
 
@@ -265,7 +277,7 @@ def _free_dirs(m, i, rng, count):
         out = _unit(m.xyz[i] - cen)
         if hyb == "ar" or count == 1:
             return [out] * count
-        nrm = _unit(np.cross(m.xyz[atoms[1]] - m.xyz[atoms[0]], m.xyz[atoms[2]] - m.xyz[atoms[0]]))
+        nrm = _unit(_cross3(m.xyz[atoms[1]] - m.xyz[atoms[0]], m.xyz[atoms[2]] - m.xyz[atoms[0]]))
         return [_unit(out * 0.58 + nrm * 0.81), _unit(out * 0.58 - nrm * 0.81)][:count]
     if hyb == "sp2":
         if len(nb) == 0:
@@ -286,7 +298,7 @@ def _free_dirs(m, i, rng, count):
     if len(nb) == 1:
         a = -nb[0]
         b = _perp(a, rng)
-        c = np.cross(a, b)
+        c = _cross3(a, b)
         ca, sa = math.cos(math.radians(70.5)), math.sin(math.radians(70.5))
         out = []
         for k in range(3):
@@ -295,7 +307,7 @@ def _free_dirs(m, i, rng, count):
         return out[:count]
     if len(nb) == 2:
         bis = _unit(-(nb[0] + nb[1]))
-        nrm = _unit(np.cross(nb[0], nb[1]))
+        nrm = _unit(_cross3(nb[0], nb[1]))
         return [_unit(bis * 0.58 + nrm * 0.81), _unit(bis * 0.58 - nrm * 0.81)][:count]
     return [_unit(-(nb[0] + nb[1] + nb[2]))][:count]
 
@@ -336,8 +348,8 @@ def _place_fragment(m, f, anchor, new_atom, rng):
     else:
         own = np.array([1.0, 0.0, 0.0])
     target = -d_out
-    v = np.cross(own, target)
-    s, c = np.linalg.norm(v), float(np.dot(own, target))
+    v = _cross3(own, target)
+    s, c = _norm3(v), float(np.dot(own, target))
     if s < 1e-8:
         R = np.eye(3) if c > 0 else _rot(_perp(own, rng), math.pi)
     else:
@@ -856,3 +868,44 @@ def random_poses(ligand, box_lo, box_hi, n, seed):
     T = ligand.n_torsions
     tors = rng.uniform(-math.pi, math.pi, size=(n, T))
     return apply_parameters(ligand.tree, ligand.poses[0], centers, rots, tors)
+
+
+# ------------------------------------------------------------ screening ligand sets
+def _screening_spec_ligand(spec):
+    """One draw of screening_set: (k, heavy atoms, rotors) -> (k, ligand JSON or None)."""
+    k, h, r = spec
+    try:
+        return k, make_ligand(seed=1000 + k, n_heavy=h, n_rot=min(r, h // 3), n_n=max(1, round(0.12 * h)),
+                              n_o=max(1, round(0.15 * h)), n_other=round(0.03 * h))
+    except RuntimeError:
+        return k, None
+
+
+def screening_set(n, seed=3, processes=None, accept=None):
+    """n seeded ligands of uneven size: heavy atoms U{10..60}, rotatable bonds U{0..15},
+    C 70 % / N 12 % / O 15 % / Cl 3 %. Draw k (k = 1, 2, ...) takes (heavy, rotors) from one
+    seeded stream and builds ligand seed 1000 + k; a draw the generator cannot embed, or
+    that accept(json) refuses, is skipped, and the first n accepted draws are returned in
+    draw order. The draws are built by a process pool (started with spawn) in batches, so
+    the set is the same for any number of processes."""
+    import multiprocessing as mp
+
+    rng = np.random.default_rng(seed)
+    specs = [(k, int(rng.integers(10, 61)), int(rng.integers(0, 16))) for k in range(1, 20 * n + 1)]
+    processes = processes or os.cpu_count() or 1
+    out, pos = [], 0
+    pool = mp.get_context("spawn").Pool(processes) if processes > 1 and n > 8 else None
+    try:
+        while len(out) < n and pos < len(specs):
+            batch = specs[pos:pos + max(2 * (n - len(out)), 16)]
+            pos += len(batch)
+            done = (pool.map(_screening_spec_ligand, batch, chunksize=1) if pool
+                    else [_screening_spec_ligand(s) for s in batch])
+            for _, lj in sorted(done, key=lambda kv: kv[0]):
+                if lj is not None and (accept is None or accept(lj)) and len(out) < n:
+                    out.append(lj)
+    finally:
+        if pool:
+            pool.close()
+            pool.join()
+    return out

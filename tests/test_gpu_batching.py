@@ -97,7 +97,7 @@ def test_size_classes_match_single_ligand_launches():
     assert sorted(chosen) == [32, 64, 96] and all(v & 255 in (0, 3, 4, 5, 6) and v >> 8 in (0, 1) for v in chosen.values())
     assert np.array_equal(x.cpu().numpy(), xyz)
     tuned = run(xyz, lig_ids, maxN)
-    if all(v == 4 for v in chosen.values()):  # the default variant: the same launch
+    if all(v == 5 for v in chosen.values()):  # the default variant: the same launch
         assert np.array_equal(tuned[1], mixed[1])
     else:  # another register budget may round differently; trajectories then part
         assert abs(np.median(tuned[1]) - np.median(mixed[1])) <= 0.01 * abs(np.median(mixed[1])) + 1e-3
