@@ -749,7 +749,8 @@ def run_unroll(args):
         # adjoint and the kinematics run in FP32 kernels
         q = torch.tensor(q0[sel], dtype=torch.float64, device=dev)
         target = UN.place(be, torch.tensor(qt[sel], dtype=torch.float64, device=dev)).detach()
-        qK = UN.lbfgs_unroll(be, q, w, t, steps=steps, history=8, cap=0.3, every=10)
+        qK = UN.lbfgs_unroll(be, q, w, t, steps=steps, history=8, cap=0.3, every=10, truncate=args.unroll_truncate,
+                             clip=args.unroll_clip)
         loss = UN.rmsd_loss(UN.place(be, qK), target, n_atoms[sel])
         loss.backward()
         return loss, w.grad, t.grad
@@ -783,7 +784,8 @@ def run_unroll(args):
                                    "empirical score (no maps needed)"
                                    % (n_cplx, len(ctxs), min(l.n_atoms for l in ligs), max(l.n_atoms for l in ligs),
                                       max(l.n_torsions for l in ligs), P_each, K),
-                       "poses": n},
+                       "poses": n, "gradient": "exact" if args.unroll_truncate is None and args.unroll_clip is None
+                       else "truncated to the last %s steps, clipped at %s" % (args.unroll_truncate, args.unroll_clip)},
             "poses_per_s": n / t_ms * 1e3,
             "peak_hbm": {"torch_max_allocated_gb": peak_torch / 1e9,
                          "device_used_gb": (total_mem - min(free0, free1)) / 1e9},
@@ -836,7 +838,8 @@ def unroll_cpu_check(args, ctxs, recs, ligs, lig_of, ref, q0, qt, sf, D, K, P_ea
         t = torch.tensor(abi.smooth_pair_tables(1), dtype=tdt, device=d, requires_grad=True)
         t0 = time.perf_counter()
         target = UN.place(be, torch.tensor(qt[sel], device=d)).detach()
-        qK = UN.lbfgs_unroll(be, torch.tensor(q0[sel], device=d), w, t, steps=K, history=8, cap=0.3, every=10)
+        qK = UN.lbfgs_unroll(be, torch.tensor(q0[sel], device=d), w, t, steps=K, history=8, cap=0.3, every=10,
+                             truncate=args.unroll_truncate, clip=args.unroll_clip)
         x = UN.place(be, qK)
         mask = (torch.arange(x.shape[1], device=d)[None, :] < torch.tensor(n_atoms, device=d)[:, None]).to(x.dtype)
         rmsd = torch.sqrt((((x - target) ** 2).sum(-1) * mask).sum(1) / torch.tensor(n_atoms, device=d).to(x.dtype))
@@ -948,6 +951,10 @@ def main():
     ap.add_argument("--complexes", type=int, default=None,
                     help="differentiate / unroll: number of complexes (64 / 1024)")
     ap.add_argument("--unroll-steps", type=int, default=50, help="unroll: L-BFGS steps")
+    ap.add_argument("--unroll-truncate", type=int, default=None,
+                    help="unroll: backpropagate through the last T steps only (default: all)")
+    ap.add_argument("--unroll-clip", type=float, default=None,
+                    help="unroll: clip each pose's state gradient row at segment boundaries")
     ap.add_argument("--walkers", type=int, default=64, help="docking: Monte-Carlo walkers (exhaustiveness)")
     ap.add_argument("--mc-steps", type=int, default=2000, help="docking: Monte-Carlo steps per walker")
     ap.add_argument("--relax-steps", type=int, default=300, help="docking: L-BFGS iterations per step")

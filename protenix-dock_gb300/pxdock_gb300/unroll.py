@@ -181,17 +181,48 @@ def _lbfgs_steps(k0, k1, backend, w, t, cap, q, qp, gp, S, Y, R, M, gamma):
     return q, qp, gp, S, Y, R, M, gamma
 
 
-def lbfgs_unroll(backend, q0, w, t, steps, history=8, cap=0.3, every=10):
+class _ClipRows(torch.autograd.Function):
+    """Identity whose backward scales every row (last dimension) of the incoming gradient
+    down to a Euclidean norm of at most max_norm."""
+
+    @staticmethod
+    def forward(fctx, x, max_norm):
+        fctx.max_norm = max_norm
+        return x.view_as(x)
+
+    @staticmethod
+    def backward(fctx, g):
+        n = g.norm(dim=-1, keepdim=True)
+        return g * torch.clamp(fctx.max_norm / torch.where(n > 0, n, torch.ones_like(n)), max=1.0), None
+
+
+def lbfgs_unroll(backend, q0, w, t, steps, history=8, cap=0.3, every=10, truncate=None, clip=None):
     """q_K after `steps` unrolled L-BFGS steps from q0 [P][D], differentiable in w, t and
-    q0; segments of `every` steps are checkpointed."""
+    q0; segments of `every` steps are checkpointed.
+
+    The map q0 -> q_K is chaotic over many steps (the FP32 and FP64 trajectories part, and
+    the exact derivative through 50 steps reaches ~1e50), so two bounded alternatives to the
+    exact gradient are offered:
+      truncate=T  backpropagates through the last T steps only: the optimiser state after
+                  step steps - T enters as a constant (truncated backpropagation through
+                  time); q0 then gets no gradient for T < steps;
+      clip=c      at every segment boundary scales each pose's row of the state's incoming
+                  gradient to a norm of at most c.
+    Both leave the forward pass (q_K, the loss) unchanged; by default the gradient is exact."""
     P, D = q0.shape
     z = torch.zeros((history, P, D), dtype=q0.dtype, device=q0.device)
     state = (q0, torch.zeros_like(q0), torch.zeros_like(q0), z, z.clone(),
              torch.zeros((history, P), dtype=q0.dtype, device=q0.device),
              torch.zeros((history, P), dtype=q0.dtype, device=q0.device),
              torch.ones(P, dtype=q0.dtype, device=q0.device))
-    for k0 in range(0, steps, every):
-        k1 = min(k0 + every, steps)
+    cut = None if truncate is None else max(0, steps - int(truncate))
+    bounds = sorted(set(list(range(0, steps, every)) + ([cut] if cut is not None and cut < steps else [])))
+    for i, k0 in enumerate(bounds):
+        k1 = bounds[i + 1] if i + 1 < len(bounds) else steps
+        if k0 == cut:
+            state = tuple(s.detach() for s in state)
+        elif clip is not None and k0 > 0:
+            state = tuple(_ClipRows.apply(s, clip) if s.requires_grad and s.dim() >= 2 else s for s in state)
         state = checkpoint(_lbfgs_steps, k0, k1, backend, w, t, cap, *state, use_reentrant=False)
     return state[0]
 
