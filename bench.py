@@ -260,8 +260,12 @@ def run_screening(args):
     ligs = screening_ligands(args.ligands)
     ctx = native.Context(local)
     ctx.set_receptor(rec)
-    ctx.build_grid(box, sorted(set(int(t) for l in ligs for t in l.vdw_type)))
+    types = sorted(set(int(t) for l in ligs for t in l.vdw_type))
+    n_maps = 1 + len(types)
+    ctx.build_grid(box, types)
     ctx.set_slope(SLOPE)
+    if args.l2_residency:
+        ctx.set_l2_residency(args.l2_residency)
     ids = [ctx.add_ligand(l) for l in ligs]
     lo = np.array(box.init_xyz)
     hi = lo + (np.array(box.npoints) - 1) * box.spacing
@@ -314,7 +318,9 @@ def run_screening(args):
                                    "81^3 maps, m=%d, max_iter=%d, tol_grad=%g"
                                    % (len(ligs), min(sizes), max(sizes), max(l.n_torsions for l in ligs), P,
                                       HISTORY, MAX_ITER, TOL_GRAD),
-                       "l2": "flushed between steps (256 MiB write)"},
+                       "l2": "flushed between steps (256 MiB write)",
+                       "maps": "%d maps, %.0f MB" % (n_maps, n_maps * 81 ** 3 * 16 / 1e6),
+                       "l2_residency": args.l2_residency},
             "evals_per_s": ev / ms * 1e3, "evals_per_pose": ev / n,
             "autotuned_variants": {str(k): v for k, v in tuned.items()},
             "status_counts": {str(k): int((status == k).sum().item()) for k in range(4)}}
@@ -422,6 +428,8 @@ def run_screening_mc(args):
     types = sorted(set(int(t) for l in ligs for t in l.vdw_type))
     ctx.build_grid(box, types)
     ctx.set_slope(SLOPE)
+    if args.l2_residency:
+        ctx.set_l2_residency(args.l2_residency)
     ctx.set_scoring_function(0, pose_sf)
     ids = [ctx.add_ligand(l) for l in ligs]
     W = args.poses_per_ligand
@@ -450,7 +458,8 @@ def run_screening_mc(args):
             "config": {"workload": "screening with MC: %d ligands (%d-%d atoms, 0-%d torsions) x %d walkers x %d "
                                    "MC steps, relax <= %d L-BFGS iterations, 81^3 maps, one launch"
                                    % (len(ligs), min(l.n_atoms for l in ligs), max(l.n_atoms for l in ligs),
-                                      max(l.n_torsions for l in ligs), W, args.mc_steps, args.relax_steps)},
+                                      max(l.n_torsions for l in ligs), W, args.mc_steps, args.relax_steps),
+                       "l2_residency": args.l2_residency},
             "e2e": {"value": n * args.mc_steps / gpu_s, "unit": "walker-steps/s",
                     "h2d_bytes_per_step": int(starts.nbytes), "d2h_bytes_per_step": int(out["xyz"].nbytes + 24 * n)},
             "status_counts": {str(k): int((out["status"] == k).sum()) for k in range(3)}}
@@ -950,6 +959,9 @@ def main():
     ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
     ap.add_argument("--complexes", type=int, default=None,
                     help="differentiate / unroll: number of complexes (64 / 1024)")
+    ap.add_argument("--l2-residency", type=float, default=0.0,
+                    help="optimize / screening / screening_mc: fraction of the persisting L2 kept for the "
+                         "maps (pxd_set_l2_residency; 0: off)")
     ap.add_argument("--unroll-steps", type=int, default=50, help="unroll: L-BFGS steps")
     ap.add_argument("--unroll-truncate", type=int, default=None,
                     help="unroll: backpropagate through the last T steps only (default: all)")
@@ -1013,6 +1025,8 @@ def main():
     ctx.set_receptor(rec)
     ctx.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)))
     ctx.set_slope(SLOPE)
+    if args.l2_residency:
+        ctx.set_l2_residency(args.l2_residency)
     lid = ctx.add_ligand(lig)
     N = lig.n_atoms
     dev = torch.device("cuda", local)

@@ -616,6 +616,14 @@ int pxd_mc_search_multi(pxd_context* ctx, const pxd_mc_params* params, int32_t n
 int pxd_rng_draws(pxd_context* ctx, uint32_t seed, int32_t n, const int32_t* kinds,
                   const int32_t* ints, double* out);
 
+/* L2 residency of the maps (no reference counterpart; the loop it serves is
+ * receptor_cache::get, grid.cpp:197-303). Sets aside `fraction` (0..1) of the device's
+ * persisting-L2 capacity for this process and marks the context's map records as a
+ * persisting access-policy window on its optimiser and search launches; 0 turns it off.
+ * The set-aside is restored when the last context holding one turns it off or is
+ * destroyed, and ends with the process. Results are unchanged: only caching differs. */
+int pxd_set_l2_residency(pxd_context* ctx, double fraction);
+
 /* Measurement probe (no reference counterpart): the bandwidth of random 16-byte gathers
  * -- the access pattern of the map lookups inside receptor_cache::get (grid.cpp:273-303)
  * as the kernels make it -- over a working set of working_set_bytes (rounded down to a

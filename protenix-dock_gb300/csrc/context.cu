@@ -501,6 +501,7 @@ void pxd_context_destroy(pxd_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    release_l2_residency(ctx);
     pxd_clear_ligands(ctx);
     pxd_grid_drop(ctx);
     free_receptor(ctx);

@@ -15,10 +15,19 @@ struct LbfgsConsts {
     double lr, tol_grad, tol_change, c1, c2, ls_tol_change, gtd_threshold, reset;
 };
 
+// Warp-uniform scalars of the line search and the iteration, kept in the warp's shared
+// slice so that they are not live in registers across the out-of-line evaluation.
+struct LsState {
+    double t, f, fn, gtd, gn, tp, fp, gp, br0, br1, bf0, bf1, bgtd0, bgtd1, dn, loss, prev_loss, H_diag;
+    int it, lo, hi, insuf, done, base, count, pad;
+};
+constexpr int kLsFloats = (static_cast<int>(sizeof(LsState)) / 4 + 3) / 4 * 4;
+
 struct Vecs {
     float *x, *g, *gp, *d, *q, *sv, *gnew, *gprev, *bg0, *bg1;
     float *S, *Y;
     double *ro, *al;
+    LsState* ls;
 };
 
 // D_pad-long vectors in a warp's optimiser slice: x, g, gp, d and the line search's g_new,
@@ -36,7 +45,7 @@ __host__ __device__ constexpr int hist_slots(int m) { return m + 1; }
 
 // Floats of the FP64 two-loop scalars after the vectors: ro per physical slot (m + 1
 // doubles) and al per kept pair (m doubles), rounded up to 16 bytes.
-__host__ __device__ constexpr int opt_scalar_floats(int m) { return (2 * (2 * m + 1) + 3) / 4 * 4; }
+__host__ __device__ constexpr int opt_scalar_floats(int m) { return (2 * (2 * m + 1) + 3) / 4 * 4 + kLsFloats; }
 
 // Carves the vectors from vb (kOptVecs * Dp floats) and the FP64 two-loop scalars ro, al
 // (opt_scalar_floats(m) floats) after them.
@@ -54,6 +63,7 @@ __device__ __forceinline__ Vecs carve_vecs(float* vb, int Dp, int m) {
     v.sv = v.gnew;
     v.ro = reinterpret_cast<double*>(vb + kOptVecs * Dp);
     v.al = v.ro + hist_slots(m);
+    v.ls = reinterpret_cast<LsState*>(vb + kOptVecs * Dp + (2 * (2 * m + 1) + 3) / 4 * 4);
     v.S = v.Y = nullptr;
     return v;
 }
@@ -88,164 +98,126 @@ __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double
     return (lo + hi) / 2.0;
 }
 
-// The two ends of the line search's bracket (step, value, directional derivative,
-// gradient) as named scalars selected by index 0 / 1: no dynamically indexed local arrays.
-struct Bracket {
-    double br0 = 0.0, br1 = 0.0, bf0 = 0.0, bf1 = 0.0, bgtd0 = 0.0, bgtd1 = 0.0;
-    float *bg0, *bg1;
-    __device__ double br(int i) const { return i ? br1 : br0; }
-    __device__ double bf(int i) const { return i ? bf1 : bf0; }
-    __device__ double bgtd(int i) const { return i ? bgtd1 : bgtd0; }
-    __device__ float* bg(int i) const { return i ? bg1 : bg0; }
-    __device__ void set_br(int i, double x) {
-        if (i) br1 = x;
-        else br0 = x;
-    }
-    __device__ void set_bf(int i, double x) {
-        if (i) bf1 = x;
-        else bf0 = x;
-    }
-    __device__ void set_bgtd(int i, double x) {
-        if (i) bgtd1 = x;
-        else bgtd0 = x;
-    }
-};
-
 // strong_wolfe (optimizer.cpp:235-427); g holds the current gradient on entry and the
-// accepted one on exit.
-static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_io, const float* d,
-                             double& f_io, float* g, double gtd, const Vecs& v, int D,
-                             int lane) {
-    double t = t_io;
-    const double f = f_io;
+// accepted one on exit. Its scalars live in v.ls (shared memory).
+static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, const float* d, float* g,
+                                    const Vecs& v, int D, int lane) {
+    LsState& S = *v.ls;
     float* g_new = v.gnew;
     float* g_prev = v.gprev;
-    Bracket B;
-    B.bg0 = v.bg0;
-    B.bg1 = v.bg1;
-    double gtd_new = 0.0;
-    double f_new = closure_eval(c, t, d, g_new, &gtd_new);
-    if (isnan(f_new)) {
-        f_io = f_new;
+    S.f = S.loss;
+    S.fn = closure_eval(c, S.t, d, g_new, &S.gn);
+    if (isnan(S.fn)) {
+        S.loss = S.fn;
         return;
     }
-    if (fabs(gtd_new) > p.gtd_threshold) {
-        f_io = f_new;
+    if (fabs(S.gn) > p.gtd_threshold) {
+        S.loss = S.fn;
         vcopy(g, g_new, D, lane);
         return;
     }
-    double t_prev = 0.0, f_prev = f, gtd_prev = gtd;
+    S.tp = 0.0;
+    S.fp = S.f;
+    S.gp = S.gtd;
     // the previous trial's gradient: g itself until the first interpolation step
     const float* gpv = g;
-    int ls_iter = 0;
-    while (ls_iter < p.ls_max) {
-        if ((f_new > f + p.c1 * t * gtd) || (ls_iter > 1 && f_new >= f_prev)) {
-            B.br0 = t_prev; B.br1 = t; B.bf0 = f_prev; B.bf1 = f_new;
-            vcopy(B.bg0, gpv, D, lane);
-            vcopy(B.bg1, g_new, D, lane);
-            B.bgtd0 = gtd_prev; B.bgtd1 = gtd_new;
+    S.it = 0;
+    while (S.it < p.ls_max) {
+        if ((S.fn > S.f + p.c1 * S.t * S.gtd) || (S.it > 1 && S.fn >= S.fp)) {
+            S.br0 = S.tp; S.br1 = S.t; S.bf0 = S.fp; S.bf1 = S.fn;
+            vcopy(v.bg0, gpv, D, lane);
+            vcopy(v.bg1, g_new, D, lane);
+            S.bgtd0 = S.gp; S.bgtd1 = S.gn;
             break;
         }
-        if (fabs(gtd_new) <= -p.c2 * gtd) {
+        if (fabs(S.gn) <= -p.c2 * S.gtd) {
             // strong Wolfe holds at this trial: it is the accepted step
-            t_io = t;
-            f_io = f_new;
+            S.loss = S.fn;
             vcopy(g, g_new, D, lane);
             return;
         }
-        if (gtd_new >= 0.0) {
-            B.br0 = t_prev; B.br1 = t; B.bf0 = f_prev; B.bf1 = f_new;
-            vcopy(B.bg0, gpv, D, lane);
-            vcopy(B.bg1, g_new, D, lane);
-            B.bgtd0 = gtd_prev; B.bgtd1 = gtd_new;
+        if (S.gn >= 0.0) {
+            S.br0 = S.tp; S.br1 = S.t; S.bf0 = S.fp; S.bf1 = S.fn;
+            vcopy(v.bg0, gpv, D, lane);
+            vcopy(v.bg1, g_new, D, lane);
+            S.bgtd0 = S.gp; S.bgtd1 = S.gn;
             break;
         }
-        const double min_step = t + 0.01 * (t - t_prev);
-        const double max_step = t * 10.0;
-        const double tmp = t;
-        t = cubic_interpolate(t_prev, f_prev, gtd_prev, t, f_new, gtd_new, min_step, max_step);
-        t_prev = tmp;
-        f_prev = f_new;
+        const double min_step = S.t + 0.01 * (S.t - S.tp);
+        const double max_step = S.t * 10.0;
+        const double tmp = S.t;
+        S.t = cubic_interpolate(S.tp, S.fp, S.gp, S.t, S.fn, S.gn, min_step, max_step);
+        S.tp = tmp;
+        S.fp = S.fn;
         vcopy(g_prev, g_new, D, lane);
         gpv = g_prev;
-        gtd_prev = gtd_new;
-        f_new = closure_eval(c, t, d, g_new, &gtd_new);
-        ++ls_iter;
+        S.gp = S.gn;
+        S.fn = closure_eval(c, S.t, d, g_new, &S.gn);
+        ++S.it;
     }
-    double d_norm = 0.0;
-    if (ls_iter == p.ls_max) {
-        B.br0 = 0.0; B.br1 = t; B.bf0 = f; B.bf1 = f_new;
-        vcopy(B.bg0, g, D, lane);
-        vcopy(B.bg1, g_new, D, lane);
+    S.dn = 0.0;
+    if (S.it == p.ls_max) {
+        S.br0 = 0.0; S.br1 = S.t; S.bf0 = S.f; S.bf1 = S.fn;
+        vcopy(v.bg0, g, D, lane);
+        vcopy(v.bg1, g_new, D, lane);
     } else {
-        d_norm = vabsmax(d, D, lane);
+        S.dn = vabsmax(d, D, lane);
     }
-    bool insuf = false, done = false;
-    int lo = 0, hi = 1;
-    if (B.bf0 > B.bf1) {
-        lo = 1;
-        hi = 0;
-    }
-    while (!done && ls_iter < p.ls_max) {
+    S.insuf = 0;
+    S.done = 0;
+    S.lo = S.bf0 > S.bf1 ? 1 : 0;
+    S.hi = 1 - S.lo;
+    while (!S.done && S.it < p.ls_max) {
         double min_step, max_step;
-        if (B.br0 > B.br1) {
-            min_step = B.br1;
-            max_step = B.br0;
+        if (S.br0 > S.br1) {
+            min_step = S.br1;
+            max_step = S.br0;
         } else {
-            min_step = B.br0;
-            max_step = B.br1;
+            min_step = S.br0;
+            max_step = S.br1;
         }
         double eps = max_step - min_step;
-        if (eps * d_norm < p.ls_tol_change) break;
-        t = cubic_interpolate(B.br0, B.bf0, B.bgtd0, B.br1, B.bf1, B.bgtd1, min_step, max_step);
+        if (eps * S.dn < p.ls_tol_change) break;
+        double t = cubic_interpolate(S.br0, S.bf0, S.bgtd0, S.br1, S.bf1, S.bgtd1, min_step, max_step);
         eps *= 0.1;
         if (fmin(max_step - t, t - min_step) < eps) {
-            if (insuf || t >= max_step || t <= min_step) {
+            if (S.insuf || t >= max_step || t <= min_step) {
                 if (fabs(t - max_step) < fabs(t - min_step))
                     t = max_step - eps;
                 else
                     t = min_step + eps;
-                insuf = false;
+                S.insuf = 0;
             } else {
-                insuf = true;
+                S.insuf = 1;
             }
         } else {
-            insuf = false;
+            S.insuf = 0;
         }
-        f_new = closure_eval(c, t, d, g_new, &gtd_new);
-        ++ls_iter;
-        if (f_new > (f + p.c1 * t * gtd) || f_new >= B.bf(lo)) {
-            B.set_br(hi, t);
-            B.set_bf(hi, f_new);
-            vcopy(B.bg(hi), g_new, D, lane);
-            B.set_bgtd(hi, gtd_new);
-            if (B.bf0 > B.bf1) {
-                lo = 1;
-                hi = 0;
-            } else {
-                lo = 0;
-                hi = 1;
-            }
+        S.t = t;
+        S.fn = closure_eval(c, S.t, d, g_new, &S.gn);
+        ++S.it;
+        const int lo = S.lo, hi = S.hi;
+        const double bf_lo = lo ? S.bf1 : S.bf0;
+        if (S.fn > (S.f + p.c1 * S.t * S.gtd) || S.fn >= bf_lo) {
+            if (hi) { S.br1 = S.t; S.bf1 = S.fn; S.bgtd1 = S.gn; } else { S.br0 = S.t; S.bf0 = S.fn; S.bgtd0 = S.gn; }
+            vcopy(hi ? v.bg1 : v.bg0, g_new, D, lane);
+            S.lo = S.bf0 > S.bf1 ? 1 : 0;
+            S.hi = 1 - S.lo;
         } else {
-            if (fabs(gtd_new) <= -p.c2 * gtd) {
-                done = true;
-            } else if (gtd_new * (B.br(hi) - B.br(lo)) >= 0.0) {
-                B.set_br(hi, B.br(lo));
-                B.set_bf(hi, B.bf(lo));
-                vcopy(B.bg(hi), B.bg(lo), D, lane);
-                B.set_bgtd(hi, B.bgtd(lo));
+            if (fabs(S.gn) <= -p.c2 * S.gtd) {
+                S.done = 1;
+            } else if (S.gn * ((hi ? S.br1 : S.br0) - (lo ? S.br1 : S.br0)) >= 0.0) {
+                if (hi) { S.br1 = S.br0; S.bf1 = S.bf0; S.bgtd1 = S.bgtd0; } else { S.br0 = S.br1; S.bf0 = S.bf1; S.bgtd0 = S.bgtd1; }
+                vcopy(hi ? v.bg1 : v.bg0, lo ? v.bg1 : v.bg0, D, lane);
             }
-            B.set_br(lo, t);
-            B.set_bf(lo, f_new);
-            vcopy(B.bg(lo), g_new, D, lane);
-            B.set_bgtd(lo, gtd_new);
+            if (lo) { S.br1 = S.t; S.bf1 = S.fn; S.bgtd1 = S.gn; } else { S.br0 = S.t; S.bf0 = S.fn; S.bgtd0 = S.gn; }
+            vcopy(lo ? v.bg1 : v.bg0, g_new, D, lane);
         }
     }
-    t_io = B.br(lo);
-    f_io = B.bf(lo);
-    vcopy(g, B.bg(lo), D, lane);
+    S.t = S.lo ? S.br1 : S.br0;
+    S.loss = S.lo ? S.bf1 : S.bf0;
+    vcopy(g, S.lo ? v.bg1 : v.bg0, D, lane);
 }
-
 
 // lbfgs_step::apply (optimizer.cpp:429-560) on the pose held in v.x; returns status.
 //
@@ -259,7 +231,8 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, double& t_
 //   - the second loop: d += (al_k - be_k) s_k fused with the next y_{k+1} . d, the last
 //     step with g . d for the line search.
 // Kept pairs sit in physical slots (base + j) % (m + 1), j = 0 .. count - 1 oldest first;
-// the spare slot (base + count) % (m + 1) receives the next pair.
+// the spare slot (base + count) % (m + 1) receives the next pair. The iteration's scalars
+// (loss, step, H_diag, the history ring) live with the line search's in v.ls.
 //
 // energy receives the FP64 objective at the returned pose (energy64), or, with
 // final_energy false (a caller that does not use it), the last FP32 loss.
@@ -270,24 +243,27 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
     const int max_eval = p.max_eval > 0 ? p.max_eval : p.max_iter * 5 / 4;
     c.x0 = v.x;
     c.nevals = 0;
-    double loss = closure_eval(c, 0.0, nullptr, v.g);
+    LsState& S = *v.ls;
+    S.loss = closure_eval(c, 0.0, nullptr, v.g);
     if (vabsmax(v.g, D, lane) < p.tol_grad) {
-        energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : loss;
+        energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : S.loss;
         return PXD_POSE_CONVERGED;
     }
     int status = PXD_POSE_NOT_CONVERGED;
-    int base = 0, count = 0;
-    double H_diag = 1.0, t = 0.0, prev_loss;
+    S.base = 0;
+    S.count = 0;
+    S.H_diag = 1.0;
+    S.t = 0.0;
     int n_iter = 0;
     bool updated = false;
     while (n_iter < p.max_iter && c.nevals < max_eval) {
         ++n_iter;
         bool reset = n_iter == 1;
         if (!reset) {
-            const int spare = (base + count) % slots;
+            const int spare = (S.base + S.count) % slots;
             float* ys_ = v.Y + spare * Dp;
             float* ss_ = v.S + spare * Dp;
-            const float tf = static_cast<float>(t);
+            const float tf = static_cast<float>(S.t);
             float ymax = 0.f;
             DS a_ys{0.f, 0.f}, a_yy{0.f, 0.f};
             for (int e = lane; e < D; e += kWarp) {
@@ -304,24 +280,24 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
                 const double ys = ds_warp_sum(a_ys);
                 const double yy = ds_warp_sum(a_yy);
                 if (ys > 1e-10) {
-                    if (count == m)
-                        base = (base + 1) % slots;  // the oldest slot becomes the spare
+                    if (S.count == m)
+                        S.base = (S.base + 1) % slots;  // the oldest slot becomes the spare
                     else
-                        ++count;
-                    H_diag = ys / yy;
+                        ++S.count;
+                    S.H_diag = ys / yy;
                     if (lane == 0) v.ro[spare] = 1.0 / ys;
                 }
             }
             __syncwarp();
         }
         double gtd;
-        if (reset || count == 0) {
+        if (reset || S.count == 0) {
             // d = -H_diag g (H_diag = 1 after a reset), g_prev = g, g . d and |g|_1
             if (reset) {
-                base = count = 0;
-                H_diag = 1.0;
+                S.base = S.count = 0;
+                S.H_diag = 1.0;
             }
-            const float hd = static_cast<float>(H_diag);
+            const float hd = static_cast<float>(S.H_diag);
             DS acc{0.f, 0.f}, a_abs{0.f, 0.f};
             for (int e = lane; e < D; e += kWarp) {
                 const float ge = v.g[e];
@@ -335,15 +311,15 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
             gtd = ds_warp_sum(acc);
             if (reset) {
                 const double inv = 1.0 / ds_warp_sum(a_abs);
-                t = fmin(1.0, inv) * p.lr * 0.1;
+                S.t = fmin(1.0, inv) * p.lr * 0.1;
             } else {
-                t = p.lr;
+                S.t = p.lr;
             }
         } else {
             // first loop, newest to oldest: q = -g - sum al_k y_k
             DS acc{0.f, 0.f};
             {
-                const float* sk = v.S + ((base + count - 1) % slots) * Dp;
+                const float* sk = v.S + ((S.base + S.count - 1) % slots) * Dp;
                 for (int e = lane; e < D; e += kWarp) {
                     const float ge = v.g[e];
                     v.q[e] = -ge;
@@ -351,15 +327,15 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
                     ds_dot_acc(acc, sk[e], -ge);
                 }
             }
-            for (int k = count - 1; k >= 0; --k) {
-                const int sl = (base + k) % slots;
+            for (int k = S.count - 1; k >= 0; --k) {
+                const int sl = (S.base + k) % slots;
                 const double al = ds_warp_sum(acc) * v.ro[sl];
                 if (lane == 0) v.al[k] = al;
                 const float nal = static_cast<float>(-al);
                 const float* yk = v.Y + sl * Dp;
                 acc = DS{0.f, 0.f};
                 if (k > 0) {
-                    const float* sn = v.S + ((base + k - 1) % slots) * Dp;
+                    const float* sn = v.S + ((S.base + k - 1) % slots) * Dp;
                     for (int e = lane; e < D; e += kWarp) {
                         const float qe = fmaf(yk[e], nal, v.q[e]);
                         v.q[e] = qe;
@@ -367,7 +343,7 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
                     }
                 } else {
                     // the last update, then d = H_diag q and the second loop's first dot
-                    const float hd = static_cast<float>(H_diag);
+                    const float hd = static_cast<float>(S.H_diag);
                     for (int e = lane; e < D; e += kWarp) {
                         const float de = fmaf(yk[e], nal, v.q[e]) * hd;
                         v.d[e] = de;
@@ -377,12 +353,12 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
                 __syncwarp();
             }
             // second loop, oldest to newest: d += (al_k - be_k) s_k
-            for (int k = 0; k < count; ++k) {
-                const int sl = (base + k) % slots;
+            for (int k = 0; k < S.count; ++k) {
+                const int sl = (S.base + k) % slots;
                 const double be = ds_warp_sum(acc) * v.ro[sl];
                 const float w = static_cast<float>(v.al[k] - be);
                 const float* sk = v.S + sl * Dp;
-                const float* nx = k + 1 < count ? v.Y + ((base + k + 1) % slots) * Dp : v.g;
+                const float* nx = k + 1 < S.count ? v.Y + ((S.base + k + 1) % slots) * Dp : v.g;
                 acc = DS{0.f, 0.f};
                 for (int e = lane; e < D; e += kWarp) {
                     const float de = fmaf(sk[e], w, v.d[e]);
@@ -392,21 +368,22 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
                 __syncwarp();
             }
             gtd = ds_warp_sum(acc);  // g . d after the last step
-            t = p.lr;
+            S.t = p.lr;
         }
-        prev_loss = loss;
+        S.prev_loss = S.loss;
         if (gtd > -p.tol_change) {
             status = PXD_POSE_CONVERGED;
             break;
         }
         Vecs w = v;
-        strong_wolfe(c, p, t, v.d, loss, v.g, gtd, w, D, lane);
-        if (isnan(loss)) {
+        S.gtd = gtd;
+        strong_wolfe(c, p, v.d, v.g, w, D, lane);
+        if (isnan(S.loss)) {
             status = PXD_POSE_NAN;
             break;
         }
         // x += t d, with max|g| and max|t d| for the convergence tests
-        const float tf = static_cast<float>(t);
+        const float tf = static_cast<float>(S.t);
         float gmax = 0.f, smax = 0.f;
         for (int e = lane; e < D; e += kWarp) {
             const float de = v.d[e];
@@ -424,7 +401,7 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
             status = PXD_POSE_CONVERGED;
             break;
         }
-        if (fabs(loss - prev_loss) < p.tol_change) {
+        if (fabs(S.loss - S.prev_loss) < p.tol_change) {
             status = PXD_POSE_CONVERGED;
             break;
         }
@@ -432,7 +409,7 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
     // the reported energy: the FP64 objective at the returned pose; an optimisation that
     // moved counts it as its final evaluation, as the reference does (optimizer.cpp:552-556)
     if (updated) ++c.nevals;
-    energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : loss;
+    energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : S.loss;
     return status;
 }
 

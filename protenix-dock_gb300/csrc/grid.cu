@@ -15,8 +15,10 @@
 // The energy channel is also kept in FP64 for the final FP64 energy of a pose: every LJ
 // pair term above kFp64Term kcal/mol in magnitude is recomputed in FP64 from FP64 sigma,
 // epsilon and coordinates (an FP32 term carries ~1e-6 of its size, 100 kcal/mol on a
-// 1e8 clash), the smaller ones stay FP32 (each under 1e-9 kcal/mol of rounding), and the
-// record's energy is the FP64 sum rounded to FP32 with the remainder stored in e_lo.
+// 1e8 clash), the smaller ones stay FP32 (each under ~1e-8 kcal/mol of rounding, ~1e-6
+// over a point's atoms), and the record's energy is the FP64 sum rounded to FP32 with the
+// remainder stored in e_lo. The FP64 terms (atoms within ~6.5 A of the point) bound the
+// build by the FP64 pipe.
 #include "device_eval.cuh"
 #include "../../include/pxdock_gb300_vdw.h"
 
@@ -27,7 +29,7 @@ constexpr int kGridTile = 256;
 constexpr float kR2Floor = 1e-4f;
 constexpr double kRecordCeil = 1e30;
 constexpr double kCoulombD = 332.0637141491396;  // kCoulombFactor, system.h:83
-constexpr float kFp64Term = 1e-3f;
+constexpr float kFp64Term = 1e-2f;
 
 struct GridArgs {
     const float4* atoms;   // x, y, z, charge of every non-rotor receptor atom (FP32 hi part)

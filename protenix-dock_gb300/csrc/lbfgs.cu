@@ -520,8 +520,9 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
             a.order = counters + 2 * n_cls + k * static_cast<size_t>(n_poses);
             ks = ctx->class_streams[k];
         }
-        plan[k].kern<<<plan[k].blocks, kWarpsPerBlock * kWarp, plan[k].smem, ks>>>(a);
-        rc = cuda_check(ctx, cudaGetLastError(), "lbfgs_kernel launch");
+        rc = cuda_check(ctx, launch_with_map_window(ctx, plan[k].kern, plan[k].blocks, kWarpsPerBlock * kWarp,
+                                                    plan[k].smem, ks, a),
+                        "lbfgs_kernel launch");
         if (!rc && classes) rc = class_join(ctx, k, s);
         if (rc) return rc;
     }

@@ -604,8 +604,8 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(int), s), "counter reset");
     if (rc) return rc;
-    mc_kernel<<<blocks, wpb * kWarp, smem, s>>>(a);
-    return cuda_check(ctx, cudaGetLastError(), "mc_kernel launch");
+    return cuda_check(ctx, launch_with_map_window(ctx, mc_kernel, blocks, wpb * kWarp, smem, s, a),
+                      "mc_kernel launch");
 }
 
 int pxd_mc_search(pxd_context* ctx, const pxd_mc_params* p, int32_t lig, int32_t n, const int32_t* walker_ids,

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/pxdock_gb300.h"
@@ -218,6 +219,10 @@ struct pxd_context {
     bool sf_set[2] = {false, false};
     // autotuned L-BFGS variant (minimum resident blocks per SM) per size-class bound
     std::map<int, int> lbfgs_tuned;
+    // L2 residency of the maps (pxd_set_l2_residency): persisting set-aside this context
+    // holds (0: off) and the device's largest access-policy window
+    size_t l2_setaside = 0;
+    size_t l2_max_window = 0;
     // scratch
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -249,6 +254,28 @@ int launch_size_classes(pxd_context* ctx, int n_items, const int* lig_ids, const
 // Fork: the class streams wait for what s has queued. Join: s waits for class k's stream.
 int class_fork(pxd_context* ctx, size_t n_cls, cudaStream_t s);
 int class_join(pxd_context* ctx, size_t k, cudaStream_t s);
+
+// L2 residency (residency.cu): the access-policy window over the context's map records
+// when residency control is on (*on false otherwise), and the release of its set-aside.
+cudaLaunchAttribute map_window(const pxd_context* ctx, bool* on);
+int release_l2_residency(pxd_context* ctx);
+
+// Launches kern<<<grid, block, smem, s>>>(args) with the map window attached when the
+// context has residency control on; a plain launch otherwise.
+template <class... KArgs, class... Args>
+cudaError_t launch_with_map_window(const pxd_context* ctx, void (*kern)(KArgs...), dim3 grid, dim3 block,
+                                   size_t smem, cudaStream_t s, Args&&... args) {
+    bool on = false;
+    cudaLaunchAttribute attr = map_window(ctx, &on);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = on ? &attr : nullptr;
+    cfg.numAttrs = on ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // kernels (launchers), one per translation unit
 int launch_grid_build(pxd_context* ctx, const float4* atoms_xyzq, const float4* atoms_lo,

@@ -80,6 +80,7 @@ def load(auto_build=False):
                                         abi.f64p, abi.i32p, abi.i32p, abi.f64p]
     lib.pxd_rng_draws.argtypes = [vp, C.c_uint32, C.c_int32, abi.i32p, abi.i32p, abi.f64p]
     lib.pxd_gather_bandwidth.argtypes = [C.c_int32, C.c_int64, C.c_int32, abi.f64p]
+    lib.pxd_set_l2_residency.argtypes = [vp, C.c_double]
     lib.pxd_sf_weights.argtypes = [C.POINTER(abi.SfParams), abi.f64p]
     lib.pxd_sf_weights.restype = None
     lib.pxd_score_adjoint_dev.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32] + [vp] * 12
@@ -286,6 +287,11 @@ class Context:
         self._check(self.lib.pxd_score_grad_dev(self.h, n_poses, max_atoms, ids_ptr, xyz_ptr,
                                                 tors_ptr, energy_ptr, lig_grad_ptr, tors_grad_ptr,
                                                 stream))
+
+    def set_l2_residency(self, fraction):
+        """pxd_set_l2_residency: keep `fraction` of the persisting L2 for this context's
+        maps on its optimiser and search launches (0 turns it off)."""
+        self._check(self.lib.pxd_set_l2_residency(self.h, float(fraction)))
 
     def lbfgs_dev(self, params, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
                   nevals_ptr, status_ptr, stream=None):
