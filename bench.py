@@ -74,10 +74,10 @@ def config_dict(lig, box, world=1):
     }
 
 
-def lbfgs_params():
+def lbfgs_params(dof_mode=0):
     from pxdock_gb300 import native
 
-    return native.lbfgs_params(max_iter=MAX_ITER, history=HISTORY, tolerance_grad=TOL_GRAD)
+    return native.lbfgs_params(max_iter=MAX_ITER, history=HISTORY, tolerance_grad=TOL_GRAD, dof_mode=dof_mode)
 
 
 class Clocks:
@@ -233,9 +233,22 @@ def screening_ligands(n, seed=3):
     rotatable bonds U{0..15}, C 70 % / N 12 % / O 15 % / Cl 3 %), built on all host cores.
     Ligands the device path does not take (over 256 atoms, 32 torsions or 64 fragments) are
     skipped like draws the generator cannot embed."""
+    import hashlib
+
     from pxdock_gb300 import model, synth
 
-    return [model.Ligand.from_json(lj) for lj in synth.screening_set(n, seed, cpu_threads(), _screening_accept)]
+    # a set generated once on this host is kept in the temp directory, keyed by the
+    # generator's source, so that several runs on one host build it once
+    digest = hashlib.sha256(open(synth.__file__, "rb").read()).hexdigest()[:12]
+    path = os.path.join(tempfile.gettempdir(), "pxdock_screening_%d_%d_%s.json" % (n, seed, digest))
+    if os.path.exists(path):
+        js = json.load(open(path))
+    else:
+        js = synth.screening_set(n, seed, cpu_threads(), _screening_accept)
+        tmp = path + ".%d" % os.getpid()
+        json.dump(js, open(tmp, "w"))
+        os.replace(tmp, path)
+    return [model.Ligand.from_json(lj) for lj in js]
 
 
 def _screening_accept(lj):
@@ -956,6 +969,9 @@ def main():
     ap.add_argument("--workload", default="optimize", choices=["optimize", "evaluate", "screening", "screening_mc", "docking", "differentiate", "unroll"],
                     help="optimize: the headline (one ligand, 65,536 poses); screening: uneven "
                          "ligands batched in one launch")
+    ap.add_argument("--dof-mode", type=int, default=0, choices=[0, 1],
+                    help="optimize: L-BFGS variables, 0 ligand xyz + receptor torsions (the reference's), "
+                         "1 rigid body + torsions (no CPU baseline leg)")
     ap.add_argument("--ligands", type=int, default=64, help="screening: number of ligands")
     ap.add_argument("--complexes", type=int, default=None,
                     help="differentiate / unroll: number of complexes (64 / 1024)")
@@ -1038,7 +1054,7 @@ def main():
     nevals = torch.zeros(N_POSES, dtype=torch.int32, device=dev)
     status = torch.zeros(N_POSES, dtype=torch.int32, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    p = lbfgs_params()
+    p = lbfgs_params(args.dof_mode)
     stream = torch.cuda.Stream(dev)
     sptr = stream.cuda_stream
 
@@ -1111,7 +1127,9 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": float(np.mean(kernel_ms)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": config_dict(lig, box, world),
+        "config": dict(config_dict(lig, box, world),
+                       variables="ligand xyz + receptor torsions (the reference's)" if not args.dof_mode else
+                       "rigid body + torsions: centre, quaternion, %d ligand torsions" % lig.n_torsions),
         "e2e": {"value": e2e_value, "unit": UNIT,
                 # pxd_lbfgs copies the caller's FP64 coordinates both ways (narrowed to FP32
                 # on the device) and returns energy (FP64), evaluations and status per pose
@@ -1145,7 +1163,7 @@ def main():
         line["issue"] = {"warp_instructions_per_eval": wipe, "achieved": rate, "peak": peak_issue,
                          "unit": "warp instructions/s", "frac": rate / peak_issue,
                          "sm_mhz": mhz, "sms": n_sm}
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not args.dof_mode:
         import oracle
 
         keep = {}

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define PXD_ABI_VERSION 1
+#define PXD_ABI_VERSION 2
 
 /* ------------------------------------------------------------------ status */
 enum pxd_status_code {
@@ -223,7 +223,27 @@ typedef struct pxd_lbfgs_params {
     double ls_tolerance_change;  /* 1e-9 */
     double ls_gtd_threshold;     /* 1e5 */
     double reset_threshold;      /* 1e8: history is dropped when max|y| exceeds it */
+    int32_t dof_mode;            /* PXD_DOF_CARTESIAN (0, the reference) or PXD_DOF_RIGID_TORSION */
+    int32_t reserved;            /* 0 */
 } pxd_lbfgs_params;
+
+/* Variables of the batched optimiser (pxd_lbfgs_params.dof_mode).
+ *   PXD_DOF_CARTESIAN       [ligand xyz (3N) | receptor torsions (R)], the reference's
+ *                           flat closure (optimizer.cpp:155-167);
+ *   PXD_DOF_RIGID_TORSION   [centre (3) | quaternion (4) | ligand torsions (T) | receptor
+ *                           torsions (R)], D = 7 + T + R (no reference counterpart). The
+ *                           ligand is placed from the pose's own input coordinates by the
+ *                           torsion-tree forward map (free_ligand::apply_parameters,
+ *                           data.cpp:592-641) starting at centre = the input's geometric
+ *                           centre, identity orientation and zero torsion changes, so bond
+ *                           lengths and angles keep their input values; the gradient is
+ *                           the Cartesian one pulled back through the tree. The returned
+ *                           pose is the placed Cartesian pose. Ligands need <= 32 torsions
+ *                           and <= 64 fragments (else the pose's status is
+ *                           PXD_POSE_BAD_INPUT). Applies to pxd_lbfgs*, not to the
+ *                           Monte-Carlo search (PXD_ERR_INVALID there). */
+#define PXD_DOF_CARTESIAN 0
+#define PXD_DOF_RIGID_TORSION 1
 
 #define PXD_MAX_HISTORY 128
 
@@ -659,6 +679,9 @@ int pxd_engine_evaluate(pxd_engine* engine, const char* ligand_index_file, const
 /* optimize: L-BFGS of every pose (max_niters, slope), pose_ranker output per ligand */
 int pxd_engine_optimize(pxd_engine* engine, const char* ligand_index_file, const char* output_dir,
                         int32_t max_niters, double slope);
+/* Variables of optimize's L-BFGS for this engine's later optimize calls (no reference
+ * counterpart): PXD_DOF_CARTESIAN (default, the reference's) or PXD_DOF_RIGID_TORSION. */
+int pxd_engine_set_dof_mode(pxd_engine* engine, int32_t dof_mode);
 /* search: exhaustiveness Monte-Carlo walkers per ligand, pose_cluster output per ligand */
 int pxd_engine_search(pxd_engine* engine, const char* ligand_index_file, const char* output_dir,
                       int32_t seed, int32_t exhaustiveness, int32_t max_nsteps, int32_t relax_nsteps,
@@ -675,6 +698,21 @@ int pxd_write_poses(const char* path, const char* smiles, int32_t best_id, doubl
                     const double* pscore, const int64_t* nevals, int32_t n_rotors,
                     const double* torsions, const double* xyz, const int32_t* bond_mappings,
                     int32_t num_rotatable_bonds);
+/* pose_cluster::preprocess (writer.cpp:99-177) for many ligands in one launch, one warp per
+ * ligand: group g's candidates are poses group_start[g] .. group_start[g + 1] - 1 of xyz
+ * ([poses][stride_atoms][3]), of which the first group_atoms[g] atoms count. kept
+ * ([n_groups][num_modes]) receives each group's kept pose indices, best pose score first,
+ * -1 past n_kept[g]; num_modes at most 32. The kept lists are those of pxd_cluster_poses.
+ * The _dev form takes device buffers on `stream`; the _batch form host buffers (xyz as
+ * double, FP32-representable as search outputs are). */
+int pxd_cluster_poses_dev(pxd_context* ctx, int32_t n_groups, const int32_t* group_start,
+                          const int32_t* group_atoms, int32_t stride_atoms, const float* xyz,
+                          const double* pscore, const int32_t* nevals, int32_t num_modes, double min_rmsd,
+                          int32_t* kept, int32_t* n_kept, void* stream);
+int pxd_cluster_poses_batch(pxd_context* ctx, int32_t n_groups, const int32_t* group_start,
+                            const int32_t* group_atoms, int32_t stride_atoms, const double* xyz,
+                            const double* pscore, const int32_t* nevals, int32_t num_modes, double min_rmsd,
+                            int32_t* kept, int32_t* n_kept);
 int pxd_cluster_poses(int32_t n_poses, int32_t n_atoms, const double* xyz, const double* pscore,
                       const int64_t* nevals, int32_t num_modes, double min_rmsd, int32_t* kept,
                       int32_t* n_kept);

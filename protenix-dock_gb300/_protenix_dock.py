@@ -47,6 +47,7 @@ def _lib():
         lib.pxd_engine_drop_maps.argtypes = [vp]
         lib.pxd_engine_evaluate.argtypes = [vp, cp, cp]
         lib.pxd_engine_optimize.argtypes = [vp, cp, cp, i32, d]
+        lib.pxd_engine_set_dof_mode.argtypes = [vp, i32]
         lib.pxd_engine_search.argtypes = [vp, cp, cp, i32, i32, i32, i32, i32, d, d, d]
         lib.pxd_engine_log2file.argtypes = [cp, i32]
         f64p, i32p, i64p = C.POINTER(d), C.POINTER(i32), C.POINTER(C.c_int64)
@@ -133,7 +134,11 @@ class ReusableEngine:
         finally:
             os.unlink(path)
 
-    def optimize(self, ligand_index_file, output_dir, max_niters=240, slope=1e6, rank=0, world=1):
+    def optimize(self, ligand_index_file, output_dir, max_niters=240, slope=1e6, rank=0, world=1, dof_mode=0):
+        """dof_mode 0: L-BFGS over ligand coordinates and receptor torsions (the reference);
+        1: over rigid body + ligand torsions + receptor torsions (bond lengths and angles
+        keep their input values)."""
+        self._call(self._lib.pxd_engine_set_dof_mode, dof_mode)
         self._sharded(ligand_index_file, rank, world, None,
                       lambda idx: self._call(self._lib.pxd_engine_optimize, _b(idx), _b(output_dir),
                                              max_niters, slope))

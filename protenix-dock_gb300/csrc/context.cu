@@ -538,6 +538,8 @@ void pxd_lbfgs_defaults(pxd_lbfgs_params* p) {
     p->ls_tolerance_change = 1e-9;
     p->ls_gtd_threshold = 1e5;
     p->reset_threshold = 1e8;
+    p->dof_mode = PXD_DOF_CARTESIAN;
+    p->reserved = 0;
 }
 
 int pxd_set_receptor(pxd_context* ctx, const pxd_receptor_desc* r) {
@@ -1085,7 +1087,8 @@ int pxd_lbfgs_dev(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n_poses, 
                   int32_t* status, void* stream) {
     int rc = check_ready(ctx);
     if (rc) return rc;
-    if (!p || p->history < 1 || p->history > PXD_MAX_HISTORY || p->max_iter < 0 || p->ls_max < 1)
+    if (!p || p->history < 1 || p->history > PXD_MAX_HISTORY || p->max_iter < 0 || p->ls_max < 1 ||
+        (p->dof_mode != PXD_DOF_CARTESIAN && p->dof_mode != PXD_DOF_RIGID_TORSION))
         return set_error(ctx, PXD_ERR_INVALID, "bad L-BFGS parameters");
     if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS)
         return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");
@@ -1098,7 +1101,8 @@ int pxd_lbfgs_dev_noalloc(pxd_context* ctx, const pxd_lbfgs_params* p, int32_t n
                           int32_t* status, void* stream) {
     int rc = check_ready(ctx);
     if (rc) return rc;
-    if (!p || p->history < 1 || p->history > PXD_MAX_HISTORY || p->max_iter < 0 || p->ls_max < 1)
+    if (!p || p->history < 1 || p->history > PXD_MAX_HISTORY || p->max_iter < 0 || p->ls_max < 1 ||
+        (p->dof_mode != PXD_DOF_CARTESIAN && p->dof_mode != PXD_DOF_RIGID_TORSION))
         return set_error(ctx, PXD_ERR_INVALID, "bad L-BFGS parameters");
     if (n_poses < 0 || max_atoms <= 0 || max_atoms > PXD_MAX_LIGAND_ATOMS)
         return set_error(ctx, PXD_ERR_INVALID, "bad pose batch shape");

@@ -31,6 +31,18 @@ __device__ __forceinline__ Mat3 matmul(const Mat3& a, const Mat3& b) {
     return m;
 }
 
+// Rotation matrix of the quaternion q4 = (w, x, y, z) after normalisation
+// (get_rotation_matrix, math.cpp:22-42).
+__device__ __forceinline__ Mat3 unit_quat_rotation(const float* q4) {
+    const float inv = rsqrtf(q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
+    const float a = q4[0] * inv, b = q4[1] * inv, c = q4[2] * inv, d = q4[3] * inv;
+    Mat3 m;
+    m.r0 = make_float3(a * a + b * b - c * c - d * d, 2.f * (b * c - a * d), 2.f * (a * c + b * d));
+    m.r1 = make_float3(2.f * (a * d + b * c), a * a - b * b + c * c - d * d, 2.f * (c * d - a * b));
+    m.r2 = make_float3(2.f * (b * d - a * c), 2.f * (a * b + c * d), a * a - b * b - c * c + d * d);
+    return m;
+}
+
 struct KinShared {
     Mat3 fused[kMaxFrags];
     float3 origin[kMaxFrags];

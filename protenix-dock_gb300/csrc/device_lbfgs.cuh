@@ -83,6 +83,11 @@ __device__ __forceinline__ double closure_eval(Closure& c, double t, const float
     return eval_pose(*c.env, *c.L, c.x0, d, static_cast<float>(t), g, *c.b, c.lane, gdot);
 }
 
+// FP64 objective at the optimiser's variables x (the reported energy).
+__device__ __forceinline__ double closure_energy64(Closure& c, const float* x) {
+    return energy64(*c.env, *c.L, x, *c.b, c.lane);
+}
+
 __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double g1, double x2,
                                                     double f2, double g2, double lo, double hi) {
     double d1 = g1 + g2 - 3.0 * (f1 - f2) / (x1 - x2);
@@ -99,8 +104,10 @@ __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double
 }
 
 // strong_wolfe (optimizer.cpp:235-427); g holds the current gradient on entry and the
-// accepted one on exit. Its scalars live in v.ls (shared memory).
-static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, const float* d, float* g,
+// accepted one on exit. Its scalars live in v.ls (shared memory). Cl is the closure over
+// the variables: Closure (Cartesian) or DofClosure (rigid body + torsions).
+template <class Cl>
+static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d, float* g,
                                     const Vecs& v, int D, int lane) {
     LsState& S = *v.ls;
     float* g_new = v.gnew;
@@ -236,7 +243,8 @@ static __device__ void strong_wolfe(Closure& c, const LbfgsConsts& p, const floa
 //
 // energy receives the FP64 objective at the returned pose (energy64), or, with
 // final_energy false (a caller that does not use it), the last FP32 loss.
-static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v, int D,
+template <class Cl>
+static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int D,
                           size_t Dp, int lane, double& energy, bool final_energy = true) {
     const int m = p.m;
     const int slots = hist_slots(m);
@@ -246,7 +254,7 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
     LsState& S = *v.ls;
     S.loss = closure_eval(c, 0.0, nullptr, v.g);
     if (vabsmax(v.g, D, lane) < p.tol_grad) {
-        energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : S.loss;
+        energy = final_energy ? closure_energy64(c, v.x) : S.loss;
         return PXD_POSE_CONVERGED;
     }
     int status = PXD_POSE_NOT_CONVERGED;
@@ -409,7 +417,7 @@ static __device__ int lbfgs_pose(Closure& c, const LbfgsConsts& p, const Vecs& v
     // the reported energy: the FP64 objective at the returned pose; an optimisation that
     // moved counts it as its final evaluation, as the reference does (optimizer.cpp:552-556)
     if (updated) ++c.nevals;
-    energy = final_energy ? energy64(*c.env, *c.L, v.x, *c.b, lane) : S.loss;
+    energy = final_energy ? closure_energy64(c, v.x) : S.loss;
     return status;
 }
 

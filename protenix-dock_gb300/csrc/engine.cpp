@@ -410,6 +410,12 @@ void Engine::evaluate(const std::string& ligand_index_file, const std::string& o
     log(1, "Number of successful evaluations is: " + std::to_string(n_out));
 }
 
+void Engine::set_dof_mode(int mode) {
+    if (mode != PXD_DOF_CARTESIAN && mode != PXD_DOF_RIGID_TORSION)
+        throw std::runtime_error("dof_mode must be 0 (Cartesian) or 1 (rigid body + torsions)");
+    dof_mode_ = mode;
+}
+
 void Engine::optimize(const std::string& ligand_index_file, const std::string& output_dir, int max_niters, double slope) {
     if (has_maps_)
         check(ctx_, pxd_grid_set_slope(ctx_, slope));
@@ -437,6 +443,7 @@ void Engine::optimize(const std::string& ligand_index_file, const std::string& o
     pxd_lbfgs_params prm;
     pxd_lbfgs_defaults(&prm);
     prm.max_iter = max_niters;
+    prm.dof_mode = dof_mode_;
     if (n_total) check(ctx_, pxd_lbfgs_multi(ctx_, &prm, static_cast<int32_t>(n_total), max_atoms, ids.data(), xyz.data(),
                                               tors.data(), energy.data(), nev.data(), st.data()));
     row = 0;
@@ -528,9 +535,26 @@ void Engine::search(const std::string& ligand_index_file, const std::string& out
     check(ctx_, pxd_mc_search_multi(ctx_, &prm, static_cast<int32_t>(W), max_atoms, ids.data(), walker.data(),
                                     first.data(), start.data(), out.data(), tors.data(), energy.data(), ps.data(),
                                     nev.data(), st.data(), gmin.data()));
+    // clustering of every ligand's walkers in one launch (num_modes <= 32; beyond, the same
+    // rule runs on the host per ligand)
+    const int n_l = static_cast<int>(ligs.size());
+    std::vector<int32_t> g_start(n_l + 1), g_atoms(n_l), kept_rows, kept_n(n_l);
+    const bool on_device = num_modes >= 1 && num_modes <= 32;
+    if (on_device) {
+        for (int g = 0; g < n_l; ++g) {
+            g_start[g] = g * exhaustiveness;
+            g_atoms[g] = ligs[g].lig.n_atoms();
+        }
+        g_start[n_l] = n_l * exhaustiveness;
+        kept_rows.assign(static_cast<size_t>(n_l) * num_modes, -1);
+        check(ctx_, pxd_cluster_poses_batch(ctx_, n_l, g_start.data(), g_atoms.data(), max_atoms, out.data(),
+                                            ps.data(), nev.data(), num_modes, min_rmsd, kept_rows.data(),
+                                            kept_n.data()));
+    }
     row = 0;
     int written = 0;
-    for (auto& l : ligs) {
+    for (int gi = 0; gi < n_l; ++gi) {
+        auto& l = ligs[gi];
         const int N = l.lig.n_atoms();
         std::vector<PoseResult> cands(exhaustiveness);
         for (int w = 0; w < exhaustiveness; ++w, ++row) {
@@ -542,7 +566,13 @@ void Engine::search(const std::string& ligand_index_file, const std::string& out
             p.xyz.assign(out.begin() + row * max_atoms * 3, out.begin() + row * max_atoms * 3 + N * 3);
             p.torsions.assign(tors.begin() + row * R, tors.begin() + row * R + R);
         }
-        std::vector<PoseResult> kept = cluster_poses(cands, num_modes, min_rmsd);
+        std::vector<PoseResult> kept;
+        if (on_device) {
+            for (int k = 0; k < kept_n[gi]; ++k)
+                kept.push_back(cands[kept_rows[static_cast<size_t>(gi) * num_modes + k] - g_start[gi]]);
+        } else {
+            kept = cluster_poses(cands, num_modes, min_rmsd);
+        }
         if (kept.empty()) {
             log(2, "Tasks with prefix [" + stem(l.path) + "] has failed.");
             continue;
@@ -628,6 +658,9 @@ int pxd_engine_optimize(pxd_engine* h, const char* index_file, const char* outpu
     return guarded(h, [&](Engine& e) {
         e.optimize(index_file ? index_file : "", output_dir ? output_dir : "", max_niters, slope);
     });
+}
+int pxd_engine_set_dof_mode(pxd_engine* h, int32_t dof_mode) {
+    return guarded(h, [&](Engine& e) { e.set_dof_mode(dof_mode); });
 }
 int pxd_engine_search(pxd_engine* h, const char* index_file, const char* output_dir, int32_t seed,
                       int32_t exhaustiveness, int32_t max_nsteps, int32_t relax_nsteps, int32_t num_modes,

@@ -40,6 +40,8 @@ public:
     void drop_maps();
     void evaluate(const std::string& ligand_index_file, const std::string& output_file);
     void optimize(const std::string& ligand_index_file, const std::string& output_dir, int max_niters, double slope);
+    // variables of optimize's L-BFGS: PXD_DOF_CARTESIAN (the reference) or PXD_DOF_RIGID_TORSION
+    void set_dof_mode(int mode);
     void search(const std::string& ligand_index_file, const std::string& output_dir, int seed, int exhaustiveness,
                 int max_nsteps, int relax_nsteps, int num_modes, double min_rmsd, double mc_mmenergy_threshold,
                 double slope);
@@ -53,6 +55,7 @@ private:
     bool has_maps_ = false;
     pxd_box grid_{};
     int nthreads_ = 1;
+    int dof_mode_ = PXD_DOF_CARTESIAN;
 };
 
 // pose_writer::consume (writer.cpp:40-81): the <ligand>_out.json text

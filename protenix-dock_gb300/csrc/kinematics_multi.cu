@@ -34,16 +34,6 @@ struct PoseMultiArgs {
     float* out_dir;                // [P][max_atoms][3] (JVP) or [P][dof] (backward's derivative)
 };
 
-__device__ __forceinline__ Mat3 unit_quat_rotation(const float* q4) {
-    const float inv = rsqrtf(q4[0] * q4[0] + q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);
-    const float a = q4[0] * inv, b = q4[1] * inv, c = q4[2] * inv, d = q4[3] * inv;
-    Mat3 m;  // get_rotation_matrix (math.cpp:22-42)
-    m.r0 = make_float3(a * a + b * b - c * c - d * d, 2.f * (b * c - a * d), 2.f * (a * c + b * d));
-    m.r1 = make_float3(2.f * (a * d + b * c), a * a - b * b + c * c - d * d, 2.f * (c * d - a * b));
-    m.r2 = make_float3(2.f * (b * d - a * c), 2.f * (a * b + c * d), a * a - b * b - c * c + d * d);
-    return m;
-}
-
 __global__ void __launch_bounds__(kPoseWarps * kWarp) pose_multi_kernel(const __grid_constant__ PoseMultiArgs a) {
     extern __shared__ __align__(16) float umem[];
     const int lane = threadIdx.x & (kWarp - 1);

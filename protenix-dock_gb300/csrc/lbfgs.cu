@@ -3,7 +3,9 @@
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
+#include <type_traits>
 
+#include "device_dof.cuh"
 #include "device_lbfgs.cuh"
 
 namespace pxd {
@@ -30,22 +32,32 @@ struct LbfgsArgs {
     float* hist;       // per warp: S [m][D_pad], Y [m][D_pad]
     size_t hist_stride;
     int hist_smem;     // 1: the history lives in the warp's shared memory instead
+    int X_pad;         // rigid-body + torsion variables: padded 3 * max_atoms + R (0: Cartesian)
 };
 
 constexpr int kWarpsPerBlock = 4;
 constexpr int kDefaultMinBlocks = 5;  // measured best on GB300 for the 42-atom bench ligand (296.7k poses/s against 293.3k for 4)
 
+// Floats of one warp's shared-memory slice: the evaluation buffers, the optimiser
+// vectors and scalars, the history when it is held there, and for rigid-body + torsion
+// variables (xp > 0) the forward-map frames, the input-frame relative coordinates and
+// torsion axes, the placed pose, its Cartesian gradient and the evaluated variables.
+__host__ __device__ inline int lbfgs_warp_floats(int cap, int n_local, int dp, int m, int hist_smem, int xp) {
+    return pose_bufs_floats(cap, n_local) + kOptVecs * dp + opt_scalar_floats(m) +
+           (hist_smem ? 2 * hist_slots(m) * dp : 0) + (xp > 0 ? kKinFloats + 4 * cap + 4 * kWarp + 2 * xp + dp : 0);
+}
+
 // kMinBlocks > 0 asks the compiler to fit that many blocks per SM (register cap);
-// variants are chosen per launch (lbfgs_variant).
-template <int kMinBlocks>
+// variants are chosen per launch (lbfgs_variant). kDof: the variables are rigid body +
+// torsions (DofClosure) instead of Cartesian coordinates (Closure).
+template <int kMinBlocks, bool kDof>
 __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinBlocks : 1)
     lbfgs_kernel(const __grid_constant__ LbfgsArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
     const int Dp = a.D_pad;
-    const int per_warp = pose_bufs_floats(a.max_atoms, a.n_local) + kOptVecs * Dp + opt_scalar_floats(a.c.m) +
-                         (a.hist_smem ? 2 * hist_slots(a.c.m) * Dp : 0);
+    const int per_warp = lbfgs_warp_floats(a.max_atoms, a.n_local, Dp, a.c.m, a.hist_smem, kDof ? a.X_pad : 0);
     float* base = smem + wib * per_warp;
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
@@ -54,10 +66,20 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
     v.S = a.hist_smem ? vb + kOptVecs * Dp + opt_scalar_floats(a.c.m) : a.hist + gw * a.hist_stride;
     v.Y = v.S + static_cast<size_t>(hist_slots(a.c.m)) * Dp;
     const int R = a.env.rec.n_rotors;
-    Closure c;
+    using Cl = typename std::conditional<kDof, DofClosure, Closure>::type;
+    Cl c;
     c.env = &a.env;
     c.b = &b;
     c.lane = lane;
+    if constexpr (kDof) {
+        float* xb = vb + kOptVecs * Dp + opt_scalar_floats(a.c.m) + (a.hist_smem ? 2 * hist_slots(a.c.m) * Dp : 0);
+        c.ks = reinterpret_cast<KinShared*>(xb);
+        c.rel = reinterpret_cast<float4*>(xb + kKinFloats);
+        c.axes = c.rel + a.max_atoms;
+        c.xc = reinterpret_cast<float*>(c.axes + kWarp);
+        c.gc = c.xc + a.X_pad;
+        c.q = c.gc + a.X_pad;
+    }
     const int n_queue = a.count_dev ? *a.count_dev : a.n_poses;
     while (true) {
         int k = 0;
@@ -76,17 +98,40 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
         }
         const DevLigand& L = a.ligands[lid];
         const int N = L.n_atoms;
-        const int D = 3 * N + R;
-        const float* px = a.xyz + static_cast<size_t>(pose) * a.stride_atoms * 3;
-        for (int e = lane; e < 3 * N; e += kWarp) v.x[e] = px[e];
-        for (int r = lane; r < R; r += kWarp) v.x[3 * N + r] = a.tors[static_cast<size_t>(pose) * R + r];
-        __syncwarp();
+        float* px = a.xyz + static_cast<size_t>(pose) * a.stride_atoms * 3;
+        float* pt = a.tors + static_cast<size_t>(pose) * R;
         c.L = &L;
         double energy = 0.0;
-        const int st = lbfgs_pose(c, a.c, v, D, Dp, lane, energy);
-        float* ox = a.xyz + static_cast<size_t>(pose) * a.stride_atoms * 3;
-        for (int e = lane; e < 3 * N; e += kWarp) ox[e] = v.x[e];
-        for (int r = lane; r < R; r += kWarp) a.tors[static_cast<size_t>(pose) * R + r] = v.x[3 * N + r];
+        int st;
+        if constexpr (kDof) {
+            const int T = L.n_tors;
+            if (T > kWarp || L.n_frags < 1 || L.n_frags > kMaxFrags || 7 + T + R > Dp || 3 * N + R > a.X_pad) {
+                if (lane == 0) {
+                    a.status[pose] = PXD_POSE_BAD_INPUT;
+                    a.nevals[pose] = 0;
+                    a.energy[pose] = 0.0;
+                }
+                continue;
+            }
+            // q0: the input's centre, the identity quaternion, no torsion change
+            const int D = 7 + T + R;
+            const float3 c0 = dof_prepare(c, px);
+            for (int e = lane; e < D; e += kWarp)
+                v.x[e] = e == 0 ? c0.x : e == 1 ? c0.y : e == 2 ? c0.z : e == 3 ? 1.f : e < 7 + T ? 0.f : pt[e - 7 - T];
+            __syncwarp();
+            st = lbfgs_pose(c, a.c, v, D, Dp, lane, energy);
+            // the final energy placed the returned variables: c.xc is the returned pose
+            for (int e = lane; e < 3 * N; e += kWarp) px[e] = c.xc[e];
+            for (int r = lane; r < R; r += kWarp) pt[r] = c.xc[3 * N + r];
+        } else {
+            const int D = 3 * N + R;
+            for (int e = lane; e < 3 * N; e += kWarp) v.x[e] = px[e];
+            for (int r = lane; r < R; r += kWarp) v.x[3 * N + r] = pt[r];
+            __syncwarp();
+            st = lbfgs_pose(c, a.c, v, D, Dp, lane, energy);
+            for (int e = lane; e < 3 * N; e += kWarp) px[e] = v.x[e];
+            for (int r = lane; r < R; r += kWarp) pt[r] = v.x[3 * N + r];
+        }
         if (lane == 0) {
             a.energy[pose] = energy;
             a.nevals[pose] = c.nevals;
@@ -163,13 +208,17 @@ using LbfgsKernelFn = void (*)(LbfgsArgs);
 constexpr int kHistSmem = PXD_LBFGS_HIST_SMEM;
 static LbfgsKernelFn variant_fn(int variant) {
     switch (variant & 255) {
-        case 3: return lbfgs_kernel<3>;
-        case 4: return lbfgs_kernel<4>;
-        case 5: return lbfgs_kernel<5>;
-        case 6: return lbfgs_kernel<6>;
-        default: return lbfgs_kernel<0>;
+        case 3: return lbfgs_kernel<3, false>;
+        case 4: return lbfgs_kernel<4, false>;
+        case 5: return lbfgs_kernel<5, false>;
+        case 6: return lbfgs_kernel<6, false>;
+        default: return lbfgs_kernel<0, false>;
     }
 }
+
+// Rigid-body + torsion variables run one register budget, the default's, whatever the
+// class's variant (its shared-memory history flag still applies).
+static LbfgsKernelFn dof_kernel() { return lbfgs_kernel<kDefaultMinBlocks, true>; }
 
 // Size class of a per-warp atom capacity: the smallest bound of 32, 64, ..., 256 it fits.
 static int class_bound(int cap) { return std::min(256, (cap + 31) / 32 * 32); }
@@ -186,16 +235,26 @@ static int lbfgs_variant_id(const pxd_context* ctx, int cap) {
     }();
     return choice;
 }
-static LbfgsKernelFn lbfgs_variant(const pxd_context* ctx, int cap) {
-    return variant_fn(lbfgs_variant_id(ctx, cap));
+static LbfgsKernelFn lbfgs_variant(const pxd_context* ctx, int cap, bool dof) {
+    return dof ? dof_kernel() : variant_fn(lbfgs_variant_id(ctx, cap));
 }
 
+// Padded length of the optimiser's vectors for ligands of up to `cap` atoms: 3 cap + R
+// Cartesian, or 7 + T + R with T the most torsions of the context's ligands (at most 32;
+// a ligand with more is a bad input of that mode).
+static int vec_pad(const pxd_context* ctx, int cap, bool dof) {
+    if (!dof) return padded(3 * cap + ctx->rec.n_rotors);
+    int t = 0;
+    for (auto& e : ctx->ligands) t = std::max(t, std::min(e.n_tors, kWarp));
+    return padded(7 + t + ctx->rec.n_rotors);
+}
+static int dof_xpad(const pxd_context* ctx, int cap, bool dof) { return dof ? padded(3 * cap + ctx->rec.n_rotors) : 0; }
+
 // Dynamic shared memory of one lbfgs_kernel block for ligands of up to `cap` atoms.
-static size_t lbfgs_block_smem(const pxd_context* ctx, int cap, int history, bool hist_smem) {
-    const int dp = padded(3 * cap + ctx->rec.n_rotors);
-    const int per_warp = pose_bufs_floats(cap, ctx->rec.n_local) + kOptVecs * dp + opt_scalar_floats(history) +
-                         (hist_smem ? 2 * hist_slots(history) * dp : 0);
-    return sizeof(float) * kWarpsPerBlock * per_warp;
+static size_t lbfgs_block_smem(const pxd_context* ctx, int cap, int history, bool hist_smem, bool dof) {
+    return sizeof(float) * kWarpsPerBlock *
+           lbfgs_warp_floats(cap, ctx->rec.n_local, vec_pad(ctx, cap, dof), history, hist_smem ? 1 : 0,
+                             dof_xpad(ctx, cap, dof));
 }
 
 int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_ids,
@@ -443,7 +502,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     const std::vector<int> caps = size_class_caps(ctx, max_atoms, n_poses);
     const bool classes = caps.size() > 1;
     struct Plan {
-        int cap, dp, blocks, hist_smem;
+        int cap, dp, xp, blocks, hist_smem;
         size_t smem, stride;
         LbfgsKernelFn kern;
     };
@@ -453,16 +512,18 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     rc = cuda_check(ctx, cudaDeviceGetAttribute(&smem_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device),
                     "shared memory limit");
     if (rc) return rc;
+    const bool dof = p.dof_mode == PXD_DOF_RIGID_TORSION;
     for (int cap : caps) {
         Plan q;
         q.cap = cap;
-        q.kern = lbfgs_variant(ctx, cap);
+        q.kern = lbfgs_variant(ctx, cap, dof);
         q.hist_smem = (lbfgs_variant_id(ctx, cap) & kHistSmem) ? 1 : 0;
         // a pinned shared-memory history that does not fit this class falls back to the slab
-        if (q.hist_smem && lbfgs_block_smem(ctx, cap, p.history, true) > static_cast<size_t>(smem_limit))
+        if (q.hist_smem && lbfgs_block_smem(ctx, cap, p.history, true, dof) > static_cast<size_t>(smem_limit))
             q.hist_smem = 0;
-        q.dp = padded(3 * cap + ctx->rec.n_rotors);
-        q.smem = lbfgs_block_smem(ctx, cap, p.history, q.hist_smem);
+        q.dp = vec_pad(ctx, cap, dof);
+        q.xp = dof_xpad(ctx, cap, dof);
+        q.smem = lbfgs_block_smem(ctx, cap, p.history, q.hist_smem, dof);
         q.stride = q.hist_smem ? 0 : static_cast<size_t>(2) * hist_slots(p.history) * q.dp;
         plan.push_back(q);
     }
@@ -510,6 +571,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
         LbfgsArgs a = base;
         a.max_atoms = plan[k].cap;
         a.D_pad = plan[k].dp;
+        a.X_pad = plan[k].xp;
         a.hist = hist + hist_off[k];
         a.hist_stride = plan[k].stride;
         a.hist_smem = plan[k].hist_smem;
@@ -591,9 +653,11 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.count_dev = nullptr;
     fill_consts(a, p);
     a.n_local = ctx->rec.n_local;
-    a.D_pad = padded(3 * max_atoms + ctx->rec.n_rotors);
-    const size_t smem = lbfgs_block_smem(ctx, max_atoms, p.history, false);
-    const LbfgsKernelFn kern = lbfgs_variant(ctx, max_atoms);
+    const bool dof = p.dof_mode == PXD_DOF_RIGID_TORSION;
+    a.D_pad = vec_pad(ctx, max_atoms, dof);
+    a.X_pad = dof_xpad(ctx, max_atoms, dof);
+    const size_t smem = lbfgs_block_smem(ctx, max_atoms, p.history, false, dof);
+    const LbfgsKernelFn kern = lbfgs_variant(ctx, max_atoms, dof);
     rc = raise_smem_limit(ctx, kern, smem);
     if (rc) return rc;
     int per_sm = 0;
@@ -788,7 +852,8 @@ extern "C" int pxd_lbfgs_autotune_dev(pxd_context* ctx, const pxd_lbfgs_params* 
         int smem_limit = 0;
         cudaDeviceGetAttribute(&smem_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
         for (int v : kVariants) {
-            if ((v & kHistSmem) && lbfgs_block_smem(ctx, cap, p.history, true) > static_cast<size_t>(smem_limit))
+            if ((v & kHistSmem) && lbfgs_block_smem(ctx, cap, p.history, true, p.dof_mode == PXD_DOF_RIGID_TORSION) >
+                                        static_cast<size_t>(smem_limit))
                 continue;  // the history does not fit beside the pose buffers
             ctx->lbfgs_tuned[bound] = v;
             queue_copy(ctx, &rc, d_x, d_x0, sizeof(float) * m * cap * 3, cudaMemcpyDeviceToDevice, s,

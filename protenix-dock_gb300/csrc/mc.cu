@@ -138,14 +138,15 @@ struct McArgs {
     uint32_t seed;
     int n_local, D_pad;
     int warps_per_block;  // kMcWarps, or 1 when there are too few walkers to fill the SMs
+    int hist_smem;        // 1: the L-BFGS history lives in the warp's shared memory
     float* hist;
     size_t hist_stride;
     MtState* rng;
 };
 
-__host__ __device__ inline int mc_warp_floats(int max_atoms, int n_local, int Dp, int m) {
+__host__ __device__ inline int mc_warp_floats(int max_atoms, int n_local, int Dp, int m, int hist_smem) {
     return pose_bufs_floats(max_atoms, n_local) + kOptVecs * Dp + opt_scalar_floats(m) + 2 * Dp + 4 * max_atoms +
-           static_cast<int>(sizeof(KinShared) / sizeof(float)) + 64 + 16;
+           static_cast<int>(sizeof(KinShared) / sizeof(float)) + 64 + 16 + (hist_smem ? 2 * hist_slots(m) * Dp : 0);
 }
 
 __device__ bool all_in_box(const float* x, int N, const McArgs& a, int lane) {
@@ -245,7 +246,8 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     const int wib = threadIdx.x / kWarp;
     const int Dp = a.D_pad;
     const int m = a.full.m;
-    float* base = smem + static_cast<size_t>(wib) * mc_warp_floats(a.max_atoms, a.n_local, Dp, m);
+    const int per_warp = mc_warp_floats(a.max_atoms, a.n_local, Dp, m, a.hist_smem);
+    float* base = smem + static_cast<size_t>(wib) * per_warp;
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
     Vecs v = carve_vecs(vb, Dp, m);
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     float* tq = reinterpret_cast<float*>(&ks + 1);          // [64] torsions of a move
     double* bc = reinterpret_cast<double*>(tq + 64);         // [8] broadcast slots
     const size_t gw = static_cast<size_t>(blockIdx.x) * a.warps_per_block + wib;
-    v.S = a.hist + gw * a.hist_stride;
+    v.S = a.hist_smem ? base + per_warp - 2 * hist_slots(m) * Dp : a.hist + gw * a.hist_stride;
     v.Y = v.S + static_cast<size_t>(hist_slots(m)) * Dp;
     MtState* rng = a.rng + gw;
     const int R = a.env.rec.n_rotors;
@@ -504,6 +506,8 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
                       const float* start, float* out_xyz, float* out_tors, double* out_e, double* out_ps,
                       int32_t* out_nev, int32_t* out_st, double* gmin, void* stream) {
     if (!ctx || !p) return PXD_ERR_INVALID;
+    if (p->lbfgs.dof_mode != PXD_DOF_CARTESIAN)
+        return set_error(ctx, PXD_ERR_INVALID, "the search relaxes in Cartesian variables (dof_mode 0)");
     if (!ctx->has_receptor) return set_error(ctx, PXD_ERR_STATE, "set a receptor first");
     if (!ctx->sf_set[0] || !ctx->rec_score.has)
         return set_error(ctx, PXD_ERR_STATE, "the search needs the pose-selection scoring function and receptor lists");
@@ -561,7 +565,19 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     // walker has an SM's L1, shared-memory pipe and issue slots to itself.
     a.warps_per_block = n_walkers < kMcWarps * ctx->n_sm ? 1 : kMcWarps;
     const int wpb = a.warps_per_block;
-    const size_t smem = sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history);
+    // With one walker per SM its L-BFGS history (2 (m + 1) D_pad floats, 103 KB at m = 100
+    // and 42 atoms) moves into shared memory when it fits beside the pose buffers: the
+    // two-loop's passes then read shared memory instead of L1 / L2.
+    int smem_optin = 0;
+    rc = cuda_check(ctx, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device),
+                    "shared memory limit");
+    if (rc) return rc;
+    a.hist_smem = wpb == 1 && sizeof(float) * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history, 1) <=
+                                  static_cast<size_t>(smem_optin)
+                      ? 1
+                      : 0;
+    const size_t smem =
+        sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history, a.hist_smem);
     rc = cuda_check(ctx, cudaFuncSetAttribute(mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(smem)),
                     "mc smem attribute");
@@ -592,7 +608,7 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     const int need = (n_walkers + wpb - 1) / wpb;
     if (blocks > need) blocks = need;
     const size_t warps = static_cast<size_t>(blocks) * wpb;
-    a.hist_stride = static_cast<size_t>(2) * hist_slots(p->lbfgs.history) * a.D_pad;
+    a.hist_stride = a.hist_smem ? 0 : static_cast<size_t>(2) * hist_slots(p->lbfgs.history) * a.D_pad;
     const size_t hist_bytes = sizeof(float) * a.hist_stride * warps;
     const size_t rng_off = (hist_bytes + 255) / 256 * 256;
     rc = ensure_scratch(ctx, rng_off + sizeof(MtState) * warps);

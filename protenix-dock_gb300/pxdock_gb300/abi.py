@@ -126,6 +126,8 @@ class LbfgsParams(C.Structure):
         ("ls_tolerance_change", C.c_double),
         ("ls_gtd_threshold", C.c_double),
         ("reset_threshold", C.c_double),
+        ("dof_mode", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -146,8 +148,12 @@ class McParams(C.Structure):
     ]
 
 
+DOF_CARTESIAN = 0
+DOF_RIGID_TORSION = 1
+
+
 def lbfgs_params(max_iter=240, max_eval=0, history=100, tolerance_grad=0.5,
-                 tolerance_change=1e-4, lr=1.0):
+                 tolerance_change=1e-4, lr=1.0, dof_mode=DOF_CARTESIAN):
     """Reference constants by default (lbfgs_step, optimizer.h:50-67)."""
     p = LbfgsParams()
     p.max_iter = max_iter
@@ -162,6 +168,7 @@ def lbfgs_params(max_iter=240, max_eval=0, history=100, tolerance_grad=0.5,
     p.ls_tolerance_change = 1e-9
     p.ls_gtd_threshold = 1e5
     p.reset_threshold = 1e8
+    p.dof_mode = dof_mode
     return p
 
 

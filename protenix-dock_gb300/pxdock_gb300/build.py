@@ -18,7 +18,10 @@ REPO = os.path.dirname(PKG_ROOT)
 OUT_DIR = os.path.join(HERE, "_native")
 LIB_NAME = "libpxdock_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+# host code without fused multiply-add contraction, so that its FP64 results (the pose
+# clustering rule, conversions) are the same on x86-64 and aarch64 hosts
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr",
               "-Xptxas", "-v"] + ARCH
 
 

@@ -42,7 +42,7 @@ def test_library_loads_and_reports_version(lib_path):
     lib = C.CDLL(lib_path)
     lib.pxd_abi_version.restype = C.c_int32
     lib.pxd_version.restype = C.c_char_p
-    assert lib.pxd_abi_version() == 1
+    assert lib.pxd_abi_version() == 2
     assert b"sm_103a" in lib.pxd_version()
 
 

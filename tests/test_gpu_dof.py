@@ -1,0 +1,191 @@
+"""GPU parity of the rigid-body + torsion mode of the batched optimiser
+(pxd_lbfgs_params.dof_mode = PXD_DOF_RIGID_TORSION) against the FP64 restatement of the
+same DOF-space L-BFGS in oracle/dof_ref.py, on identical FP32 input poses.
+
+Tolerances:
+  short runs (3 iterations), where the trajectories coincide: final poses within 1e-3 A and
+      the same evaluation count and status for at least 90 % of the poses;
+  full runs (240 iterations, 96 starts): as many final poses within 0.05 A of the FP64 run
+      as the FP64 optimiser reproduces itself from starts moved by 1e-5 A (less a
+      small-sample margin), and no bias in the final energies: the fractions of runs that
+      end more than 1 kcal/mol worse and better than the FP64 run differ by at most 0.15
+      (the FP64 control's by up to 0.10 over four draws), the median paired difference
+      within 0.5 kcal/mol;
+  every run: the reported energy is the FP64 objective at the returned pose (1e-3 kcal/mol),
+      and every bond length of the input pose is kept to 1e-4 A (poses within 100 A of the
+      box; a start flung far out, as the FP64 optimiser flings it too, is counted instead).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import dof_ref as DR
+import oracle as O
+from pxdock_gb300 import abi, model, native, synth
+from unroll_ref import quat_rot
+
+pytestmark = pytest.mark.gpu
+
+E_ABS = 1e-3
+
+
+@pytest.fixture(scope="module")
+def system():
+    native.load(auto_build=True)
+    rec = model.Receptor.from_json(synth.make_receptor(seed=0, n_heavy=1000, cube=26.0, cavity=8.5, n_rotors=3))
+    lig = model.Ligand.from_json(synth.make_ligand(seed=1))
+    box = model.make_box((0.0, 0.0, 0.0), (16.0, 16.0, 16.0), 0.375)
+    types = sorted(set(int(t) for t in lig.vdw_type))
+    ctx = native.Context(0)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, types)
+    ctx.set_slope(1e6)
+    lid = ctx.add_ligand(lig)
+    port = O.PortSystem(rec, lig)
+    port.build_grid(box, types, nthreads=os.cpu_count() or 1)
+    port.set_slope(1e6)
+    yield dict(rec=rec, lig=lig, ctx=ctx, lid=lid, port=port)
+    ctx.close()
+
+
+def starts(c, n, seed):
+    """Input poses with the ligand's own bond geometry: turned, moved and twisted, then
+    rounded to FP32 (the GPU's input precision; the oracle gets the same values)."""
+    rng = np.random.default_rng(seed)
+    x0 = c["lig"].poses[0]
+    out = []
+    for _ in range(n):
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        ang = rng.normal(scale=0.3)
+        q = np.concatenate([[np.cos(ang / 2)], np.sin(ang / 2) * ax])
+        tors = rng.normal(scale=0.3, size=c["lig"].n_torsions)
+        ctr = x0.mean(axis=0) + rng.normal(scale=0.5, size=3)
+        out.append(c["port"].ligand_apply(x0, ctr, quat_rot(q), tors))
+    return np.array(out).astype(np.float32).astype(np.float64)
+
+
+def rmsd(a, b):
+    return float(np.sqrt(np.mean(np.sum((a - b) ** 2, axis=-1))))
+
+
+def covalent_kept(lig, x_in, x_out):
+    """Largest change of a bond length of the ligand's force field."""
+    b = lig.ff.bonds
+    d0 = np.linalg.norm(x_in[b[:, 0]] - x_in[b[:, 1]], axis=-1)
+    d1 = np.linalg.norm(x_out[b[:, 0]] - x_out[b[:, 1]], axis=-1)
+    return float(np.max(np.abs(d1 - d0)))
+
+
+def check_energies(c, out):
+    """The reported energy is the FP64 objective at the returned pose, except for a pose
+    flung so far out that its energy leaves the FP32 range of the device's pair terms
+    (above 1e30 kcal/mol; reported as NaN or as a huge value): at most 2 of a batch."""
+    flung = 0
+    for i in range(len(out["energy"])):
+        e, _, _ = c["port"].score_grad(out["torsions"][i], out["xyz"][i])
+        if abs(e) > 1e30:
+            flung += 1
+            assert not abs(out["energy"][i]) < 1e30, (i, out["energy"][i], e)
+            continue
+        assert abs(out["energy"][i] - e) <= E_ABS + 1e-9 * abs(e), (i, out["energy"][i], e)
+    assert flung <= 2, flung
+
+
+def test_short_runs_follow_the_oracle(system):
+    c = system
+    x = starts(c, 48, 3)
+    p = native.lbfgs_params(max_iter=3, history=10, dof_mode=abi.DOF_RIGID_TORSION)
+    out = c["ctx"].lbfgs(p, c["lid"], x)
+    check_energies(c, out)
+    R = c["rec"].n_rotors
+    same, near = 0, 0
+    for i in range(len(x)):
+        assert covalent_kept(c["lig"], x[i], out["xyz"][i]) <= 1e-4
+        xf, ef, nev, st = DR.optimize_dof(c["port"], c["rec"], c["lig"], x[i], p)
+        near += rmsd(out["xyz"][i], xf) <= 1e-3
+        same += (out["nevals"][i] == nev) and (out["status"][i] == st)
+        assert out["torsions"][i].shape == (R,)
+    print("short runs: within 1e-3 A %d, same nevals/status %d of %d" % (near, same, len(x)))
+    assert near >= 0.9 * len(x) and same >= 0.9 * len(x), (near, same)
+
+
+def test_full_runs_match_the_oracle_distribution(system):
+    c = system
+    n = 96
+    x = starts(c, n, 4)
+    p = native.lbfgs_params(max_iter=240, history=100, dof_mode=abi.DOF_RIGID_TORSION)
+    out = c["ctx"].lbfgs(p, c["lid"], x)
+    check_energies(c, out)
+    rng = np.random.default_rng(11)
+    close, close_ctl, flung, flung_ref = 0, 0, 0, 0
+    e_gpu, e_ref, e_ctl = [], [], []
+    for i in range(n):
+        xf, ef, _, _ = DR.optimize_dof(c["port"], c["rec"], c["lig"], x[i], p)
+        xc, ec, _, _ = DR.optimize_dof(c["port"], c["rec"], c["lig"], x[i] + rng.normal(scale=1e-5, size=x[i].shape), p)
+        # a start whose line search leaps out of the box ends far away (the FP64 optimiser
+        # flings such starts too); there FP32 coordinates cannot hold bond lengths
+        if np.abs(out["xyz"][i]).max() < 100.0:
+            assert covalent_kept(c["lig"], x[i], out["xyz"][i]) <= 1e-4
+        else:
+            flung += 1
+        flung_ref += np.abs(xf).max() >= 100.0
+        close += rmsd(out["xyz"][i], xf) <= 0.05
+        close_ctl += rmsd(xc, xf) <= 0.05
+        e_gpu.append(out["energy"][i])
+        e_ref.append(ef)
+        e_ctl.append(ec)
+    e_gpu, e_ref, e_ctl = np.array(e_gpu), np.array(e_ref), np.array(e_ctl)
+    ok = np.abs(e_ref) < 1e6  # poses the FP64 run keeps in the box
+    stats = {}
+    for name, e in (("gpu", e_gpu), ("control", e_ctl)):
+        d = (e - e_ref)[ok]
+        stats[name] = (float(np.mean(d > 1.0)), float(np.mean(d < -1.0)), float(np.median(d)))
+    print("within 0.05 A: gpu %d, fp64 control %d of %d; flung gpu %d, fp64 %d; "
+          "(worse, better, median difference) gpu %s control %s" % (close, close_ctl, n, flung, flung_ref,
+                                                                    stats["gpu"], stats["control"]))
+    assert flung <= flung_ref + 2, (flung, flung_ref)
+    assert close >= close_ctl - 12, (close, close_ctl)
+    # no bias: as many runs end > 1 kcal/mol worse as better than the FP64 run (the FP64
+    # control's fractions differ by up to 0.10 over four draws), median difference ~0
+    worse, better, med = stats["gpu"]
+    assert abs(worse - better) <= 0.15 and abs(med) <= 0.5, stats
+    # the mode optimises: final energies below the inputs'
+    e_in = [c["port"].score_grad(np.zeros(c["rec"].n_rotors), xi)[0] for xi in x]
+    assert np.median(np.array(e_in) - e_gpu) > 0
+
+
+def test_dof_mode_through_the_batched_and_no_alloc_calls(system):
+    """The device-pointer calls (size classes and the allocation-free launcher) give the
+    host call's results, pose for pose."""
+    import torch
+
+    c = system
+    x = starts(c, 16, 5)
+    p = native.lbfgs_params(max_iter=40, history=8, dof_mode=abi.DOF_RIGID_TORSION)
+    host = c["ctx"].lbfgs(p, c["lid"], x)
+    dev = torch.device("cuda:0")
+    N, R = c["lig"].n_atoms, c["rec"].n_rotors
+    for call in (c["ctx"].lbfgs_dev, c["ctx"].lbfgs_dev_noalloc):
+        d_x = torch.from_numpy(x.astype(np.float32)).to(dev)
+        d_i = torch.full((len(x),), c["lid"], dtype=torch.int32, device=dev)
+        d_t = torch.zeros((len(x), max(R, 1)), dtype=torch.float32, device=dev)
+        d_e = torch.zeros(len(x), dtype=torch.float64, device=dev)
+        d_n = torch.zeros(len(x), dtype=torch.int32, device=dev)
+        d_s = torch.zeros(len(x), dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        call(p, len(x), N, d_i.data_ptr(), d_x.data_ptr(), d_t.data_ptr(), d_e.data_ptr(), d_n.data_ptr(),
+             d_s.data_ptr(), c["ctx"].stream)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(d_e.cpu().numpy(), host["energy"])
+        np.testing.assert_array_equal(d_n.cpu().numpy(), host["nevals"])
+        np.testing.assert_array_equal(d_x.cpu().numpy().astype(np.float64), host["xyz"])
+
+
+def test_search_rejects_the_dof_mode(system):
+    c = system
+    lo, hi = (-8.0, -8.0, -8.0), (8.0, 8.0, 8.0)
+    p = native.mc_params(lo, hi, lbfgs=dict(dof_mode=abi.DOF_RIGID_TORSION))
+    with pytest.raises(RuntimeError, match="Cartesian"):
+        c["ctx"].mc_search(p, c["lid"], [0], [1], c["lig"].poses[0][None])

@@ -3,10 +3,12 @@ outputs (tests/golden/engine, written by oracle/_ref).
 
 - evaluate: every pose's pscore / bscore within 1e-3 + 1e-5 |s| of the reference's;
 - optimize: the reference's schema and pose order; every energy and score is the FP64
-  value at the returned pose (|dE| <= 1e-3); the final energies of the 30-iteration
-  runs from the same starts agree with the reference's to the optimiser's FP32 bound;
+  value at the returned pose (|dE| <= 1e-3); the final energies of the 30-iteration runs
+  from the same starts differ from the reference's by no more than the FP64 port's own
+  final energies do when its starts move by FP32 rounding (+ 1e-3 kcal/mol);
 - search: schema, at most num_modes poses sorted by pose score, poses inside the box,
-  every energy / score the FP64 value at the pose; best scores comparable;
+  every energy / score the FP64 value at the pose; the best pose score no worse than the
+  FP64 port's walkers (from the same and from FP32-rounded starts) by more than 1 kcal/mol;
 - dump_maps / load_maps round trip; the reference's precondition errors.
 """
 import csv
@@ -79,11 +81,27 @@ def test_optimize_matches_reference(setup):
     ref = json.load(open(os.path.join(ENG, "ref_optimize", "ligand_out.json")))
     assert list(ours) == list(ref)
     assert [p["offset"] for p in ours["poses"]] == [p["offset"] for p in ref["poses"]]
+    # the FP64 port reproduces the reference's runs from the same starts; the control is the
+    # port from the starts moved by FP32 rounding and 1e-6 A (four draws): the spread of
+    # final energies that input precision alone causes after these iterations
+    pp = abi.lbfgs_params(max_iter=s["calls"]["optimize"]["max_niters"])
+    R = s["rec"].n_rotors
+    rng = np.random.default_rng(3)
     for a, b in zip(ours["poses"], ref["poses"]):
         assert list(a) == list(b)
         consistent(s, a)
         assert a["nevals"] > 0
-        assert abs(a["energy"] - b["energy"]) <= 0.5 + 0.02 * abs(b["energy"]), (a["energy"], b["energy"])
+        x0 = s["lig"].poses[a["offset"]]
+        same = s["port"].lbfgs(pp, np.zeros(R), x0)["energy"]
+        # (the fixture's numbers carry six significant digits)
+        assert abs(same - b["energy"]) <= 1e-5 * max(1.0, abs(b["energy"])), (same, b["energy"])
+        spread = max(abs(s["port"].lbfgs(pp, np.zeros(R), x0.astype(np.float32).astype(np.float64) +
+                                         rng.normal(scale=1e-6, size=x0.shape))["energy"] - b["energy"])
+                     for _ in range(4))
+        print("optimize pose %d: gpu %.6f ref %.6f control spread %.6f" % (a["offset"], a["energy"], b["energy"],
+                                                                           spread))
+        assert abs(a["energy"] - b["energy"]) <= spread + 1e-3 + 1e-5 * abs(b["energy"]), \
+            (a["energy"], b["energy"], spread)
     best = ours["poses"][ours["best_pose"]["index"]]
     assert best["pscore"] == min(p["pscore"] for p in ours["poses"])
 
@@ -107,7 +125,21 @@ def test_search_outputs(setup):
     t, x = consistent(s, ours["poses"][0])
     bs, _ = s["port"].score(s["sf"][1], s["port"].receptor_apply(t), x)
     assert abs(ours["best_pose"]["bscore"] - bs) <= 1e-3 + 1e-5 * abs(bs)
-    assert abs(ps[0] - ref["poses"][0]["pscore"]) <= 3.0 + 0.2 * abs(ref["poses"][0]["pscore"])
+    # best pose score: the FP64 port's walkers reproduce the reference's best; the GPU's best
+    # is no worse than both that and the port's walkers from FP32-rounded starts by more
+    # than 1 kcal/mol (Monte-Carlo trajectories diverge at the first different acceptance,
+    # so the bar is on the search's outcome, not on equality)
+    x0 = s["lig"].poses[0]
+    walk = lambda start: min(
+        r["pscore"] for r in (s["port"].mc_walker(s["sf"][0], lo, hi, args["seed"], w, start, True, args["max_nsteps"],
+                                                  args["relax_nsteps"], args["mc_mmenergy_threshold"])
+                              for w in range(args["exhaustiveness"])) if r["nevals"] > 0)
+    ref_best = ref["poses"][0]["pscore"]
+    port_best = walk(x0)
+    ctl_best = walk(x0.astype(np.float32).astype(np.float64))
+    print("search best pscore: gpu %.4f ref %.4f port %.4f control %.4f" % (ps[0], ref_best, port_best, ctl_best))
+    assert abs(port_best - ref_best) <= 1e-5 * max(1.0, abs(ref_best)), (port_best, ref_best)
+    assert ps[0] <= max(ref_best, ctl_best) + 1.0, (ps[0], ref_best, ctl_best)
 
 
 def test_maps_round_trip(setup):
