@@ -140,7 +140,7 @@ def test_full_runs_match_the_oracle_distribution(system):
     ok = np.abs(e_ref) < 1e6  # poses the FP64 run keeps in the box
     stats = {}
     for name, e in (("gpu", e_gpu), ("control", e_ctl)):
-        d = (e - e_ref)[ok]
+        d = (np.where(np.isfinite(e), e, np.inf) - e_ref)[ok]  # a NaN end counts as worse
         stats[name] = (float(np.mean(d > 1.0)), float(np.mean(d < -1.0)), float(np.median(d)))
     print("within 0.05 A: gpu %d, fp64 control %d of %d; flung gpu %d, fp64 %d; "
           "(worse, better, median difference) gpu %s control %s" % (close, close_ctl, n, flung, flung_ref,
@@ -153,7 +153,8 @@ def test_full_runs_match_the_oracle_distribution(system):
     assert abs(worse - better) <= 0.15 and abs(med) <= 0.5, stats
     # the mode optimises: final energies below the inputs'
     e_in = [c["port"].score_grad(np.zeros(c["rec"].n_rotors), xi)[0] for xi in x]
-    assert np.median(np.array(e_in) - e_gpu) > 0
+    gain = np.array(e_in) - e_gpu
+    assert np.median(gain[np.isfinite(gain)]) > 0
 
 
 def test_dof_mode_through_the_batched_and_no_alloc_calls(system):
@@ -188,4 +189,4 @@ def test_search_rejects_the_dof_mode(system):
     lo, hi = (-8.0, -8.0, -8.0), (8.0, 8.0, 8.0)
     p = native.mc_params(lo, hi, lbfgs=dict(dof_mode=abi.DOF_RIGID_TORSION))
     with pytest.raises(RuntimeError, match="Cartesian"):
-        c["ctx"].mc_search(p, c["lid"], [0], [1], c["lig"].poses[0][None])
+        c["ctx"].mc_search(p, c["lid"], c["lig"].poses[0][None], [1])

@@ -9,6 +9,7 @@ Tolerances (the parity bar of the path, written here once):
            chaotic), with the same distribution of final energies;
   integer / index work (nevals, status) exact where trajectories coincide.
 """
+import json
 import math
 import os
 
@@ -177,6 +178,37 @@ def test_lbfgs_reference_fixtures(lib, golden, iters, evals, t0, E, tors, e_tol,
 
 def rmsd(a, b):
     return float(np.sqrt(np.mean(np.sum((a - b) ** 2, axis=-1))))
+
+
+@pytest.mark.parametrize("history", [100, 8])
+def test_lbfgs_with_receptor_rotors_follows_port(lib, golden, history):
+    """The reference engine's own optimize inputs (a pocket with two receptor rotors, three
+    clashing starts at 1e6-1e10 kcal/mol), 30 iterations: a descent that FP32 follows
+    closely, so every pose ends within 0.01 kcal/mol of the FP64 port with the same
+    evaluation count and status. (A racy line-search state once advanced its counter twice
+    here and ended pose 2 at -9.6 instead of -18.8 kcal/mol.)"""
+    eng = os.path.join(golden, "engine")
+    calls = json.load(open(os.path.join(eng, "calls.json")))
+    rec = model.Receptor.from_file(os.path.join(eng, "receptor.json"))
+    lig = model.Ligand.from_file(os.path.join(eng, "ligand.json"))
+    assert rec.n_rotors > 0
+    box = model.make_box(calls["box"][:3], calls["box"][3:], calls["spacing"])
+    types = sorted(set(int(t) for t in lig.vdw_type))
+    ctx = native.Context(0)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, types)
+    ctx.set_slope(1e6)
+    lid = ctx.add_ligand(lig)
+    port = O.PortSystem(rec, lig)
+    port.build_grid(box, types, nthreads=os.cpu_count() or 1)
+    port.set_slope(1e6)
+    out = ctx.lbfgs(native.lbfgs_params(max_iter=30, history=history), lid, lig.poses)
+    pp = abi.lbfgs_params(max_iter=30, history=history)
+    for k in range(len(lig.poses)):
+        r = port.lbfgs(pp, np.zeros(rec.n_rotors), lig.poses[k])
+        assert abs(out["energy"][k] - r["energy"]) <= 1e-2, (k, out["energy"][k], r["energy"])
+        assert out["nevals"][k] == r["nevals"] and out["status"][k] == r["status"], k
+    ctx.close()
 
 
 def test_lbfgs_matches_oracle_trajectories(complex_small):
