@@ -1148,7 +1148,7 @@ def main():
         "evals_per_s": world * evals_total / t_dev,
         "evals_per_pose": evals_step / N_POSES,
         "status_counts": {str(k): int((st == k).sum()) for k in range(4)},
-        "final_energy_median": float(np.median(e_final)),
+        "final_energy_median": float(np.nanmedian(e_final)),
         "wall_s": wall,
     }
     clocks = clk.summary()

@@ -25,41 +25,11 @@ struct LsState {
     int it, lo, hi, insuf, done, base, count, pad;
 };
 
-// Gram matrices of a warp's L-BFGS history, for the matrix form of the two-loop recursion
-// (shared memory, physical slot indices a, b of the m + 1 history slots):
-//   SY[a * slots + b] = s_a . y_b (a older than b), YY[a * slots + b] = y_a . y_b,
-//   SG[a] = s_a . g and YG[a] = y_a . g at the current gradient (compensated pairs),
-//   rf[a] = 1 / (y_a . s_a), and per logical pair k the two-loop's alpha (al) and
-//   alpha - beta (cf).
-struct Gram {
-    float *SY, *YY;
-    DS *SG, *YG;
-    float *rf, *al, *cf;
-};
-
-__host__ __device__ constexpr int gram_floats(int m) {
-    return (2 * (m + 1) * (m + 1) + 4 * (m + 1) + 3 * (m + 1) + 3) / 4 * 4;
-}
-
-__device__ __forceinline__ Gram carve_gram(float* base, int m) {
-    const int slots = m + 1;
-    Gram h;
-    h.SG = reinterpret_cast<DS*>(base);
-    h.YG = h.SG + slots;
-    h.SY = base + 4 * slots;
-    h.YY = h.SY + slots * slots;
-    h.rf = h.YY + slots * slots;
-    h.al = h.rf + slots;
-    h.cf = h.al + slots;
-    return h;
-}
-
 struct Vecs {
     float *x, *g, *gp, *d, *q, *sv, *gnew, *gprev, *bg0, *bg1;
     float *S, *Y;
     double *ro, *al;
     LsState* ls;
-    Gram gram;  // kMat optimisers only
 };
 
 // D_pad-long vectors in a warp's optimiser slice: x, g, gp, d and the line search's g_new,
@@ -276,160 +246,7 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
 //
 // energy receives the FP64 objective at the returned pose (energy64), or, with
 // final_energy false (a caller that does not use it), the last FP32 loss.
-// The history's new column of Gram products, after the update pass wrote the pair
-// (s_n, y_n) into slot n: for every kept pair a (logical 0 .. count - 1 from base),
-// s_a . y_n and y_a . y_n, one pair per lane (lanes start their sweeps at different
-// elements, so the lanes' rows fall in distinct banks). The products advance SG and YG
-// from the previous gradient to the current one (g = g_prev + y_n), whether or not the
-// pair is kept; a kept pair also stores them as its column of SY and YY.
-__device__ __forceinline__ void gram_column(const Vecs& v, int D, size_t Dp, int slots, int base, int count, int n,
-                                            bool keep, int lane) {
-    const Gram& h = v.gram;
-    const float* yn = v.Y + n * Dp;
-    for (int k = lane; k < count; k += kWarp) {
-        const int a = (base + k) % slots;
-        const float* sa = v.S + a * Dp;
-        const float* ya = v.Y + a * Dp;
-        DS sy{0.f, 0.f}, yy{0.f, 0.f};
-        int e = lane % D;
-        for (int i = 0; i < D; ++i) {
-            ds_dot_acc(sy, sa[e], yn[e]);
-            ds_dot_acc(yy, ya[e], yn[e]);
-            e = e + 1 == D ? 0 : e + 1;
-        }
-        ds_add_ds(h.SG[a], sy);
-        ds_add_ds(h.YG[a], yy);
-        if (keep) {
-            h.SY[a * slots + n] = sy.hi + sy.lo;
-            const float yyf = yy.hi + yy.lo;
-            h.YY[a * slots + n] = yyf;
-            h.YY[n * slots + a] = yyf;
-        }
-    }
-}
-
-// The two-loop recursion (optimizer.cpp:485-505) in matrix form: with the Gram products,
-// the dots s_k . q and y_k . d of the loops are scalar recurrences,
-//   alpha_k = rho_k (-s_k . g - sum_{j newer} alpha_j s_k . y_j),       newest to oldest,
-//   beta_k  = rho_k (H (-y_k . g - sum_j alpha_j y_k . y_j)
-//                    + sum_{j older} (alpha_j - beta_j) s_j . y_k),      oldest to newest,
-// and the direction is one pass, d = H (-g - sum alpha_j y_j) + sum (alpha_j - beta_j) s_j:
-// the same iterates as the two loops up to rounding, without their 2 m dependent
-// reductions over the vectors. Lane k % 32 holds pair k's running sum (k < 128). Writes d
-// and g_prev = g; returns g . d.
-__device__ __forceinline__ double two_loop_gram(const Vecs& v, int D, size_t Dp, int slots, int base, int count,
-                                                float H, int lane) {
-    const Gram& h = v.gram;
-    constexpr int kU = (PXD_MAX_HISTORY + kWarp - 1) / kWarp;
-    const auto wrap = [slots](int p) { return p >= slots ? p - slots : p; };
-    DS t[kU];
-    int pk[kU];  // physical slot of this lane's pairs k = lane + 32 u
-#pragma unroll
-    for (int u = 0; u < kU; ++u) {
-        const int k = lane + u * kWarp;
-        pk[u] = wrap(base + (k < count ? k : 0));
-        t[u] = DS{0.f, 0.f};
-        if (k < count) {
-            const DS sg = h.SG[pk[u]];
-            t[u] = DS{-sg.hi, -sg.lo};
-        }
-    }
-    int pj = wrap(base + count - 1);
-    for (int j = count - 1; j >= 0; --j) {
-        DS tj = t[0];
-#pragma unroll
-        for (int u = 1; u < kU; ++u)
-            if ((j >> 5) == u) tj = t[u];
-        const float th = __shfl_sync(kFull, tj.hi, j & 31), tl = __shfl_sync(kFull, tj.lo, j & 31);
-        const float a = (th + tl) * h.rf[pj];
-        if (lane == 0) h.al[j] = a;
-#pragma unroll
-        for (int u = 0; u < kU; ++u)
-            if (lane + u * kWarp < j) ds_dot_acc(t[u], -a, h.SY[pk[u] * slots + pj]);
-        pj = pj == 0 ? slots - 1 : pj - 1;
-    }
-    __syncwarp();
-    // w_k = H (-y_k . g - sum_j alpha_j y_k . y_j)
-#pragma unroll
-    for (int u = 0; u < kU; ++u) {
-        if (lane + u * kWarp < count) {
-            const DS yg = h.YG[pk[u]];
-            DS acc{-yg.hi, -yg.lo};
-            const float* row = h.YY + pk[u] * slots;
-            int q = base;
-            for (int j = 0; j < count; ++j) {
-                ds_dot_acc(acc, -h.al[j], row[q]);
-                q = q + 1 == slots ? 0 : q + 1;
-            }
-            const float hi = acc.hi * H;
-            t[u] = DS{hi, fmaf(acc.hi, H, -hi) + acc.lo * H};
-        }
-    }
-    pj = base;
-    for (int j = 0; j < count; ++j) {
-        DS tj = t[0];
-#pragma unroll
-        for (int u = 1; u < kU; ++u)
-            if ((j >> 5) == u) tj = t[u];
-        const float th = __shfl_sync(kFull, tj.hi, j & 31), tl = __shfl_sync(kFull, tj.lo, j & 31);
-        const float cf = h.al[j] - (th + tl) * h.rf[pj];
-        if (lane == 0) h.cf[j] = cf;
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-            const int k = lane + u * kWarp;
-            if (k > j && k < count) ds_dot_acc(t[u], cf, h.SY[pj * slots + pk[u]]);
-        }
-        pj = pj + 1 == slots ? 0 : pj + 1;
-    }
-    __syncwarp();
-    // d = H (-g - sum alpha_j y_j) + sum cf_j s_j, four elements per lane at a time
-    DS acc{0.f, 0.f};
-    for (int e0 = 0; e0 < D; e0 += 4 * kWarp) {
-        float r[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int e = e0 + lane + u * kWarp;
-            r[u] = e < D ? -v.g[e] : 0.f;
-        }
-        int q = base;
-        for (int j = 0; j < count; ++j) {
-            const float na = -h.al[j];
-            const float* yj = v.Y + q * Dp + e0 + lane;
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (e0 + lane + u * kWarp < D) r[u] = fmaf(na, yj[u * kWarp], r[u]);
-            q = q + 1 == slots ? 0 : q + 1;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) r[u] *= H;
-        q = base;
-        for (int j = 0; j < count; ++j) {
-            const float c = h.cf[j];
-            const float* sj = v.S + q * Dp + e0 + lane;
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (e0 + lane + u * kWarp < D) r[u] = fmaf(c, sj[u * kWarp], r[u]);
-            q = q + 1 == slots ? 0 : q + 1;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int e = e0 + lane + u * kWarp;
-            if (e < D) {
-                const float ge = v.g[e];
-                v.d[e] = r[u];
-                v.gp[e] = ge;
-                ds_dot_acc(acc, ge, r[u]);
-            }
-        }
-    }
-    __syncwarp();
-    return ds_warp_sum(acc);
-}
-
-// kMat: the two-loop recursion in matrix form over the Gram products (v.gram), for a warp
-// that runs alone on its SM, where the classic loops' 2 m dependent reductions are the
-// critical path.
-template <bool kMat = false, class Cl>
+template <class Cl>
 static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int D,
                           size_t Dp, int lane, double& energy, bool final_energy = true) {
     const int m = p.m;
@@ -461,7 +278,7 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
             float* ss_ = v.S + spare * Dp;
             const float tf = static_cast<float>(S.t);
             float ymax = 0.f;
-            DS a_ys{0.f, 0.f}, a_yy{0.f, 0.f}, a_sg{0.f, 0.f}, a_yg{0.f, 0.f};
+            DS a_ys{0.f, 0.f}, a_yy{0.f, 0.f};
             for (int e = lane; e < D; e += kWarp) {
                 const float y = v.g[e] - v.gp[e];
                 const float sv = v.d[e] * tf;
@@ -470,30 +287,12 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
                 ymax = fmaxf(ymax, fabsf(y));
                 ds_dot_acc(a_ys, y, sv);
                 ds_dot_acc(a_yy, y, y);
-                if constexpr (kMat) {
-                    ds_dot_acc(a_sg, sv, v.g[e]);
-                    ds_dot_acc(a_yg, y, v.g[e]);
-                }
             }
             reset = warp_max(ymax) > p.reset;
             if (!reset) {
                 const double ys = ds_warp_sum(a_ys);
                 const double yy = ds_warp_sum(a_yy);
-                const bool keep = ys > 1e-10;
-                if constexpr (kMat) {
-                    __syncwarp();  // the new pair, written above, is read across lanes
-                    gram_column(v, D, Dp, slots, S.base, S.count, spare, keep, lane);
-                    if (keep) {
-                        const double sg = ds_warp_sum(a_sg), yg = ds_warp_sum(a_yg);
-                        if (lane == 0) {
-                            v.gram.SG[spare] = DS{static_cast<float>(sg), static_cast<float>(sg - static_cast<float>(sg))};
-                            v.gram.YG[spare] = DS{static_cast<float>(yg), static_cast<float>(yg - static_cast<float>(yg))};
-                            v.gram.YY[spare * slots + spare] = static_cast<float>(yy);
-                            v.gram.rf[spare] = static_cast<float>(1.0 / ys);
-                        }
-                    }
-                }
-                if (keep) {
+                if (ys > 1e-10) {
                     if (S.count == m)
                         S.base = (S.base + 1) % slots;  // the oldest slot becomes the spare
                     else
@@ -529,9 +328,6 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
             } else {
                 S.t = p.lr;
             }
-        } else if constexpr (kMat) {
-            gtd = two_loop_gram(v, D, Dp, slots, S.base, S.count, static_cast<float>(S.H_diag), lane);
-            S.t = p.lr;
         } else {
             // first loop, newest to oldest: q = -g - sum al_k y_k
             DS acc{0.f, 0.f};

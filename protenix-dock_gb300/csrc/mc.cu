@@ -138,20 +138,14 @@ struct McArgs {
     uint32_t seed;
     int n_local, D_pad;
     int warps_per_block;  // kMcWarps, or 1 when there are too few walkers to fill the SMs
-    int hist_smem;        // 1: the L-BFGS history lives in the warp's shared memory
-    int gram_smem;        // 1: so do its Gram products (else a per-warp slab in global memory)
     float* hist;
     size_t hist_stride;
-    float* gram;
-    size_t gram_stride;
     MtState* rng;
 };
 
-__host__ __device__ inline int mc_warp_floats(int max_atoms, int n_local, int Dp, int m, int hist_smem,
-                                              int gram_smem) {
+__host__ __device__ inline int mc_warp_floats(int max_atoms, int n_local, int Dp, int m) {
     return pose_bufs_floats(max_atoms, n_local) + kOptVecs * Dp + opt_scalar_floats(m) + 2 * Dp + 4 * max_atoms +
-           static_cast<int>(sizeof(KinShared) / sizeof(float)) + 64 + 16 + (hist_smem ? 2 * hist_slots(m) * Dp : 0) +
-           (gram_smem ? gram_floats(m) : 0);
+           static_cast<int>(sizeof(KinShared) / sizeof(float)) + 64 + 16;
 }
 
 __device__ bool all_in_box(const float* x, int N, const McArgs& a, int lane) {
@@ -245,18 +239,13 @@ __device__ void atomic_min_double(double* p, double v) {
     }
 }
 
-// The relaxations run the two-loop recursion in matrix form (lbfgs_pose<true>): a warp
-// alone on its SM (a single docking search) waits on the classic loops' 2 m dependent
-// reductions (m = 100 by default), and every launch shape runs the same arithmetic, so a
-// walker ends where it ends in any batch.
 __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_constant__ McArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
     const int Dp = a.D_pad;
     const int m = a.full.m;
-    const int per_warp = mc_warp_floats(a.max_atoms, a.n_local, Dp, m, a.hist_smem, a.gram_smem);
-    float* base = smem + static_cast<size_t>(wib) * per_warp;
+    float* base = smem + static_cast<size_t>(wib) * mc_warp_floats(a.max_atoms, a.n_local, Dp, m);
     const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
     Vecs v = carve_vecs(vb, Dp, m);
@@ -267,10 +256,8 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     float* tq = reinterpret_cast<float*>(&ks + 1);          // [64] torsions of a move
     double* bc = reinterpret_cast<double*>(tq + 64);         // [8] broadcast slots
     const size_t gw = static_cast<size_t>(blockIdx.x) * a.warps_per_block + wib;
-    const int gram = a.gram_smem ? gram_floats(m) : 0;
-    v.S = a.hist_smem ? base + per_warp - gram - 2 * hist_slots(m) * Dp : a.hist + gw * a.hist_stride;
+    v.S = a.hist + gw * a.hist_stride;
     v.Y = v.S + static_cast<size_t>(hist_slots(m)) * Dp;
-    v.gram = carve_gram(a.gram_smem ? base + per_warp - gram : a.gram + gw * a.gram_stride, m);
     MtState* rng = a.rng + gw;
     const int R = a.env.rec.n_rotors;
     Closure c;
@@ -345,7 +332,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
         }
         // ---- full relaxation and score of the start (searcher.cpp:120-126)
         double best_e = 0.0;
-        lbfgs_pose<true>(c, a.full, v, D, Dp, lane, best_e);
+        lbfgs_pose(c, a.full, v, D, Dp, lane, best_e);
         long total = c.nevals;
         double best_ps = mc_pscore(a, L, v.x, b, lane);
         vcopy(best_x, v.x, D, lane);
@@ -410,7 +397,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                         if (pre > gm + a.threshold) continue;
                     }
                     double cdd_e = 0.0;  // unused: the step is judged by its pose score
-                    lbfgs_pose<true>(c, a.fast, v, D, Dp, lane, cdd_e, false);
+                    lbfgs_pose(c, a.fast, v, D, Dp, lane, cdd_e, false);
                     total += c.nevals;
                     const double cdd_ps = mc_pscore(a, L, v.x, b, lane);
                     bool accept = step == 0 || cdd_ps < tmp_ps;
@@ -423,7 +410,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                         tmp_ps = cdd_ps;
                         if (tmp_ps < best_ps) {
                             double e2 = 0.0;
-                            lbfgs_pose<true>(c, a.full, v, D, Dp, lane, e2);
+                            lbfgs_pose(c, a.full, v, D, Dp, lane, e2);
                             total += c.nevals;
                             tmp_ps = mc_pscore(a, L, v.x, b, lane);
                             if (tmp_ps < best_ps) {
@@ -576,25 +563,8 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     // walker has an SM's L1, shared-memory pipe and issue slots to itself.
     a.warps_per_block = n_walkers < kMcWarps * ctx->n_sm ? 1 : kMcWarps;
     const int wpb = a.warps_per_block;
-    // With one walker per SM its L-BFGS history (2 (m + 1) D_pad floats, 103 KB at m = 100
-    // and 42 atoms) moves into shared memory when it fits beside the pose buffers: the
-    // two-loop's passes then read shared memory instead of L1 / L2.
-    int smem_optin = 0;
-    rc = cuda_check(ctx, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device),
-                    "shared memory limit");
-    if (rc) return rc;
-    // ... and so do its Gram products (83 KB at m = 100), where they fit too
-    const int m = p->lbfgs.history;
-    const auto fits = [&](int h, int g) {
-        return sizeof(float) * mc_warp_floats(max_atoms, a.n_local, a.D_pad, m, h, g) <=
-               static_cast<size_t>(smem_optin);
-    };
-    a.hist_smem = wpb == 1 && fits(1, 0) ? 1 : 0;
-    a.gram_smem = wpb == 1 && fits(a.hist_smem, 1) ? 1 : 0;
-    const auto kern = mc_kernel;
-    const size_t smem =
-        sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, m, a.hist_smem, a.gram_smem);
-    rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t smem = sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history);
+    rc = cuda_check(ctx, cudaFuncSetAttribute(mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(smem)),
                     "mc smem attribute");
     if (rc) return rc;
@@ -612,11 +582,11 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
         const size_t need = per_sm_blocks * (smem + 1024);  // each block plus the driver's reserved kilobyte
         carveout = static_cast<int>(std::min<size_t>(100, (100 * need + sm_smem - 1) / sm_smem + 1));
     }
-    rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, carveout),
+    rc = cuda_check(ctx, cudaFuncSetAttribute(mc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carveout),
                     "mc carve-out");
     if (rc) return rc;
     int per_sm = 0;
-    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wpb * kWarp, smem),
+    rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel, wpb * kWarp, smem),
                     "mc occupancy");
     if (rc) return rc;
     if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
@@ -624,21 +594,20 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     const int need = (n_walkers + wpb - 1) / wpb;
     if (blocks > need) blocks = need;
     const size_t warps = static_cast<size_t>(blocks) * wpb;
-    a.hist_stride = a.hist_smem ? 0 : static_cast<size_t>(2) * hist_slots(m) * a.D_pad;
-    a.gram_stride = a.gram_smem ? 0 : static_cast<size_t>(gram_floats(m));
-    const size_t hist_bytes = (sizeof(float) * a.hist_stride * warps + 255) / 256 * 256;
-    const size_t gram_bytes = (sizeof(float) * a.gram_stride * warps + 255) / 256 * 256;
-    rc = ensure_scratch(ctx, hist_bytes + gram_bytes + sizeof(MtState) * warps);
+    a.hist_stride = static_cast<size_t>(2) * hist_slots(p->lbfgs.history) * a.D_pad;
+    const size_t hist_bytes = sizeof(float) * a.hist_stride * warps;
+    const size_t rng_off = (hist_bytes + 255) / 256 * 256;
+    rc = ensure_scratch(ctx, rng_off + sizeof(MtState) * warps);
     if (rc) return rc;
     a.hist = static_cast<float*>(ctx->scratch);
-    a.gram = reinterpret_cast<float*>(static_cast<char*>(ctx->scratch) + hist_bytes);
-    a.rng = reinterpret_cast<MtState*>(static_cast<char*>(ctx->scratch) + hist_bytes + gram_bytes);
+    a.rng = reinterpret_cast<MtState*>(static_cast<char*>(ctx->scratch) + rng_off);
     a.counter = ctx->d_counter;
     a.error = ctx->d_counter + 1;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(int), s), "counter reset");
     if (rc) return rc;
-    return cuda_check(ctx, launch_with_map_window(ctx, kern, blocks, wpb * kWarp, smem, s, a), "mc_kernel launch");
+    return cuda_check(ctx, launch_with_map_window(ctx, mc_kernel, blocks, wpb * kWarp, smem, s, a),
+                      "mc_kernel launch");
 }
 
 int pxd_mc_search(pxd_context* ctx, const pxd_mc_params* p, int32_t lig, int32_t n, const int32_t* walker_ids,

@@ -3,7 +3,8 @@
 Tolerances (the parity bar of the path, written here once):
   energy   |dE| <= 1e-3 kcal/mol on physically visited poses (ligand inside the pocket,
            no atom overlaps), relative 1e-6 of |E| elsewhere;
-  gradient max|dg| <= 1e-4 * max|g| (relative to the largest component of the pose);
+  gradient max|dg| <= 1e-4 * max|g| (relative to the largest component of the pose), and
+           |dg_i| <= 1e-3 |g_i| for every component above 1 kcal/mol/A;
   final L-BFGS poses from identical starts: RMSD <= 0.05 A as often as the FP64
            optimiser reproduces itself from FP32-rounded starts (the trajectories are
            chaotic), with the same distribution of final energies;
@@ -23,6 +24,7 @@ pytestmark = pytest.mark.gpu
 
 E_ABS = 1e-3
 G_REL = 1e-4
+G_COMP = 1e-3  # per component, where |component| > 1 kcal/mol/A
 
 
 @pytest.fixture(scope="module")
@@ -80,10 +82,17 @@ def test_score_grad_grid(complex_small, slope):
     c["port"].set_slope(slope)
     poses = near_poses(c["lig"], 32, 11)
     e, g, _ = c["ctx"].score_grad(c["lid"], poses)
+    worst = 0.0
     for i in range(len(poses)):
         er, _, gr = c["port"].score_grad([], poses[i])
         assert abs(e[i] - er) <= E_ABS, (i, e[i], er)
         assert np.max(np.abs(g[i] - gr)) <= G_REL * np.max(np.abs(gr)), i
+        # component by component where the component is at least 1 kcal/mol/A
+        big = np.abs(gr) > 1.0
+        rel = np.abs(g[i] - gr)[big] / np.abs(gr)[big]
+        worst = max(worst, float(rel.max()) if rel.size else 0.0)
+        assert np.all(rel <= G_COMP), (i, rel.max())
+    print("largest relative error of a gradient component above 1 kcal/mol/A: %.2e" % worst)
 
 
 def box_penalty(box, slope, x):
