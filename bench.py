@@ -67,7 +67,10 @@ def config_dict(lig, box, world=1):
         "poses": N_POSES,
         "ligand_atoms": lig.n_atoms,
         "grid_points": int(np.prod(list(box.npoints))),
-        "l2": "flushed between steps (256 MiB write); inputs ~100 MB < L2",
+        "l2": "flushed between steps (256 MiB write)",
+        "maps": "%d maps (%d vdW types + Coulomb), %.0f MB" % (
+            len(set(int(t) for t in lig.vdw_type)) + 1, len(set(int(t) for t in lig.vdw_type)),
+            (len(set(int(t) for t in lig.vdw_type)) + 1) * int(np.prod(list(box.npoints))) * 16 / 1e6),
         "parallelism": "replicas" if world == 1 else
                        "replicas x%d: one process per GPU, each a cost-balanced share of one set of "
                        "%d x %d starts, no collective on the data path" % (world, world, N_POSES),
@@ -959,7 +962,7 @@ def spawn_ranks(n):
 
 
 def main():
-    global N_POSES
+    global N_POSES, BOX_SIZE
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -989,8 +992,12 @@ def main():
     ap.add_argument("--poses-per-ligand", type=int, default=256, help="screening: poses per ligand")
     ap.add_argument("--poses", type=int, default=N_POSES,
                     help="poses per step (smaller only for profiling captures)")
+    ap.add_argument("--box", type=float, default=BOX_SIZE,
+                    help="optimize: box edge in A (30: the config's 81^3 maps; larger boxes give map sets "
+                         "beyond L2, for the residency experiment)")
     args = ap.parse_args()
     N_POSES = args.poses
+    BOX_SIZE = args.box
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         return spawn_ranks(args.gpus)
     if args.impl == "reference":

@@ -421,7 +421,13 @@ void Engine::optimize(const std::string& ligand_index_file, const std::string& o
         check(ctx_, pxd_grid_set_slope(ctx_, slope));
     else
         log(1, "Receptor cache is disabled in this run.");
-    auto ligs = load_ligands(read_index(ligand_index_file), false);  // multi_pose_reader
+    // multi_pose_reader; the rigid-body + torsion mode also reads each ligand's torsion tree
+    auto ligs = load_ligands(read_index(ligand_index_file), dof_mode_ == PXD_DOF_RIGID_TORSION);
+    if (dof_mode_ == PXD_DOF_RIGID_TORSION)
+        for (auto& l : ligs)
+            if (!l.lig.has_tree)
+                throw std::runtime_error("dof_mode 1 needs the torsion tree of ligand " + l.path +
+                                         " (its \"geometry\" block)");
     register_ligands(ctx_, ligs);
     make_dirs(output_dir);
     if (ligs.empty()) return;

@@ -142,6 +142,39 @@ def test_search_outputs(setup):
     assert ps[0] <= max(ref_best, ctl_best) + 1.0, (ps[0], ref_best, ctl_best)
 
 
+def test_optimize_rigid_body_torsion_mode(setup):
+    """optimize(..., dof_mode=1): the reference's schema; every energy the FP64 value at its
+    pose; each pose keeps its input bond lengths (to FP32 precision) and lowers its energy;
+    the next default call is the reference's Cartesian mode again."""
+    s = setup
+    idx = str(s["dir"] / "index.txt")
+    out = s["dir"] / "opt_dof"
+    s["eng"].optimize(idx, str(out), max_niters=60, dof_mode=1)
+    ours = json.load(open(out / "ligand_out.json"))
+    ref = json.load(open(os.path.join(ENG, "ref_optimize", "ligand_out.json")))
+    assert list(ours) == list(ref)
+    b = s["lig"].ff.bonds
+    R = s["rec"].n_rotors
+    for p in ours["poses"]:
+        t, x = consistent(s, p)
+        x0 = s["lig"].poses[p["offset"]]
+        d0 = np.linalg.norm(x0[b[:, 0]] - x0[b[:, 1]], axis=-1)
+        d1 = np.linalg.norm(x[b[:, 0]] - x[b[:, 1]], axis=-1)
+        assert np.max(np.abs(d1 - d0)) <= 1e-4
+        e0, _, _ = s["port"].score_grad(np.zeros(R), x0)
+        assert p["energy"] < e0
+    with pytest.raises(RuntimeError, match="dof_mode"):
+        s["eng"].optimize(idx, str(s["dir"] / "opt_bad"), max_niters=5, dof_mode=2)
+    cart = s["dir"] / "opt_cart"
+    s["eng"].optimize(idx, str(cart), max_niters=5)
+    moved = []
+    for p in json.load(open(cart / "ligand_out.json"))["poses"]:
+        x, x0 = np.asarray(p["ligand"]["xyz"]), s["lig"].poses[p["offset"]]
+        moved.append(np.max(np.abs(np.linalg.norm(x[b[:, 0]] - x[b[:, 1]], axis=-1) -
+                                   np.linalg.norm(x0[b[:, 0]] - x0[b[:, 1]], axis=-1))))
+    assert max(moved) > 1e-3  # Cartesian steps stretch bonds
+
+
 def test_maps_round_trip(setup):
     s = setup
     cache = s["dir"] / "maps"
