@@ -45,7 +45,10 @@ __device__ __forceinline__ void ds_add_ds(DS& a, const DS& b) {
     a.lo = a.lo + b.lo + err;
 }
 
-// Sum over the warp; every lane returns lane 0's result.
+// Sum over the warp, the same on every lane: at each butterfly level both partners add the
+// same two pairs, and the result does not depend on their order (two-sum's error term is
+// the exact rounding error of hi + hi, and lo + lo commutes), so no final broadcast is
+// needed.
 __device__ __forceinline__ double ds_warp_sum(DS v) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -54,21 +57,21 @@ __device__ __forceinline__ double ds_warp_sum(DS v) {
         o.lo = __shfl_xor_sync(kFull, v.lo, off);
         ds_add_ds(v, o);
     }
-    v.hi = __shfl_sync(kFull, v.hi, 0);
-    v.lo = __shfl_sync(kFull, v.lo, 0);
     return static_cast<double>(v.hi) + static_cast<double>(v.lo);
 }
 
+// Butterfly reductions leave every lane with the same value (max and a two-operand sum
+// commute), so they need no final broadcast.
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, off));
-    return __shfl_sync(kFull, v, 0);
+    return v;
 }
 
 __device__ __forceinline__ float warp_sum_f(float v) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
-    return __shfl_sync(kFull, v, 0);
+    return v;
 }
 
 // One step of a dot product with the exact FP32 product (fma) accumulated as a
