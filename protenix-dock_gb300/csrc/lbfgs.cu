@@ -582,9 +582,27 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
             a.order = counters + 2 * n_cls + k * static_cast<size_t>(n_poses);
             ks = ctx->class_streams[k];
         }
-        rc = cuda_check(ctx, launch_with_map_window(ctx, plan[k].kern, plan[k].blocks, kWarpsPerBlock * kWarp,
-                                                    plan[k].smem, ks, a),
-                        "lbfgs_kernel launch");
+        // A launch of at most one block per SM (a few poses, the plain per-pose calls) asks for
+        // the smallest shared-memory carve-out that holds its block, so the rest of the SM's
+        // memory serves as L1 for the map gathers, the history and the topology records; larger
+        // launches keep the driver's choice. The preference is a property of the kernel, set
+        // before each launch (a concurrent launch of the same variant can only see a different
+        // preference, never an invalid one: the driver still fits the dynamic shared memory).
+        int carveout = cudaSharedmemCarveoutDefault;
+        if (plan[k].blocks <= ctx->n_sm) {
+            int sm_smem = 0;
+            rc = cuda_check(ctx, cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                                        ctx->device),
+                            "shared memory per SM");
+            if (rc) return rc;
+            carveout = static_cast<int>(std::min<size_t>(100, (100 * (plan[k].smem + 1024) + sm_smem - 1) / sm_smem + 1));
+        }
+        rc = cuda_check(ctx, cudaFuncSetAttribute(plan[k].kern, cudaFuncAttributePreferredSharedMemoryCarveout, carveout),
+                        "lbfgs carve-out");
+        if (!rc)
+            rc = cuda_check(ctx, launch_with_map_window(ctx, plan[k].kern, plan[k].blocks, kWarpsPerBlock * kWarp,
+                                                        plan[k].smem, ks, a),
+                            "lbfgs_kernel launch");
         if (!rc && classes) rc = class_join(ctx, k, s);
         if (rc) return rc;
     }
