@@ -329,10 +329,14 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
                 S.t = p.lr;
             }
         } else {
-            // first loop, newest to oldest: q = -g - sum al_k y_k
+            // first loop, newest to oldest: q = -g - sum al_k y_k. The ring's base and count
+            // are read once into registers: the line-search state lives in the lane's frame,
+            // and its fields would otherwise be reloaded from local memory at every pass.
+            const int base = S.base, count = S.count;
+            int sl = base + count - 1 >= slots ? base + count - 1 - slots : base + count - 1;
             DS acc{0.f, 0.f};
             {
-                const float* sk = v.S + ((S.base + S.count - 1) % slots) * Dp;
+                const float* sk = v.S + sl * Dp;
                 for (int e = lane; e < D; e += kWarp) {
                     const float ge = v.g[e];
                     v.q[e] = -ge;
@@ -340,15 +344,15 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
                     ds_dot_acc(acc, sk[e], -ge);
                 }
             }
-            for (int k = S.count - 1; k >= 0; --k) {
-                const int sl = (S.base + k) % slots;
+            for (int k = count - 1; k >= 0; --k) {
                 const double al = ds_warp_sum(acc) * v.ro[sl];
                 if (lane == 0) v.al[k] = al;
                 const float nal = static_cast<float>(-al);
                 const float* yk = v.Y + sl * Dp;
+                const int sn_slot = sl == 0 ? slots - 1 : sl - 1;
                 acc = DS{0.f, 0.f};
                 if (k > 0) {
-                    const float* sn = v.S + ((S.base + k - 1) % slots) * Dp;
+                    const float* sn = v.S + sn_slot * Dp;
                     for (int e = lane; e < D; e += kWarp) {
                         const float qe = fmaf(yk[e], nal, v.q[e]);
                         v.q[e] = qe;
@@ -364,14 +368,16 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
                     }
                 }
                 __syncwarp();
+                sl = sn_slot;
             }
             // second loop, oldest to newest: d += (al_k - be_k) s_k
-            for (int k = 0; k < S.count; ++k) {
-                const int sl = (S.base + k) % slots;
+            sl = base;
+            for (int k = 0; k < count; ++k) {
                 const double be = ds_warp_sum(acc) * v.ro[sl];
                 const float w = static_cast<float>(v.al[k] - be);
                 const float* sk = v.S + sl * Dp;
-                const float* nx = k + 1 < S.count ? v.Y + ((S.base + k + 1) % slots) * Dp : v.g;
+                const int nx_slot = sl + 1 == slots ? 0 : sl + 1;
+                const float* nx = k + 1 < count ? v.Y + nx_slot * Dp : v.g;
                 acc = DS{0.f, 0.f};
                 for (int e = lane; e < D; e += kWarp) {
                     const float de = fmaf(sk[e], w, v.d[e]);
@@ -379,6 +385,7 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
                     ds_dot_acc(acc, nx[e], de);
                 }
                 __syncwarp();
+                sl = nx_slot;
             }
             gtd = ds_warp_sum(acc);  // g . d after the last step
             S.t = p.lr;
