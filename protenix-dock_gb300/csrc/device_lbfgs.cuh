@@ -29,7 +29,6 @@ struct Vecs {
     float *x, *g, *gp, *d, *q, *sv, *gnew, *gprev, *bg0, *bg1;
     float *S, *Y;
     double *ro, *al;
-    LsState* ls;
 };
 
 // D_pad-long vectors in a warp's optimiser slice: x, g, gp, d and the line search's g_new,
@@ -65,7 +64,6 @@ __device__ __forceinline__ Vecs carve_vecs(float* vb, int Dp, int m) {
     v.sv = v.gnew;
     v.ro = reinterpret_cast<double*>(vb + kOptVecs * Dp);
     v.al = v.ro + hist_slots(m);
-    v.ls = nullptr;  // set by lbfgs_pose to its lane-private state
     v.S = v.Y = nullptr;
     return v;
 }
@@ -106,16 +104,21 @@ __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double
 }
 
 // strong_wolfe (optimizer.cpp:235-427); g holds the current gradient on entry and the
-// accepted one on exit. Its scalars live in *v.ls. Cl is the closure over
-// the variables: Closure (Cartesian) or DofClosure (rigid body + torsions).
+// accepted one on exit. Its scalars live in S, the caller's lane-private state; the
+// evaluation's directional derivative comes back through a local, so no field of S has
+// its address taken and the compiler keeps S in registers. Cl is the closure over the
+// variables: Closure (Cartesian) or DofClosure (rigid body + torsions).
 template <class Cl>
 static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d, float* g,
-                                    const Vecs& v, int D, int lane) {
-    LsState& S = *v.ls;
+                                    const Vecs& v, int D, int lane, LsState& S) {
     float* g_new = v.gnew;
     float* g_prev = v.gprev;
     S.f = S.loss;
-    S.fn = closure_eval(c, S.t, d, g_new, &S.gn);
+    {
+        double gn_new;
+        S.fn = closure_eval(c, S.t, d, g_new, &gn_new);
+        S.gn = gn_new;
+    }
     if (isnan(S.fn)) {
         S.loss = S.fn;
         return;
@@ -161,7 +164,11 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
         vcopy(g_prev, g_new, D, lane);
         gpv = g_prev;
         S.gp = S.gn;
-        S.fn = closure_eval(c, S.t, d, g_new, &S.gn);
+        {
+        double gn_new;
+        S.fn = closure_eval(c, S.t, d, g_new, &gn_new);
+        S.gn = gn_new;
+    }
         ++S.it;
     }
     S.dn = 0.0;
@@ -203,7 +210,11 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
             S.insuf = 0;
         }
         S.t = t;
-        S.fn = closure_eval(c, S.t, d, g_new, &S.gn);
+        {
+        double gn_new;
+        S.fn = closure_eval(c, S.t, d, g_new, &gn_new);
+        S.gn = gn_new;
+    }
         ++S.it;
         const int lo = S.lo, hi = S.hi;
         const double bf_lo = lo ? S.bf1 : S.bf0;
@@ -255,8 +266,6 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
     c.x0 = v.x;
     c.nevals = 0;
     LsState S;
-    Vecs vs = v;
-    vs.ls = &S;
     S.loss = closure_eval(c, 0.0, nullptr, v.g);
     if (vabsmax(v.g, D, lane) < p.tol_grad) {
         energy = final_energy ? closure_energy64(c, v.x) : S.loss;
@@ -396,7 +405,7 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
             break;
         }
         S.gtd = gtd;
-        strong_wolfe(c, p, v.d, v.g, vs, D, lane);
+        strong_wolfe(c, p, v.d, v.g, v, D, lane, S);
         if (isnan(S.loss)) {
             status = PXD_POSE_NAN;
             break;
