@@ -62,6 +62,18 @@ __device__ __forceinline__ double ds_warp_sum(DS v) {
 
 // Butterfly reductions leave every lane with the same value (max and a two-operand sum
 // commute), so they need no final broadcast.
+// The warp sum rounded once to FP32 (hi + lo), without leaving the FP32 pipe.
+__device__ __forceinline__ float ds_warp_sum_f(DS v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        DS o;
+        o.hi = __shfl_xor_sync(kFull, v.hi, off);
+        o.lo = __shfl_xor_sync(kFull, v.lo, off);
+        ds_add_ds(v, o);
+    }
+    return v.hi + v.lo;
+}
+
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, off));

@@ -44,11 +44,12 @@ constexpr int kOptVecs = 8;
 // pair is written once, in the pass that forms it.
 __host__ __device__ constexpr int hist_slots(int m) { return m + 1; }
 
-// Floats of the FP64 two-loop scalars after the vectors: ro per physical slot (m + 1
-// doubles) and al per kept pair (m doubles), rounded up to 16 bytes.
+// Floats of the two-loop scalars after the vectors: ro = 1 / (y . s) per physical slot
+// (m + 1 doubles) and the pairs' coefficients (m slots of 8 bytes, read as FP32), rounded
+// up to 16 bytes.
 __host__ __device__ constexpr int opt_scalar_floats(int m) { return (2 * (2 * m + 1) + 3) / 4 * 4; }
 
-// Carves the vectors from vb (kOptVecs * Dp floats) and the FP64 two-loop scalars ro, al
+// Carves the vectors from vb (kOptVecs * Dp floats) and the two-loop scalars ro, al
 // (opt_scalar_floats(m) floats) after them.
 __device__ __forceinline__ Vecs carve_vecs(float* vb, int Dp, int m) {
     Vecs v;
@@ -353,10 +354,14 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
                     ds_dot_acc(acc, sk[e], -ge);
                 }
             }
+            // The coefficients alpha_k = rho_k s_k . q and alpha_k - beta_k are formed in FP32
+            // from the compensated dot products (each dot rounded once): they scale FP32 vectors,
+            // and keeping them off the FP64 pipe shortens every pass's dependent chain.
+            float* alf = reinterpret_cast<float*>(v.al);
             for (int k = count - 1; k >= 0; --k) {
-                const double al = ds_warp_sum(acc) * v.ro[sl];
-                if (lane == 0) v.al[k] = al;
-                const float nal = static_cast<float>(-al);
+                const float a = ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
+                if (lane == 0) alf[k] = a;
+                const float nal = -a;
                 const float* yk = v.Y + sl * Dp;
                 const int sn_slot = sl == 0 ? slots - 1 : sl - 1;
                 acc = DS{0.f, 0.f};
@@ -382,8 +387,7 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
             // second loop, oldest to newest: d += (al_k - be_k) s_k
             sl = base;
             for (int k = 0; k < count; ++k) {
-                const double be = ds_warp_sum(acc) * v.ro[sl];
-                const float w = static_cast<float>(v.al[k] - be);
+                const float w = alf[k] - ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
                 const float* sk = v.S + sl * Dp;
                 const int nx_slot = sl + 1 == slots ? 0 : sl + 1;
                 const float* nx = k + 1 < count ? v.Y + nx_slot * Dp : v.g;
