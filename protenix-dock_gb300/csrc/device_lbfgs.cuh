@@ -45,8 +45,8 @@ constexpr int kOptVecs = 8;
 __host__ __device__ constexpr int hist_slots(int m) { return m + 1; }
 
 // Floats of the two-loop scalars after the vectors: ro = 1 / (y . s) per physical slot
-// (m + 1 doubles) and the pairs' coefficients (m slots of 8 bytes, read as FP32), rounded
-// up to 16 bytes.
+// (m + 1 doubles) and the pairs' coefficients (m doubles, or FP32 in their first halves),
+// rounded up to 16 bytes.
 __host__ __device__ constexpr int opt_scalar_floats(int m) { return (2 * (2 * m + 1) + 3) / 4 * 4; }
 
 // Carves the vectors from vb (kOptVecs * Dp floats) and the two-loop scalars ro, al
@@ -258,7 +258,7 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
 //
 // energy receives the FP64 objective at the returned pose (energy64), or, with
 // final_energy false (a caller that does not use it), the last FP32 loss.
-template <class Cl>
+template <bool kFast = false, class Cl>
 static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int D,
                           size_t Dp, int lane, double& energy, bool final_energy = true) {
     const int m = p.m;
@@ -354,14 +354,22 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
                     ds_dot_acc(acc, sk[e], -ge);
                 }
             }
-            // The coefficients alpha_k = rho_k s_k . q and alpha_k - beta_k are formed in FP32
-            // from the compensated dot products (each dot rounded once): they scale FP32 vectors,
-            // and keeping them off the FP64 pipe shortens every pass's dependent chain.
+            // kFast: the coefficients alpha_k = rho_k s_k . q and alpha_k - beta_k are formed in
+            // FP32 from the compensated dot products (each dot rounded once) instead of FP64:
+            // they scale FP32 vectors, and off the FP64 pipe every pass's dependent chain is
+            // shorter (the single-walker search's relaxations, 11 % faster).
             float* alf = reinterpret_cast<float*>(v.al);
             for (int k = count - 1; k >= 0; --k) {
-                const float a = ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
-                if (lane == 0) alf[k] = a;
-                const float nal = -a;
+                float nal;
+                if constexpr (kFast) {
+                    const float a = ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
+                    if (lane == 0) alf[k] = a;
+                    nal = -a;
+                } else {
+                    const double al = ds_warp_sum(acc) * v.ro[sl];
+                    if (lane == 0) v.al[k] = al;
+                    nal = static_cast<float>(-al);
+                }
                 const float* yk = v.Y + sl * Dp;
                 const int sn_slot = sl == 0 ? slots - 1 : sl - 1;
                 acc = DS{0.f, 0.f};
@@ -387,7 +395,13 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
             // second loop, oldest to newest: d += (al_k - be_k) s_k
             sl = base;
             for (int k = 0; k < count; ++k) {
-                const float w = alf[k] - ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
+                float w;
+                if constexpr (kFast) {
+                    w = alf[k] - ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
+                } else {
+                    const double be = ds_warp_sum(acc) * v.ro[sl];
+                    w = static_cast<float>(v.al[k] - be);
+                }
                 const float* sk = v.S + sl * Dp;
                 const int nx_slot = sl + 1 == slots ? 0 : sl + 1;
                 const float* nx = k + 1 < count ? v.Y + nx_slot * Dp : v.g;

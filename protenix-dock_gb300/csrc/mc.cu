@@ -239,6 +239,9 @@ __device__ void atomic_min_double(double* p, double v) {
     }
 }
 
+// The relaxations form the two-loop coefficients in FP32 (lbfgs_pose<true>): a walker's warp
+// is usually alone on its SM, where the FP64 operations on each pass's dependent chain are
+// what it waits on.
 __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_constant__ McArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
@@ -332,7 +335,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
         }
         // ---- full relaxation and score of the start (searcher.cpp:120-126)
         double best_e = 0.0;
-        lbfgs_pose(c, a.full, v, D, Dp, lane, best_e);
+        lbfgs_pose<true>(c, a.full, v, D, Dp, lane, best_e);
         long total = c.nevals;
         double best_ps = mc_pscore(a, L, v.x, b, lane);
         vcopy(best_x, v.x, D, lane);
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                         if (pre > gm + a.threshold) continue;
                     }
                     double cdd_e = 0.0;  // unused: the step is judged by its pose score
-                    lbfgs_pose(c, a.fast, v, D, Dp, lane, cdd_e, false);
+                    lbfgs_pose<true>(c, a.fast, v, D, Dp, lane, cdd_e, false);
                     total += c.nevals;
                     const double cdd_ps = mc_pscore(a, L, v.x, b, lane);
                     bool accept = step == 0 || cdd_ps < tmp_ps;
@@ -410,7 +413,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                         tmp_ps = cdd_ps;
                         if (tmp_ps < best_ps) {
                             double e2 = 0.0;
-                            lbfgs_pose(c, a.full, v, D, Dp, lane, e2);
+                            lbfgs_pose<true>(c, a.full, v, D, Dp, lane, e2);
                             total += c.nevals;
                             tmp_ps = mc_pscore(a, L, v.x, b, lane);
                             if (tmp_ps < best_ps) {
