@@ -166,10 +166,10 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
         gpv = g_prev;
         S.gp = S.gn;
         {
-        double gn_new;
-        S.fn = closure_eval(c, S.t, d, g_new, &gn_new);
-        S.gn = gn_new;
-    }
+            double gn_new;
+            S.fn = closure_eval(c, S.t, d, g_new, &gn_new);
+            S.gn = gn_new;
+        }
         ++S.it;
     }
     S.dn = 0.0;
@@ -212,10 +212,10 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
         }
         S.t = t;
         {
-        double gn_new;
-        S.fn = closure_eval(c, S.t, d, g_new, &gn_new);
-        S.gn = gn_new;
-    }
+            double gn_new;
+            S.fn = closure_eval(c, S.t, d, g_new, &gn_new);
+            S.gn = gn_new;
+        }
         ++S.it;
         const int lo = S.lo, hi = S.hi;
         const double bf_lo = lo ? S.bf1 : S.bf0;
@@ -251,6 +251,8 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
 //     d = H_diag q with y_0 . d;
 //   - the second loop: d += (al_k - be_k) s_k fused with the next y_{k+1} . d, the last
 //     step with g . d for the line search.
+// With kRegLoop and D <= 256 both loops keep the direction in registers (two_loop_regs)
+// instead of the shared q and d, with the same arithmetic.
 // Kept pairs sit in physical slots (base + j) % (m + 1), j = 0 .. count - 1 oldest first;
 // the spare slot (base + count) % (m + 1) receives the next pair. The iteration's scalars
 // (loss, step, H_diag, the history ring) live with the line search's in the lane-private
@@ -258,7 +260,113 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
 //
 // energy receives the FP64 objective at the returned pose (energy64), or, with
 // final_energy false (a caller that does not use it), the last FP32 loss.
-template <bool kFast = false, class Cl>
+// The two-loop recursion for D <= E * 32, the direction held in registers (E elements per
+// lane) instead of the shared vectors q and d. Each pass's history elements are loaded
+// before the reduction its coefficient waits on, and no pass stores or reloads the
+// direction, so the only dependent chain left is the reduction itself: what a warp alone on
+// its SM (the single-walker search) waits on. Lane-element order, products and accumulation
+// are those of the shared-vector loops, so the result is the same bit for bit. kF32: the
+// coefficients in FP32 (see lbfgs_pose). Writes g_prev = g and d; returns g . d.
+template <int E, bool kF32>
+static __device__ __forceinline__ double two_loop_regs(const Vecs& v, int base, int count, int slots,
+                                                       size_t Dp, int D, int lane, float hd) {
+    float r[E];
+    int sl = base + count - 1 >= slots ? base + count - 1 - slots : base + count - 1;
+    DS acc{0.f, 0.f};
+    {
+        const float* sk = v.S + sl * Dp;
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const int e = lane + j * kWarp;
+            r[j] = 0.f;
+            if (e < D) {
+                const float ge = v.g[e];
+                r[j] = -ge;
+                v.gp[e] = ge;
+                ds_dot_acc(acc, sk[e], -ge);
+            }
+        }
+    }
+    float* alf = reinterpret_cast<float*>(v.al);
+    for (int k = count - 1; k >= 0; --k) {
+        const float* yk = v.Y + sl * Dp;
+        const int sn_slot = sl == 0 ? slots - 1 : sl - 1;
+        const float* sn = v.S + sn_slot * Dp;
+        float yv[E], sv[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const int e = lane + j * kWarp;
+            yv[j] = e < D ? yk[e] : 0.f;
+            sv[j] = e < D && k > 0 ? sn[e] : 0.f;
+        }
+        float nal;
+        if constexpr (kF32) {
+            const float a = ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
+            if (lane == 0) alf[k] = a;
+            nal = -a;
+        } else {
+            const double al = ds_warp_sum(acc) * v.ro[sl];
+            if (lane == 0) v.al[k] = al;
+            nal = static_cast<float>(-al);
+        }
+        acc = DS{0.f, 0.f};
+        if (k > 0) {
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                if (lane + j * kWarp < D) {
+                    r[j] = fmaf(yv[j], nal, r[j]);
+                    ds_dot_acc(acc, sv[j], r[j]);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                if (lane + j * kWarp < D) {
+                    r[j] = fmaf(yv[j], nal, r[j]) * hd;
+                    ds_dot_acc(acc, yv[j], r[j]);
+                }
+            }
+        }
+        sl = sn_slot;
+    }
+    __syncwarp();  // alf written by lane 0 above, read by every lane below
+    sl = base;
+    for (int k = 0; k < count; ++k) {
+        const float* sk = v.S + sl * Dp;
+        const int nx_slot = sl + 1 == slots ? 0 : sl + 1;
+        const float* nx = k + 1 < count ? v.Y + nx_slot * Dp : v.g;
+        float sv[E], nv[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const int e = lane + j * kWarp;
+            sv[j] = e < D ? sk[e] : 0.f;
+            nv[j] = e < D ? nx[e] : 0.f;
+        }
+        float w;
+        if constexpr (kF32)
+            w = alf[k] - ds_warp_sum_f(acc) * static_cast<float>(v.ro[sl]);
+        else
+            w = static_cast<float>(v.al[k] - ds_warp_sum(acc) * v.ro[sl]);
+        acc = DS{0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            if (lane + j * kWarp < D) {
+                r[j] = fmaf(sv[j], w, r[j]);
+                ds_dot_acc(acc, nv[j], r[j]);
+            }
+        }
+        sl = nx_slot;
+    }
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+        const int e = lane + j * kWarp;
+        if (e < D) v.d[e] = r[j];
+    }
+    __syncwarp();
+    return ds_warp_sum(acc);  // g . d after the last step
+}
+
+template <bool kFast = false, bool kRegLoop = kFast, class Cl>
 static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int D,
                           size_t Dp, int lane, double& energy, bool final_energy = true) {
     const int m = p.m;
@@ -338,6 +446,12 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
             } else {
                 S.t = p.lr;
             }
+        } else if (kRegLoop && D <= 4 * kWarp) {
+            gtd = two_loop_regs<4, kFast>(v, S.base, S.count, slots, Dp, D, lane, static_cast<float>(S.H_diag));
+            S.t = p.lr;
+        } else if (kRegLoop && D <= 8 * kWarp) {
+            gtd = two_loop_regs<8, kFast>(v, S.base, S.count, slots, Dp, D, lane, static_cast<float>(S.H_diag));
+            S.t = p.lr;
         } else {
             // first loop, newest to oldest: q = -g - sum al_k y_k. The ring's base and count
             // are read once into registers: the line-search state lives in the lane's frame,
