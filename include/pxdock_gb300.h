@@ -289,6 +289,38 @@ int pxd_grid_read_map(pxd_context* ctx, int32_t map, float* host_out);
 /* Installs a map from host records (used by load_maps). */
 int pxd_grid_write_map(pxd_context* ctx, const pxd_box* box, int32_t map,
                        const float* host_records);
+/* The same in FP64, as the reference's val_and_grad records (grid.h:54-57) hold them:
+ * read gives E = FP32 record + the map's FP64 energy remainder and the gradient
+ * widened; write rounds E to the FP32 record and keeps the remainder, so a read after a
+ * write returns the energies it was given (to ~2^-48 relative) and reading, writing and
+ * reading again is exact. Used by dump_maps / load_maps with the reference's files. */
+int pxd_grid_read_map64(pxd_context* ctx, int32_t map, double* host_out);
+int pxd_grid_write_map64(pxd_context* ctx, const pxd_box* box, int32_t map,
+                         const double* host_records);
+
+/* ------------------------------------------------ the reference's map cache files */
+
+/* Codec of receptor_cache::save / restore's files (grid.cpp:305-431), host only (no
+ * device is touched): a <tag>.bdg Boost binary archive of one map's
+ * std::vector<val_and_grad> and the meta.dat Boost text archive (format version
+ * 20241030, box origin, points per axis, spacing, excluded receptor atoms).
+ * pxd_bdg_encode: records = n_points x {E, dE/dx, dE/dy, dE/dz}; value_bytes 8 (the
+ * reference's default double build) or 4 (its float build). Returns the archive's
+ * length; the bytes are written only when out_capacity holds them (out may be NULL).
+ * pxd_bdg_decode: returns the point count and sets value_bytes; records are written
+ * only when capacity_points holds them. pxd_meta_encode returns the text length and
+ * writes it NUL-terminated when out_capacity > length. pxd_meta_decode returns the
+ * number of excluded atoms (written when capacity holds them) and sets version; when
+ * version is not 20241030 nothing after it is read. Errors are negative PXD_ERR_* codes
+ * (PXD_ERR_IO: malformed input). */
+int64_t pxd_bdg_encode(const double* records, int64_t n_points, int32_t value_bytes,
+                       uint8_t* out, int64_t out_capacity);
+int64_t pxd_bdg_decode(const uint8_t* data, int64_t size, double* records,
+                       int64_t capacity_points, int32_t* value_bytes);
+int64_t pxd_meta_encode(const pxd_box* box, const int64_t* excluded, int64_t n_excluded,
+                        char* out, int64_t out_capacity);
+int64_t pxd_meta_decode(const char* text, int64_t size, pxd_box* box, uint64_t* version,
+                        int64_t* excluded, int64_t capacity);
 
 /* Registers a ligand's topology and torsion tree on the device. */
 int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* ligand, int32_t* ligand_id);

@@ -9,9 +9,10 @@ RuntimeError with the reference's messages, as its C++ exceptions do through its
 
 Each workflow call runs one batched device launch over every pose (optimize) or every
 walker (search) of every ligand in the index. Differences a caller can see:
-  - dump_maps / load_maps use this library's own cache format (grid.json and one FP32
-    {E, dE/dx, dE/dy, dE/dz} file per map); the reference's Boost archives are not
-    readable here;
+  - dump_maps / load_maps write and read the reference's cache files (<tag>.bdg Boost
+    binary archives of FP64 records and the meta.dat text archive, grid.cpp:305-431);
+    load_maps also reads this library's earlier layout (grid.json + map_NNN.f32), and
+    refuses a cache whose excluded receptor atoms are not this receptor's movable ones;
   - output files are written in index-file order;
   - the extra keyword `device` (default 0) picks the CUDA device;
   - optimize and search take the extra keywords `rank` and `world` (default 0 and 1, the

@@ -884,12 +884,16 @@ int pxd_grid_info(pxd_context* ctx, pxd_box* box, int32_t* n_maps) {
     return PXD_OK;
 }
 
+static int map_slot(pxd_context* ctx, int32_t map) {
+    if (map == PXD_NUM_VDW_TYPES) return 0;
+    if (map >= 0 && map < PXD_NUM_VDW_TYPES) return ctx->type_slot[map];
+    return -1;
+}
+
 int pxd_grid_read_map(pxd_context* ctx, int32_t map, float* host_out) {
     if (!ctx || !host_out) return PXD_ERR_INVALID;
     if (!ctx->grid.has_grid) return set_error(ctx, PXD_ERR_STATE, "no maps");
-    int slot = -1;
-    if (map == PXD_NUM_VDW_TYPES) slot = 0;
-    else if (map >= 0 && map < PXD_NUM_VDW_TYPES) slot = ctx->type_slot[map];
+    const int slot = map_slot(ctx, map);
     if (slot < 0) return set_error(ctx, PXD_ERR_INVALID, "map not built");
     cudaSetDevice(ctx->device);
     return cuda_check(ctx, cudaMemcpy(host_out, ctx->maps + static_cast<size_t>(slot) * ctx->grid.P,
@@ -897,8 +901,35 @@ int pxd_grid_read_map(pxd_context* ctx, int32_t map, float* host_out) {
                       "map read");
 }
 
-int pxd_grid_write_map(pxd_context* ctx, const pxd_box* box, int32_t map, const float* host_records) {
-    if (!ctx || !box || !host_records) return PXD_ERR_INVALID;
+int pxd_grid_read_map64(pxd_context* ctx, int32_t map, double* host_out) {
+    if (!ctx || !host_out) return PXD_ERR_INVALID;
+    if (!ctx->grid.has_grid) return set_error(ctx, PXD_ERR_STATE, "no maps");
+    const int slot = map_slot(ctx, map);
+    if (slot < 0) return set_error(ctx, PXD_ERR_INVALID, "map not built");
+    const size_t P = ctx->grid.P;
+    std::vector<float4> rec(P);
+    std::vector<float> lo(P);
+    cudaSetDevice(ctx->device);
+    int rc = cuda_check(ctx, cudaMemcpy(rec.data(), ctx->maps + static_cast<size_t>(slot) * P, sizeof(float4) * P,
+                                        cudaMemcpyDeviceToHost),
+                        "map read");
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpy(lo.data(), ctx->grid.e_lo + static_cast<size_t>(slot) * P, sizeof(float) * P,
+                                        cudaMemcpyDeviceToHost),
+                        "map remainder read");
+    if (rc) return rc;
+    for (size_t p = 0; p < P; ++p) {
+        host_out[4 * p] = static_cast<double>(rec[p].x) + static_cast<double>(lo[p]);
+        host_out[4 * p + 1] = rec[p].y;
+        host_out[4 * p + 2] = rec[p].z;
+        host_out[4 * p + 3] = rec[p].w;
+    }
+    return PXD_OK;
+}
+
+// Installs one map's FP32 records and FP64 energy remainders (e_lo_host, or zeros).
+static int install_map(pxd_context* ctx, const pxd_box* box, int32_t map, const float* host_records,
+                       const float* e_lo_host) {
     if (map < 0 || map > PXD_NUM_VDW_TYPES) return set_error(ctx, PXD_ERR_INVALID, "map index");
     cudaSetDevice(ctx->device);
     const bool same = ctx->grid.has_grid && std::memcmp(&ctx->box, box, sizeof(pxd_box)) == 0;
@@ -917,10 +948,12 @@ int pxd_grid_write_map(pxd_context* ctx, const pxd_box* box, int32_t map, const 
                                         sizeof(float4) * ctx->grid.P, cudaMemcpyHostToDevice),
                         "map write");
     if (rc) return rc;
-    // an installed FP32 record set carries no FP64 residual: its energies are the records'
-    rc = cuda_check(ctx, cudaMemset(const_cast<float*>(ctx->grid.e_lo) + static_cast<size_t>(slot) * ctx->grid.P, 0,
-                                    sizeof(float) * ctx->grid.P),
-                    "map residual clear");
+    float* lo = const_cast<float*>(ctx->grid.e_lo) + static_cast<size_t>(slot) * ctx->grid.P;
+    if (e_lo_host)
+        rc = cuda_check(ctx, cudaMemcpy(lo, e_lo_host, sizeof(float) * ctx->grid.P, cudaMemcpyHostToDevice),
+                        "map remainder write");
+    else  // an installed FP32 record set carries no FP64 remainder: its energies are the records'
+        rc = cuda_check(ctx, cudaMemset(lo, 0, sizeof(float) * ctx->grid.P), "map remainder clear");
     if (rc) return rc;
     if (ctx->has_receptor) point_explicit(ctx, true);
     rc = refresh_ligand_slots(ctx);
@@ -931,6 +964,30 @@ int pxd_grid_write_map(pxd_context* ctx, const pxd_box* box, int32_t map, const 
         return set_error(ctx, rc, msg + " (maps dropped)");
     }
     return PXD_OK;
+}
+
+int pxd_grid_write_map(pxd_context* ctx, const pxd_box* box, int32_t map, const float* host_records) {
+    if (!ctx || !box || !host_records) return PXD_ERR_INVALID;
+    return install_map(ctx, box, map, host_records, nullptr);
+}
+
+int pxd_grid_write_map64(pxd_context* ctx, const pxd_box* box, int32_t map, const double* host_records) {
+    if (!ctx || !box || !host_records) return PXD_ERR_INVALID;
+    const size_t P = static_cast<size_t>(box->npoints[0]) * box->npoints[1] * box->npoints[2];
+    if (box->npoints[0] < 2 || box->npoints[1] < 2 || box->npoints[2] < 2)
+        return set_error(ctx, PXD_ERR_INVALID, "points per axis");
+    std::vector<float> rec(4 * P), lo(P);
+    for (size_t p = 0; p < P; ++p) {
+        const double e = host_records[4 * p];
+        // the grid build's record rule: clamp to +-1e30, E rounded to FP32, remainder kept
+        const double ec = std::fmin(std::fmax(e, -1e30), 1e30);
+        const float hi = static_cast<float>(ec);
+        rec[4 * p] = hi;
+        lo[p] = std::fabs(e) < 1e30 ? static_cast<float>(e - static_cast<double>(hi)) : 0.f;
+        for (int c = 1; c < 4; ++c)
+            rec[4 * p + c] = static_cast<float>(std::fmin(std::fmax(host_records[4 * p + c], -1e30), 1e30));
+    }
+    return install_map(ctx, box, map, rec.data(), lo.data());
 }
 
 int pxd_add_ligand(pxd_context* ctx, const pxd_ligand_desc* lig, int32_t* ligand_id) {

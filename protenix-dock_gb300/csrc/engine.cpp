@@ -15,8 +15,10 @@
 #include <sstream>
 #include <stdexcept>
 
+#include "../../include/pxdock_gb300_vdw.h"
 #include "inputs.h"
 #include "json.h"
+#include "mapcache.h"
 
 namespace pxd {
 
@@ -335,33 +337,101 @@ void Engine::drop_maps() {
     has_maps_ = false;
 }
 
+// This library's earlier cache layout (grid.json + map_NNN.f32), still read by load_maps.
 static const char* kMapFormat = "pxdock-gb300 maps 1";
 
+// The receptor atoms the maps leave out (receptor_cache::populate's excluded_, grid.cpp:118-123):
+// every rotor leaf's atoms but the axis atom they turn about (data.cpp:349-363), ascending.
+static std::vector<int64_t> excluded_atoms(const ReceptorData& r) {
+    std::vector<int64_t> out;
+    const size_t n_rot = r.rotor_axis.size() / 2;
+    for (size_t k = 0; k < n_rot && k + 1 < r.rotor_offsets.size(); ++k)
+        for (int u = r.rotor_offsets[k]; u < r.rotor_offsets[k + 1]; ++u)
+            if (r.rotor_atoms[u] != r.rotor_axis[2 * k + 1]) out.push_back(r.rotor_atoms[u]);
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+    return out;
+}
+
+static std::vector<uint8_t> read_bytes(const std::string& path) {
+    std::ifstream in(path, std::ios::binary | std::ios::ate);
+    if (!in) throw std::runtime_error("Failed to open file for reading: " + path);
+    const std::streamsize n = in.tellg();
+    std::vector<uint8_t> b(static_cast<size_t>(n));
+    in.seekg(0);
+    if (n > 0 && !in.read(reinterpret_cast<char*>(b.data()), n)) throw std::runtime_error("Failed to read " + path);
+    return b;
+}
+
+// receptor_cache::save (grid.cpp:309-345): <tag>.bdg per ligand type and coul.bdg, FP64
+// records, then meta.dat last as the completion flag.
 void Engine::dump_maps(const std::string& cache_dir) {
     require_maps();
     make_dirs(cache_dir);
     const size_t P = static_cast<size_t>(grid_.npoints[0]) * grid_.npoints[1] * grid_.npoints[2];
-    std::vector<float> rec(P * 4);
+    std::vector<double> rec(P * 4);
     for (int m = 0; m <= PXD_NUM_VDW_TYPES; ++m) {
-        check(ctx_, pxd_grid_read_map(ctx_, m, rec.data()));
-        char name[32];
-        std::snprintf(name, sizeof(name), "map_%03d.f32", m);
-        std::ofstream out(join(cache_dir, name), std::ios::binary);
-        out.write(reinterpret_cast<const char*>(rec.data()), static_cast<std::streamsize>(rec.size() * sizeof(float)));
-        if (!out) throw std::runtime_error("Failed to write map file in " + cache_dir);
+        check(ctx_, pxd_grid_read_map64(ctx_, m, rec.data()));
+        const std::vector<uint8_t> bytes = mapcache::encode_bdg(rec.data(), P, 8);
+        const std::string path = join(cache_dir, std::string(PXD_VDW_TAGS[m]) + ".bdg");
+        std::ofstream out(path, std::ios::binary);
+        out.write(reinterpret_cast<const char*>(bytes.data()), static_cast<std::streamsize>(bytes.size()));
+        if (!out) throw std::runtime_error("Failed to write map file: " + path);
     }
-    std::ofstream meta(join(cache_dir, "grid.json"));
-    meta << std::setprecision(17) << "{\"format\": \"" << kMapFormat << "\", \"init_xyz\": [" << grid_.init_xyz[0] << ", "
-         << grid_.init_xyz[1] << ", " << grid_.init_xyz[2] << "], \"npoints\": [" << grid_.npoints[0] << ", "
-         << grid_.npoints[1] << ", " << grid_.npoints[2] << "], \"spacing\": " << grid_.spacing << ", \"maps\": [";
-    for (int m = 0; m <= PXD_NUM_VDW_TYPES; ++m) meta << (m ? ", " : "") << m;
-    meta << "]}\n";
-    if (!meta) throw std::runtime_error("Failed to write the map metadata in " + cache_dir);
+    mapcache::Meta meta;
+    meta.box = grid_;
+    meta.excluded = excluded_atoms(*receptor_);
+    std::ofstream out(join(cache_dir, "meta.dat"));
+    out << mapcache::encode_meta(meta);
+    if (!out) throw std::runtime_error("Failed to write the map metadata in " + cache_dir);
 }
 
+// receptor_cache::restore (grid.cpp:347-391, 408-431), with its messages; a cache in this
+// library's earlier layout (grid.json) is read as well.
 void Engine::load_maps(const std::string& cache_dir) {
+    const std::string meta_path = join(cache_dir, "meta.dat");
+    if (!is_file(meta_path)) {
+        if (is_file(join(cache_dir, "grid.json"))) return load_own_maps(cache_dir);
+        throw std::runtime_error("The metadata file of maps is missing!");
+    }
+    std::ifstream in(meta_path);
+    std::stringstream text;
+    text << in.rdbuf();
+    const mapcache::Meta meta = mapcache::decode_meta(text.str());
+    if (meta.version != mapcache::kFormatVersion) {
+        std::ostringstream oss;
+        oss << "Format version of map files are not compatible! Expected [" << mapcache::kFormatVersion << "] vs. Got ["
+            << meta.version << "]";
+        throw std::runtime_error(oss.str());
+    }
+    std::vector<int64_t> excl = meta.excluded;
+    std::sort(excl.begin(), excl.end());
+    excl.erase(std::unique(excl.begin(), excl.end()), excl.end());
+    if (excl != excluded_atoms(*receptor_))
+        throw std::runtime_error("The maps in " + cache_dir +
+                                 " leave out other receptor atoms than this receptor's movable ones");
+    const pxd_box b = meta.box;
+    const size_t P = static_cast<size_t>(b.npoints[0]) * b.npoints[1] * b.npoints[2];
+    for (int m = 0; m <= PXD_NUM_VDW_TYPES; ++m) {
+        const std::string path = join(cache_dir, std::string(PXD_VDW_TAGS[m]) + ".bdg");
+        if (!is_file(path))
+            throw std::runtime_error(std::string("Map file for atom type [") + PXD_VDW_TAGS[m] + "] is missing!");
+        const std::vector<uint8_t> bytes = read_bytes(path);
+        std::vector<double> rec;
+        try {
+            rec = mapcache::decode_bdg(bytes.data(), bytes.size(), nullptr);
+        } catch (const std::exception& e) {
+            throw std::runtime_error(path + ": " + e.what());
+        }
+        if (rec.size() != 4 * P) throw std::runtime_error(path + ": point count does not match meta.dat's box");
+        check(ctx_, pxd_grid_write_map64(ctx_, &b, m, rec.data()));
+    }
+    grid_ = b;
+    has_maps_ = true;
+}
+
+void Engine::load_own_maps(const std::string& cache_dir) {
     const std::string meta = join(cache_dir, "grid.json");
-    if (!is_file(meta)) throw std::runtime_error("The metadata file of maps is missing!");
     const json::Value head = json::parse_file(meta);
     if (head.at("format").str != kMapFormat) throw std::runtime_error("Unknown map cache format in " + cache_dir);
     pxd_box b{};

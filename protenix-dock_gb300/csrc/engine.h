@@ -49,6 +49,7 @@ public:
 private:
     void require_box() const;
     void require_maps() const;
+    void load_own_maps(const std::string& cache_dir);
     pxd_context* ctx_ = nullptr;
     std::unique_ptr<ReceptorData> receptor_;
     std::vector<double> box_;  // set_box appends, as the reference's box_ vector does

@@ -49,6 +49,17 @@ def load(auto_build=False):
     lib.pxd_grid_info.argtypes = [vp, C.POINTER(abi.Box), abi.i32p]
     lib.pxd_grid_read_map.argtypes = [vp, C.c_int32, abi.f32p]
     lib.pxd_grid_write_map.argtypes = [vp, C.POINTER(abi.Box), C.c_int32, abi.f32p]
+    lib.pxd_grid_read_map64.argtypes = [vp, C.c_int32, abi.f64p]
+    lib.pxd_grid_write_map64.argtypes = [vp, C.POINTER(abi.Box), C.c_int32, abi.f64p]
+    lib.pxd_bdg_encode.argtypes = [abi.f64p, C.c_int64, C.c_int32, C.c_char_p, C.c_int64]
+    lib.pxd_bdg_encode.restype = C.c_int64
+    lib.pxd_bdg_decode.argtypes = [C.c_char_p, C.c_int64, abi.f64p, C.c_int64, abi.i32p]
+    lib.pxd_bdg_decode.restype = C.c_int64
+    lib.pxd_meta_encode.argtypes = [C.POINTER(abi.Box), C.POINTER(C.c_int64), C.c_int64, C.c_char_p, C.c_int64]
+    lib.pxd_meta_encode.restype = C.c_int64
+    lib.pxd_meta_decode.argtypes = [C.c_char_p, C.c_int64, C.POINTER(abi.Box), C.POINTER(C.c_uint64),
+                                    C.POINTER(C.c_int64), C.c_int64]
+    lib.pxd_meta_decode.restype = C.c_int64
     lib.pxd_add_ligand.argtypes = [vp, C.POINTER(abi.LigandDesc), abi.i32p]
     lib.pxd_clear_ligands.argtypes = [vp]
     lib.pxd_score_grad_dev.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp]

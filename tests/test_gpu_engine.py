@@ -9,7 +9,8 @@ outputs (tests/golden/engine, written by oracle/_ref).
 - search: schema, at most num_modes poses sorted by pose score, poses inside the box,
   every energy / score the FP64 value at the pose; the best pose score no worse than the
   FP64 port's walkers (from the same and from FP32-rounded starts) by more than 1 kcal/mol;
-- dump_maps / load_maps round trip; the reference's precondition errors.
+- dump_maps / load_maps round trip through the reference's cache files (.bdg + meta.dat)
+  and restore's errors; the reference's precondition errors.
 """
 import csv
 import json
@@ -20,7 +21,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from pxdock_gb300 import abi, model
+from pxdock_gb300 import abi, mapcache, model
 
 import _protenix_dock as E
 
@@ -176,9 +177,20 @@ def test_optimize_rigid_body_torsion_mode(setup):
 
 
 def test_maps_round_trip(setup):
+    """dump_maps writes the reference's cache (a <tag>.bdg per ligand type, coul.bdg,
+    meta.dat); a second engine loads it and optimises to the same file."""
     s = setup
     cache = s["dir"] / "maps"
     s["eng"].dump_maps(str(cache))
+    names = os.listdir(cache)
+    assert "meta.dat" in names and "coul.bdg" in names and "c.bdg" in names
+    assert len([n for n in names if n.endswith(".bdg")]) == 100
+    meta = mapcache.decode_meta((cache / "meta.dat").read_text())
+    assert meta["version"] == mapcache.FORMAT_VERSION and meta["spacing"] == s["calls"]["spacing"]
+    movable = {a for (_, axis), g in zip(s["rec"].rotor_axis, s["rec"].rotor_groups) for a in g if a != axis}
+    assert sorted(meta["excluded"]) == sorted(movable) and movable
+    rec, vb = mapcache.decode_bdg((cache / "coul.bdg").read_bytes())
+    assert vb == 8 and rec.shape[0] == int(np.prod(meta["npoints"]))
     a = s["dir"] / "opt_a"
     s["eng"].optimize(str(s["dir"] / "index.txt"), str(a), max_niters=10)
     other = E.ReusableEngine(str(s["dir"] / "receptor.json"), SF)
@@ -186,6 +198,32 @@ def test_maps_round_trip(setup):
     b = s["dir"] / "opt_b"
     other.optimize(str(s["dir"] / "index.txt"), str(b), max_niters=10)
     assert (a / "ligand_out.json").read_text() == (b / "ligand_out.json").read_text()
+    # dumped again from the loaded maps: the same bytes
+    again = s["dir"] / "maps_again"
+    other.dump_maps(str(again))
+    for n in ("coul.bdg", "c.bdg", "sq.bdg", "meta.dat"):
+        assert (again / n).read_bytes() == (cache / n).read_bytes(), n
+
+
+def test_map_cache_errors(setup):
+    """receptor_cache::restore's messages (grid.cpp:347-431)."""
+    s = setup
+    src = s["dir"] / "maps_err_src"
+    s["eng"].dump_maps(str(src))
+    eng = E.ReusableEngine(str(s["dir"] / "receptor.json"), SF)
+    bad = s["dir"] / "maps_err"
+    shutil.copytree(src, bad)
+    (bad / "meta.dat").write_text((src / "meta.dat").read_text().replace(" 20241030 ", " 20240101 "))
+    with pytest.raises(RuntimeError, match=r"Format version of map files are not compatible! "
+                                           r"Expected \[20241030\] vs. Got \[20240101\]"):
+        eng.load_maps(str(bad))
+    shutil.copy(src / "meta.dat", bad / "meta.dat")
+    os.remove(bad / "cl.bdg")
+    with pytest.raises(RuntimeError, match=r"Map file for atom type \[cl\] is missing!"):
+        eng.load_maps(str(bad))
+    os.remove(bad / "meta.dat")
+    with pytest.raises(RuntimeError, match="The metadata file of maps is missing!"):
+        eng.load_maps(str(bad))
 
 
 def test_precondition_errors(setup):
