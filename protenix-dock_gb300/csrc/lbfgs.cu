@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
             for (int e = lane; e < D; e += kWarp)
                 v.x[e] = e == 0 ? c0.x : e == 1 ? c0.y : e == 2 ? c0.z : e == 3 ? 1.f : e < 7 + T ? 0.f : pt[e - 7 - T];
             __syncwarp();
-            st = lbfgs_pose(c, a.c, v, D, Dp, lane, energy);
+            st = lbfgs_pose<false, true>(c, a.c, v, D, Dp, lane, energy);
             // the final energy placed the returned variables: c.xc is the returned pose
             for (int e = lane; e < 3 * N; e += kWarp) px[e] = c.xc[e];
             for (int r = lane; r < R; r += kWarp) pt[r] = c.xc[3 * N + r];
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * kWarp, kMinBlocks > 0 ? kMinB
             for (int e = lane; e < 3 * N; e += kWarp) v.x[e] = px[e];
             for (int r = lane; r < R; r += kWarp) v.x[3 * N + r] = pt[r];
             __syncwarp();
-            st = lbfgs_pose(c, a.c, v, D, Dp, lane, energy);
+            st = lbfgs_pose<false, true>(c, a.c, v, D, Dp, lane, energy);
             for (int e = lane; e < 3 * N; e += kWarp) px[e] = v.x[e];
             for (int r = lane; r < R; r += kWarp) pt[r] = v.x[3 * N + r];
         }
