@@ -267,6 +267,118 @@ static __device__ void strong_wolfe(Cl& c, const LbfgsConsts& p, const float* d,
 // its SM (the single-walker search) waits on. Lane-element order, products and accumulation
 // are those of the shared-vector loops, so the result is the same bit for bit. kF32: the
 // coefficients in FP32 (see lbfgs_pose). Writes g_prev = g and d; returns g . d.
+// Dot product of a lane's E register elements (x[j] * y[j] where lane + 32 j < D) with
+// the products' exact errors, summed as a pairwise two-sum tree (depth log2 E instead of E
+// dependent compensated additions), rounded once to FP32, then summed over the warp by a
+// plain FP32 butterfly: the same value on every lane. The single-walker search's two-loop
+// dot products, whose dependent chain is what a warp alone on its SM waits on.
+template <int E>
+__device__ __forceinline__ float lane_tree_warp_dot(const float* x, const float* y, int lane, int D) {
+    float p[E], pe = 0.f;
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+        const bool ok = lane + j * kWarp < D;
+        const float a = ok ? x[j] : 0.f, b = ok ? y[j] : 0.f;
+        p[j] = a * b;
+        pe += fmaf(a, b, -p[j]);
+    }
+#pragma unroll
+    for (int w = 1; w < E; w *= 2) {
+#pragma unroll
+        for (int j = 0; j + w < E; j += 2 * w) {
+            const float s = p[j] + p[j + w];
+            const float bb = s - p[j];
+            pe += (p[j] - (s - bb)) + (p[j + w] - bb);
+            p[j] = s;
+        }
+    }
+    float f = p[0] + pe;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) f += __shfl_xor_sync(kFull, f, off);
+    return f;
+}
+
+// two_loop_regs with FP32 coefficients and the per-pass dot products of
+// lane_tree_warp_dot (the single-walker search). Writes g_prev = g and d; returns g . d.
+template <int E>
+static __device__ __forceinline__ double two_loop_regs_tree(const Vecs& v, int base, int count, int slots,
+                                                            size_t Dp, int D, int lane, float hd) {
+    float r[E], xv[E];
+    int sl = base + count - 1 >= slots ? base + count - 1 - slots : base + count - 1;
+    {
+        const float* sk = v.S + sl * Dp;
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const int e = lane + j * kWarp;
+            r[j] = 0.f;
+            xv[j] = 0.f;
+            if (e < D) {
+                const float ge = v.g[e];
+                r[j] = -ge;
+                v.gp[e] = ge;
+                xv[j] = sk[e];
+            }
+        }
+    }
+    float dot = lane_tree_warp_dot<E>(xv, r, lane, D);
+    float* alf = reinterpret_cast<float*>(v.al);
+    for (int k = count - 1; k >= 0; --k) {
+        const float* yk = v.Y + sl * Dp;
+        const int sn_slot = sl == 0 ? slots - 1 : sl - 1;
+        const float* sn = v.S + sn_slot * Dp;
+        float yv[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const int e = lane + j * kWarp;
+            yv[j] = e < D ? yk[e] : 0.f;
+            xv[j] = e < D && k > 0 ? sn[e] : 0.f;
+        }
+        const float a = dot * static_cast<float>(v.ro[sl]);
+        alf[k] = a;  // every lane holds the same value
+#pragma unroll
+        for (int j = 0; j < E; ++j) r[j] = fmaf(yv[j], -a, r[j]);
+        if (k > 0) {
+            dot = lane_tree_warp_dot<E>(xv, r, lane, D);
+        } else {
+#pragma unroll
+            for (int j = 0; j < E; ++j) r[j] *= hd;
+            dot = lane_tree_warp_dot<E>(yv, r, lane, D);
+        }
+        sl = sn_slot;
+    }
+    __syncwarp();
+    sl = base;
+    for (int k = 0; k < count; ++k) {
+        const float* sk = v.S + sl * Dp;
+        const int nx_slot = sl + 1 == slots ? 0 : sl + 1;
+        const float* nx = k + 1 < count ? v.Y + nx_slot * Dp : v.g;
+        float sv[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const int e = lane + j * kWarp;
+            sv[j] = e < D ? sk[e] : 0.f;
+            xv[j] = e < D ? nx[e] : 0.f;
+        }
+        const float w = alf[k] - dot * static_cast<float>(v.ro[sl]);
+#pragma unroll
+        for (int j = 0; j < E; ++j) r[j] = fmaf(sv[j], w, r[j]);
+        if (k + 1 < count) dot = lane_tree_warp_dot<E>(xv, r, lane, D);
+        sl = nx_slot;
+    }
+    // g . d for the line search, compensated as elsewhere
+    DS acc{0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+        const int e = lane + j * kWarp;
+        if (e < D) {
+            v.d[e] = r[j];
+            ds_dot_acc(acc, v.g[e], r[j]);
+        }
+    }
+    __syncwarp();
+    return ds_warp_sum(acc);
+}
+
 template <int E, bool kF32>
 static __device__ __forceinline__ double two_loop_regs(const Vecs& v, int base, int count, int slots,
                                                        size_t Dp, int D, int lane, float hd) {
@@ -446,6 +558,12 @@ static __device__ int lbfgs_pose(Cl& c, const LbfgsConsts& p, const Vecs& v, int
             } else {
                 S.t = p.lr;
             }
+        } else if (kFast && D <= 4 * kWarp) {
+            gtd = two_loop_regs_tree<4>(v, S.base, S.count, slots, Dp, D, lane, static_cast<float>(S.H_diag));
+            S.t = p.lr;
+        } else if (kFast && D <= 8 * kWarp) {
+            gtd = two_loop_regs_tree<8>(v, S.base, S.count, slots, Dp, D, lane, static_cast<float>(S.H_diag));
+            S.t = p.lr;
         } else if (kRegLoop && D <= 4 * kWarp) {
             gtd = two_loop_regs<4, kFast>(v, S.base, S.count, slots, Dp, D, lane, static_cast<float>(S.H_diag));
             S.t = p.lr;
