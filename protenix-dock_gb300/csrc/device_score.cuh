@@ -103,21 +103,27 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
 #pragma unroll
     for (int k = 0; k < PXD_NUM_TERMS - 1; ++k) acc[k] = DS{0.f, 0.f};
     const bool coul = sf.coef[PXD_TERM_COULOMB] != 0.f, vdw = sf.coef[PXD_TERM_VDW] != 0.f;
-    // Coulomb and clamped LJ over every ligand x receptor pair (scorer.cpp:222-276)
+    // Coulomb and clamped LJ over every ligand x receptor pair (scorer.cpp:222-276). Each
+    // lane takes receptor atoms and walks the ligand atoms (shared memory and L1-resident
+    // records, read by every lane at once): a receptor atom's records are loaded once per
+    // call instead of once per ligand atom, which leaves a lone warp (the single-walker
+    // search) arithmetic instead of load latency. The pairs are the same; their sum runs
+    // in another order.
     if (coul || vdw) {
-        for (int i = 0; i < N; ++i) {
-            const float3 xi = xyz(X[i]);
-            const float qi = __ldg(&L.charge[i]);
-            const float2 ti = sf.vdw_type[__ldg(&L.type[i])];
+        for (int j = lane; j < rs.n_all; j += kWarp) {
+            const float4 rj = __ldg(&rs.all_xyzq[j]);
+            const int l = __ldg(&rs.all_local[j]);
+            const float3 xj = l >= 0 ? xyz(loc_xyz[l]) : xyz(rj);
+            const float2 sej = __ldg(&rs.all_se[j]);
             float ec = 0.f, ev = 0.f;
-            for (int j = lane; j < rs.n_all; j += kWarp) {
-                const float4 rj = __ldg(&rs.all_xyzq[j]);
-                const int l = __ldg(&rs.all_local[j]);
-                const float3 xj = l >= 0 ? xyz(loc_xyz[l]) : xyz(rj);
+#pragma unroll 4
+            for (int i = 0; i < N; ++i) {
+                const float3 xi = xyz(X[i]);
+                const float qi = __ldg(&L.charge[i]);
+                const float2 ti = sf.vdw_type[__ldg(&L.type[i])];
                 const float d = dist3(xi, xj);
                 const float rinv = 1.f / (d + kEpsF);
                 ec = fmaf(qi * rj.w, rinv, ec);
-                const float2 sej = __ldg(&rs.all_se[j]);
                 const float s = (ti.x + sej.x) * 0.5f * rinv;
                 const float s2 = s * s;
                 const float u6 = s2 * s2 * s2;
