@@ -60,6 +60,18 @@ __device__ __forceinline__ double ds_warp_sum(DS v) {
     return static_cast<double>(v.hi) + static_cast<double>(v.lo);
 }
 
+// The same butterfly, the compensated pair kept (identical on every lane).
+__device__ __forceinline__ DS ds_warp_reduce(DS v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        DS o;
+        o.hi = __shfl_xor_sync(kFull, v.hi, off);
+        o.lo = __shfl_xor_sync(kFull, v.lo, off);
+        ds_add_ds(v, o);
+    }
+    return v;
+}
+
 // Butterfly reductions leave every lane with the same value (max and a two-operand sum
 // commute), so they need no final broadcast.
 // The warp sum rounded once to FP32 (hi + lo), without leaving the FP32 pipe.
@@ -209,15 +221,19 @@ __device__ __forceinline__ float3 pair_grad(float4 p, float4 xi, float4 xj, floa
 // slots (-1) compute nothing. Every loop runs a multiple of 32 slots, so all lanes
 // meet every barrier. The caller sums the arrays. Matches
 // intra_molecular_interactions::put_gradients.
+//
+// A team of nw warps (warp w of them) splits the rounds: warp w takes rounds w, w + nw, ...
+// into its own arrays G (nw = 1: every round).
 __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, float4* G, int gs, DS& e,
-                                           int lane) {
+                                           int lane, int w = 0, int nw = 1) {
     float4* G0 = G;
     float4* G1 = G + gs;
     float4* G2 = G + 2 * gs;
     float4* G3 = G + 3 * gs;
+    const int first = lane + w * kWarp, step = nw * kWarp;
     __syncwarp();
     // harmonic bonds (interaction.cpp:27-47)
-    for (int s = lane; s < t.n_bond_slots; s += kWarp) {
+    for (int s = first; s < t.n_bond_slots; s += step) {
         const int2 ij = __ldg(&t.bond_ij[s]);
         if (ij.x >= 0) {
             const float2 p = __ldg(&t.bond_p[s]);
@@ -233,7 +249,7 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
         __syncwarp();
     }
     // harmonic angles (interaction.cpp:49-74, math.cpp:96-110)
-    for (int s = lane; s < t.n_angle_slots; s += kWarp) {
+    for (int s = first; s < t.n_angle_slots; s += step) {
         const int4 ijk = __ldg(&t.angle_ijk[s]);
         if (ijk.x >= 0) {
             const float2 p = __ldg(&t.angle_p[s]);
@@ -256,7 +272,7 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
         __syncwarp();
     }
     // Fourier dihedrals, impropers then propers (interaction.cpp:76-117, math.cpp:130-167)
-    for (int s = lane; s < t.n_dih_slots; s += kWarp) {
+    for (int s = first; s < t.n_dih_slots; s += step) {
         const int4 q = __ldg(&t.dih_ijkl[s]);
         if (q.x >= 0) {
             const float3 pi = xyz(X[q.x]), pj = xyz(X[q.y]), pk = xyz(X[q.z]), pl = xyz(X[q.w]);
@@ -300,14 +316,14 @@ __device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, fl
     // 1-4 and all other pairs: Coulomb + LJ 12-6 (interaction.cpp:127-168, pair.h:25-60).
     // The next round's record is loaded while this round computes, so its L1/L2 latency
     // is not exposed at the round's barrier (the pair rounds are the most numerous).
-    int2 ij_n = lane < t.n_pair_slots ? __ldg(&t.pair_ij[lane]) : make_int2(-1, -1);
-    float4 p_n = lane < t.n_pair_slots ? __ldg(&t.pair_p[lane]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int s = lane; s < t.n_pair_slots; s += kWarp) {
+    int2 ij_n = first < t.n_pair_slots ? __ldg(&t.pair_ij[first]) : make_int2(-1, -1);
+    float4 p_n = first < t.n_pair_slots ? __ldg(&t.pair_p[first]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = first; s < t.n_pair_slots; s += step) {
         const int2 ij = ij_n;
         const float4 pp = p_n;
-        if (s + kWarp < t.n_pair_slots) {
-            ij_n = __ldg(&t.pair_ij[s + kWarp]);
-            p_n = __ldg(&t.pair_p[s + kWarp]);
+        if (s + step < t.n_pair_slots) {
+            ij_n = __ldg(&t.pair_ij[s + step]);
+            p_n = __ldg(&t.pair_p[s + step]);
         }
         if (ij.x >= 0) {
             float en;
@@ -396,6 +412,53 @@ __device__ __forceinline__ float grid_lookup(const DevGrid& g, int slot, float q
     return e;
 }
 
+// A team of warps of one block that evaluate one pose together (the single-walker
+// search): the shared barrier state and each member's energy partial.
+struct TeamShared {
+    int count, gen, abort, slot;
+    double gmin;
+    float2 e[4];
+};
+
+// Spin limit of a team barrier: ~0.1 s at the loop's pace, far beyond any wait of members
+// doing the same work. A member that is not seen by then sets abort: the team's later
+// barriers return at once and its evaluations return NaN, so the search ends.
+constexpr long long kTeamSpin = 1LL << 22;
+
+// Barrier of the nw warps of a team (all lanes of each member call it). Orders the
+// members' earlier shared-memory writes before their later reads. Returns false once the
+// team has aborted.
+static __device__ __noinline__ bool team_sync(TeamShared* ts, int nw, int lane) {
+    __threadfence_block();
+    __syncwarp();
+    int ok = 1;
+    if (lane == 0) {
+        volatile int* vgen = &ts->gen;
+        volatile int* vabort = &ts->abort;
+        if (*vabort) {
+            ok = 0;
+        } else {
+            const int g = *vgen;
+            if (atomicAdd(&ts->count, 1) == nw - 1) {
+                atomicExch(&ts->count, 0);
+                __threadfence_block();
+                atomicAdd(&ts->gen, 1);
+            } else {
+                for (long long it = 0; *vgen == g; ++it) {
+                    if (it > kTeamSpin || *vabort) {
+                        atomicExch(&ts->abort, 1);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    __threadfence_block();
+    return __shfl_sync(kFull, ok, 0) != 0;
+}
+
 // Per-warp shared-memory slice for one pose evaluation.
 struct PoseBufs {
     float4* lig_xyz;   // [N]
@@ -404,6 +467,10 @@ struct PoseBufs {
     float4* loc_grad;  // [4][n_local]
     float4* mov_jac;   // [n_mov]
     int lig_gs, loc_gs;  // array strides
+    // team evaluation: this warp's index, the team's size, the float4 distance between
+    // members' slices and the team's shared state (team_n = 1: a warp alone)
+    int team_w, team_n, team_f4;
+    TeamShared* ts;
 };
 
 struct EvalEnv {
@@ -416,6 +483,7 @@ struct EvalEnv {
 // directional derivative), accumulated while the flat gradient is written. Replaces
 // binding_system_interactions::put_gradients as the optimiser's closure calls it
 // (optimizer.cpp:155-167).
+template <bool kTeam = false>
 __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLigand& L, const float* x0,
                                                 const float* d, float t, float* gout, const PoseBufs& b,
                                                 int lane, const float* gdir = nullptr, double* gdot = nullptr) {
@@ -454,12 +522,14 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
         for (int k = 0; k < 4; ++k) b.loc_grad[k * b.loc_gs + l] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
+    // a team splits the terms, lookups and explicit pairs among its warps (tw of tn)
+    const int tw = kTeam ? b.team_w : 0, tn = kTeam ? b.team_n : 1;
     DS e{0.f, 0.f};
-    topo_terms(L.topo, b.lig_xyz, b.lig_grad, b.lig_gs, e, lane);
-    if (R.n_local > 0) topo_terms(R.intra, b.loc_xyz, b.loc_grad, b.loc_gs, e, lane);
+    topo_terms(L.topo, b.lig_xyz, b.lig_grad, b.lig_gs, e, lane, tw, tn);
+    if (R.n_local > 0) topo_terms(R.intra, b.loc_xyz, b.loc_grad, b.loc_gs, e, lane, tw, tn);
     // grid lookups (inter_molecular_interactions, cached branch)
     if (env.grid.has_grid) {
-        for (int a = lane; a < N; a += kWarp) {
+        for (int a = lane + tw * kWarp; a < N; a += tn * kWarp) {
             float3 g = make_float3(0.f, 0.f, 0.f);
             const float ea = grid_lookup(env.grid, __ldg(&L.map_slot[a]), __ldg(&L.charge[a]),
                                          xyz(b.lig_xyz[a]), g);
@@ -471,7 +541,7 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
     // explicit inter pairs (rotor atoms with maps, every receptor atom without)
     const int M = R.n_explicit;
     if (M >= kWarp) {
-        for (int i = 0; i < N; ++i) {
+        for (int i = tw; i < N; i += tn) {
             const float3 xi = xyz(b.lig_xyz[i]);
             const float qi = __ldg(&L.charge[i]);
             const float2 sei = __ldg(&L.se[i]);
@@ -502,7 +572,7 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
             if (lane == 0) atomic_add3(&b.lig_grad[i], gi);
         }
     } else if (M > 0) {
-        for (int i = lane; i < N; i += kWarp) {
+        for (int i = lane + tw * kWarp; i < N; i += tn * kWarp) {
             const float3 xi = xyz(b.lig_xyz[i]);
             const float qi = __ldg(&L.charge[i]);
             const float2 sei = __ldg(&L.se[i]);
@@ -531,14 +601,33 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
         }
     }
     __syncwarp();
-    // flat gradient and the receptor-torsion chain rule (interaction.cpp:338-350)
+    DS et = e;  // the pose's energy (the team's partials summed in member order)
+    if (kTeam && tn > 1) {
+        const DS ew = ds_warp_reduce(e);
+        if (lane == 0) b.ts->e[tw] = make_float2(ew.hi, ew.lo);
+        if (!team_sync(b.ts, tn, lane)) {  // the team aborted: NaN ends the caller's search
+            if (gdot) *gdot = __longlong_as_double(0x7ff8000000000000LL);
+            return __longlong_as_double(0x7ff8000000000000LL);
+        }
+        et = DS{b.ts->e[0].x, b.ts->e[0].y};
+        for (int u = 1; u < tn; ++u) ds_add_ds(et, DS{b.ts->e[u].x, b.ts->e[u].y});
+    }
+    // flat gradient and the receptor-torsion chain rule (interaction.cpp:338-350), the
+    // team's arrays summed in member order
     DS gd{0.f, 0.f};
     for (int a = lane; a < N; a += kWarp) {
-        const float4 g0 = b.lig_grad[a], g1 = b.lig_grad[b.lig_gs + a];
-        const float4 g2 = b.lig_grad[2 * b.lig_gs + a], g3 = b.lig_grad[3 * b.lig_gs + a];
-        const float gx = (g0.x + g1.x) + (g2.x + g3.x);
-        const float gy = (g0.y + g1.y) + (g2.y + g3.y);
-        const float gz = (g0.z + g1.z) + (g2.z + g3.z);
+        float gx = 0.f, gy = 0.f, gz = 0.f;
+        for (int u = 0; u < tn; ++u) {
+            const float4* G = b.lig_grad + (u - tw) * b.team_f4;
+            const float4 g0 = G[a], g1 = G[b.lig_gs + a];
+            const float4 g2 = G[2 * b.lig_gs + a], g3 = G[3 * b.lig_gs + a];
+            const float sx = (g0.x + g1.x) + (g2.x + g3.x);
+            const float sy = (g0.y + g1.y) + (g2.y + g3.y);
+            const float sz = (g0.z + g1.z) + (g2.z + g3.z);
+            gx = u == 0 ? sx : gx + sx;
+            gy = u == 0 ? sy : gy + sy;
+            gz = u == 0 ? sz : gz + sz;
+        }
         gout[3 * a] = gx;
         gout[3 * a + 1] = gy;
         gout[3 * a + 2] = gz;
@@ -552,26 +641,39 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
         float acc = 0.f;
         const int l0 = __ldg(&R.rotor_mov[r]), l1 = __ldg(&R.rotor_mov[r + 1]);
         for (int l = l0; l < l1; ++l) {
-            const float4 g0 = b.loc_grad[l], g1 = b.loc_grad[b.loc_gs + l];
-            const float4 g2 = b.loc_grad[2 * b.loc_gs + l], g3 = b.loc_grad[3 * b.loc_gs + l];
-            const float3 g = make_float3((g0.x + g1.x) + (g2.x + g3.x), (g0.y + g1.y) + (g2.y + g3.y),
-                                         (g0.z + g1.z) + (g2.z + g3.z));
+            float3 g = make_float3(0.f, 0.f, 0.f);
+            for (int u = 0; u < tn; ++u) {
+                const float4* G = b.loc_grad + (u - tw) * b.team_f4;
+                const float4 g0 = G[l], g1 = G[b.loc_gs + l];
+                const float4 g2 = G[2 * b.loc_gs + l], g3 = G[3 * b.loc_gs + l];
+                const float3 gu = make_float3((g0.x + g1.x) + (g2.x + g3.x), (g0.y + g1.y) + (g2.y + g3.y),
+                                              (g0.z + g1.z) + (g2.z + g3.z));
+                g = u == 0 ? gu : add3(g, gu);
+            }
             acc += dot3(xyz(b.mov_jac[l]), g);
         }
         gout[n3 + r] = acc;
         if (gdir) ds_dot_acc(gd, acc, gdir[n3 + r]);
     }
     __syncwarp();
+    // no member clears its arrays for the next evaluation before every member has read them
+    if (kTeam && tn > 1 && !team_sync(b.ts, tn, lane)) {
+        if (gdot) *gdot = __longlong_as_double(0x7ff8000000000000LL);
+        return __longlong_as_double(0x7ff8000000000000LL);
+    }
     if (gdir) *gdot = ds_warp_sum(gd);
+    if (kTeam && tn > 1) return static_cast<double>(et.hi) + static_cast<double>(et.lo) + R.e_const;
     return ds_warp_sum(e) + R.e_const;
 }
 
 // Kept out of line: the optimiser calls it from five places, and inlined copies of this
 // much code overflow the instruction cache (the top stall of the batched kernel).
+// kTeam: the evaluation is shared by a team of warps (PoseBufs' team fields).
+template <bool kTeam = false>
 static __device__ __noinline__ double eval_pose(const EvalEnv& env, const DevLigand& L, const float* x0,
                                                 const float* d, float t, float* gout, const PoseBufs& b,
                                                 int lane, double* gdot = nullptr) {
-    return eval_pose_body(env, L, x0, d, t, gout, b, lane, gdot ? d : nullptr, gdot);
+    return eval_pose_body<kTeam>(env, L, x0, d, t, gout, b, lane, gdot ? d : nullptr, gdot);
 }
 
 // Shared-memory floats needed by PoseBufs for a ligand of up to n_atoms atoms.
@@ -588,6 +690,10 @@ __device__ inline PoseBufs carve_pose_bufs(float* base, int n_atoms, int n_local
     b.mov_jac = b.loc_grad + 4 * n_local;
     b.lig_gs = n_atoms;
     b.loc_gs = n_local;
+    b.team_w = 0;
+    b.team_n = 1;
+    b.team_f4 = 0;
+    b.ts = nullptr;
     return b;
 }
 

@@ -89,6 +89,15 @@ __device__ __forceinline__ double closure_energy64(Closure& c, const float* x) {
     return energy64(*c.env, *c.L, x, *c.b, c.lane);
 }
 
+// The same closure evaluated by a team of warps (the single-walker search's team mode).
+struct TeamClosure : Closure {};
+
+__device__ __forceinline__ double closure_eval(TeamClosure& c, double t, const float* d, float* g,
+                                               double* gdot = nullptr) {
+    ++c.nevals;
+    return eval_pose<true>(*c.env, *c.L, c.x0, d, static_cast<float>(t), g, *c.b, c.lane, gdot);
+}
+
 __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double g1, double x2,
                                                     double f2, double g2, double lo, double hi) {
     double d1 = g1 + g2 - 3.0 * (f1 - f2) / (x1 - x2);

@@ -137,7 +137,8 @@ struct McArgs {
     double blo[3], bhi[3];  // the box as given, for the random centre draws
     uint32_t seed;
     int n_local, D_pad;
-    int warps_per_block;  // kMcWarps, or 1 when there are too few walkers to fill the SMs
+    int warps_per_block;  // kMcWarps
+    int team;             // kMcWarps: the block's warps search one walker together; 1: a walker per warp
     float* hist;
     size_t hist_stride;
     MtState* rng;
@@ -242,14 +243,41 @@ __device__ void atomic_min_double(double* p, double v) {
 // The relaxations form the two-loop coefficients in FP32 (lbfgs_pose<true>): a walker's warp
 // is usually alone on its SM, where the FP64 operations on each pass's dependent chain are
 // what it waits on.
+//
+// Team mode (a.team = kMcWarps, fewer walkers than SMs' worth of warps): the block's warps
+// search one walker together. Every member runs the walker's whole search on its own slice
+// with its own copy of the generator, seeded alike, so all members draw the same numbers and
+// take the same branches; the evaluations split their terms, lookups and explicit pairs
+// among the members and sum the members' parts in member order (eval_pose_body), so every
+// member holds the same energy and gradient. The history slab is the team's: members write
+// the same values to it. Only member 0 takes walkers from the queue, updates the global
+// minimum and writes the outputs, and its queue slot and minimum reach the others through
+// the team's shared state. Team barriers spin a bounded number of times; a team that gives
+// up flags the launch (a.error[1]) and leaves its walkers with status 3.
 __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_constant__ McArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
     const int wib = threadIdx.x / kWarp;
     const int Dp = a.D_pad;
     const int m = a.full.m;
-    float* base = smem + static_cast<size_t>(wib) * mc_warp_floats(a.max_atoms, a.n_local, Dp, m);
-    const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
+    const int slice = mc_warp_floats(a.max_atoms, a.n_local, Dp, m);
+    const bool team = a.team > 1;
+    const bool lead = !team || wib == 0;  // the member that takes walkers and writes results
+    float* base = smem + static_cast<size_t>(wib) * slice;
+    PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
+    if (team) {
+        b.team_w = wib;
+        b.team_n = a.team;
+        b.team_f4 = slice / 4;
+        b.ts = reinterpret_cast<TeamShared*>(smem + static_cast<size_t>(a.warps_per_block) * slice);
+        if (threadIdx.x == 0) {
+            b.ts->count = 0;
+            b.ts->gen = 0;
+            b.ts->abort = 0;
+            b.ts->slot = 0;
+        }
+        __syncthreads();
+    }
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
     Vecs v = carve_vecs(vb, Dp, m);
     float* best_x = vb + kOptVecs * Dp + opt_scalar_floats(m);
@@ -259,23 +287,30 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     float* tq = reinterpret_cast<float*>(&ks + 1);          // [64] torsions of a move
     double* bc = reinterpret_cast<double*>(tq + 64);         // [8] broadcast slots
     const size_t gw = static_cast<size_t>(blockIdx.x) * a.warps_per_block + wib;
-    v.S = a.hist + gw * a.hist_stride;
+    v.S = a.hist + (team ? static_cast<size_t>(blockIdx.x) : gw) * a.hist_stride;
     v.Y = v.S + static_cast<size_t>(hist_slots(m)) * Dp;
     MtState* rng = a.rng + gw;
     const int R = a.env.rec.n_rotors;
-    Closure c;
+    TeamClosure c;
     c.env = &a.env;
     c.b = &b;
     c.lane = lane;
     while (true) {
         int w = 0;
-        if (lane == 0) w = atomicAdd(a.counter, 1);
-        w = __shfl_sync(kFull, w, 0);
+        if (team) {
+            if (threadIdx.x == 0) b.ts->slot = atomicAdd(a.counter, 1);
+            if (!team_sync(b.ts, a.team, lane)) break;
+            w = *reinterpret_cast<volatile int*>(&b.ts->slot);
+            if (!team_sync(b.ts, a.team, lane)) break;  // read by all before the next take
+        } else {
+            if (lane == 0) w = atomicAdd(a.counter, 1);
+            w = __shfl_sync(kFull, w, 0);
+        }
         if (w >= a.n_walkers) break;
         const int lid = a.lig_ids[w];
         if (lid < 0 || lid >= a.n_ligands || a.ligands[lid].n_atoms > a.max_atoms || !a.ligands[lid].score.has ||
             a.ligands[lid].n_frags == 0) {
-            if (lane == 0) {
+            if (lead && lane == 0) {
                 a.out_st[w] = 3;
                 a.out_nev[w] = 0;
             }
@@ -331,7 +366,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                     continue;
                 placed = tries > 1999 || vdw_check(a.senv, L, v.x, lane) < 100.0;
             }
-            if (!placed && lane == 0) atomicAdd(a.error, 1);
+            if (!placed && lead && lane == 0) atomicAdd(a.error, 1);
         }
         // ---- full relaxation and score of the start (searcher.cpp:120-126)
         double best_e = 0.0;
@@ -393,10 +428,23 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                     // optional pruning on the pre-relaxation energy (searcher.cpp:141-157)
                     if (a.threshold > 0.0 && a.gmin) {
                         c.x0 = v.x;
-                        const double pre = eval_pose(a.env, L, v.x, nullptr, 0.f, v.gnew, b, lane);
-                        if (lane == 0) atomic_min_double(&a.gmin[lid], pre);
-                        __syncwarp();
-                        const double gm = *reinterpret_cast<volatile double*>(&a.gmin[lid]);
+                        const double pre = eval_pose<true>(a.env, L, v.x, nullptr, 0.f, v.gnew, b, lane);
+                        double gm;
+                        if (team) {
+                            // the leader's view of the shared minimum, so that every member
+                            // takes the same branch
+                            if (threadIdx.x == 0) {
+                                atomic_min_double(&a.gmin[lid], pre);
+                                b.ts->gmin = *reinterpret_cast<volatile double*>(&a.gmin[lid]);
+                            }
+                            team_sync(b.ts, a.team, lane);
+                            gm = *reinterpret_cast<volatile double*>(&b.ts->gmin);
+                            team_sync(b.ts, a.team, lane);
+                        } else {
+                            if (lane == 0) atomic_min_double(&a.gmin[lid], pre);
+                            __syncwarp();
+                            gm = *reinterpret_cast<volatile double*>(&a.gmin[lid]);
+                        }
                         if (pre > gm + a.threshold) continue;
                     }
                     double cdd_e = 0.0;  // unused: the step is judged by its pose score
@@ -432,14 +480,18 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                 if (status == 1) total = 0;
             }
         }
-        float* ox = a.out_xyz + static_cast<size_t>(w) * a.max_atoms * 3;
-        for (int e = lane; e < 3 * N; e += kWarp) ox[e] = best_x[e];
-        for (int r = lane; r < R; r += kWarp) a.out_tors[static_cast<size_t>(w) * R + r] = best_x[3 * N + r];
-        if (lane == 0) {
-            a.out_e[w] = best_e;
-            a.out_ps[w] = best_ps;
-            a.out_nev[w] = static_cast<int>(total);
-            a.out_st[w] = status;
+        if (lead) {
+            float* ox = a.out_xyz + static_cast<size_t>(w) * a.max_atoms * 3;
+            for (int e = lane; e < 3 * N; e += kWarp) ox[e] = best_x[e];
+            for (int r = lane; r < R; r += kWarp) a.out_tors[static_cast<size_t>(w) * R + r] = best_x[3 * N + r];
+            if (lane == 0) {
+                const bool aborted = team && *reinterpret_cast<volatile int*>(&b.ts->abort);
+                a.out_e[w] = best_e;
+                a.out_ps[w] = best_ps;
+                a.out_nev[w] = static_cast<int>(total);
+                a.out_st[w] = aborted ? 3 : status;
+                if (aborted) atomicExch(a.error + 1, 1);
+            }
         }
         __syncwarp();
     }
@@ -562,21 +614,25 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     a.seed = p->seed;
     a.n_local = ctx->rec.n_local;
     a.D_pad = (3 * max_atoms + ctx->rec.n_rotors + kWarp - 1) / kWarp * kWarp;
-    // Fewer walkers than 4 per SM (a single docking search): one warp per block, so each
-    // walker has an SM's L1, shared-memory pipe and issue slots to itself.
-    a.warps_per_block = n_walkers < kMcWarps * ctx->n_sm ? 1 : kMcWarps;
+    // At most one walker per SM (a single docking search): a block of kMcWarps warps per
+    // walker searching as a team, so each walker has an SM's L1, shared-memory pipe and issue
+    // slots, and its four schedulers share the evaluations. Fewer walkers than 4 per SM: one
+    // warp per block, so each walker has an SM to itself or shares it with few others.
+    a.team = n_walkers <= ctx->n_sm ? kMcWarps : 1;
+    a.warps_per_block = a.team > 1 || n_walkers >= kMcWarps * ctx->n_sm ? kMcWarps : 1;
     const int wpb = a.warps_per_block;
-    const size_t smem = sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history);
+    const size_t smem = sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history) +
+                        (a.team > 1 ? (sizeof(TeamShared) + 15) / 16 * 16 : 0);
     rc = cuda_check(ctx, cudaFuncSetAttribute(mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(smem)),
                     "mc smem attribute");
     if (rc) return rc;
-    // One-warp blocks leave the SMs nearly empty: ask for the smallest shared-memory carve-out
+    // One walker per block leaves the SMs nearly empty: ask for the smallest shared-memory carve-out
     // (percent of the SM's shared memory) that still holds the blocks each SM must run at
     // once for every walker to start together, so the rest serves as L1; full launches keep
     // the driver's choice.
     int carveout = cudaSharedmemCarveoutDefault;
-    if (wpb == 1) {
+    if (a.team > 1 || wpb == 1) {
         int sm_smem = 0;
         rc = cuda_check(ctx, cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device),
                         "shared memory per SM");
@@ -594,11 +650,12 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     if (rc) return rc;
     if (per_sm < 1) return set_error(ctx, PXD_ERR_INVALID, "ligand too large for shared memory");
     int blocks = per_sm * ctx->n_sm;
-    const int need = (n_walkers + wpb - 1) / wpb;
+    const int walkers_per_block = a.team > 1 ? 1 : wpb;
+    const int need = (n_walkers + walkers_per_block - 1) / walkers_per_block;
     if (blocks > need) blocks = need;
     const size_t warps = static_cast<size_t>(blocks) * wpb;
     a.hist_stride = static_cast<size_t>(2) * hist_slots(p->lbfgs.history) * a.D_pad;
-    const size_t hist_bytes = sizeof(float) * a.hist_stride * warps;
+    const size_t hist_bytes = sizeof(float) * a.hist_stride * warps;  // a slab per warp, or per team
     const size_t rng_off = (hist_bytes + 255) / 256 * 256;
     rc = ensure_scratch(ctx, rng_off + sizeof(MtState) * warps);
     if (rc) return rc;
@@ -607,7 +664,7 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     a.counter = ctx->d_counter;
     a.error = ctx->d_counter + 1;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-    rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, 2 * sizeof(int), s), "counter reset");
+    rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_counter, 0, 3 * sizeof(int), s), "counter reset");
     if (rc) return rc;
     return cuda_check(ctx, launch_with_map_window(ctx, mc_kernel, blocks, wpb * kWarp, smem, s, a),
                       "mc_kernel launch");
@@ -667,13 +724,15 @@ int pxd_mc_search(pxd_context* ctx, const pxd_mc_params* p, int32_t lig, int32_t
     cudaFreeAsync(mem, ctx->stream);
     rc = sync_copies(ctx, rc, ctx->stream, "search");
     if (rc) return rc;
-    int err = 0;
-    rc = cuda_check(ctx, cudaMemcpy(&err, ctx->d_counter + 1, sizeof(int), cudaMemcpyDeviceToHost),
-                    "search start flag");
+    int err[2] = {0, 0};
+    rc = cuda_check(ctx, cudaMemcpy(err, ctx->d_counter + 1, 2 * sizeof(int), cudaMemcpyDeviceToHost),
+                    "search flags");
     if (rc) return rc;
     for (size_t i = 0; i < nx; ++i) out_xyz[i] = ho[i];
     for (size_t i = 0; i < nt; ++i) out_tors[i] = ht[i];
-    if (err) return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a random start found no pose inside the box");
+    if (err[1])
+        return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a search team stopped waiting at a barrier (walkers with status 3)");
+    if (err[0]) return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a random start found no pose inside the box");
     return PXD_OK;
 }
 
@@ -738,15 +797,17 @@ int pxd_mc_search_multi(pxd_context* ctx, const pxd_mc_params* p, int32_t n, int
     cudaFreeAsync(mem, ctx->stream);
     rc = sync_copies(ctx, rc, ctx->stream, "search");
     if (rc) return rc;
-    int err = 0;
-    rc = cuda_check(ctx, cudaMemcpy(&err, ctx->d_counter + 1, sizeof(int), cudaMemcpyDeviceToHost),
-                    "search start flag");
+    int err[2] = {0, 0};
+    rc = cuda_check(ctx, cudaMemcpy(err, ctx->d_counter + 1, 2 * sizeof(int), cudaMemcpyDeviceToHost),
+                    "search flags");
     if (rc) return rc;
     for (size_t i = 0; i < nx; ++i) out_xyz[i] = ho[i];
     for (size_t i = 0; i < nt; ++i) out_tors[i] = ht[i];
     if (global_min)
         for (size_t i = 0; i < nl; ++i) global_min[i] = gm[i];
-    if (err) return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a random start found no pose inside the box");
+    if (err[1])
+        return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a search team stopped waiting at a barrier (walkers with status 3)");
+    if (err[0]) return set_error(ctx, PXD_ERR_DEVICE_FLAG, "a random start found no pose inside the box");
     return PXD_OK;
 }
 
