@@ -418,6 +418,7 @@ struct TeamShared {
     int count, gen, abort, slot;
     double gmin;
     float2 e[4];
+    float2 terms[4][PXD_NUM_TERMS - 1];  // members' pose-score partials (score_pose)
 };
 
 // Spin limit of a team barrier: ~0.1 s at the loop's pace, far beyond any wait of members

@@ -94,11 +94,24 @@ __device__ __forceinline__ float signed_dihedral(float3 pi, float3 pj, float3 pk
 // Score of the pose in X (ligand, smem) with receptor rotor atoms in loc_xyz (smem).
 // Returns sum(coef * term) over the active terms except GB/SA; when `terms` is given,
 // lane 0 stores the unweighted values.
+//
+// kTeam (a team of warps of one block, PoseBufs' team fields in tw / tn / ts): the members
+// split the all-pairs Coulomb / LJ loop, members 1, 2 and 3 add the hydrophobic, the
+// ionic / cation-pi / stacking and the hydrogen-bond / torsion-strain terms, and the
+// partials are summed in member order, so every member returns the same score.
+template <bool kTeam = false>
 static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, const DevLigScore& ls,
-                             const float4* X, const float4* loc_xyz, int lane, double* terms) {
+                             const float4* X, const float4* loc_xyz, int lane, double* terms,
+                             int tw = 0, int tn = 1, TeamShared* ts = nullptr) {
     const DevRecScore& rs = env.rs;
     const DevSf& sf = *env.sf;
     const int N = L.n_atoms;
+    if (!kTeam) {
+        tw = 0;
+        tn = 1;
+    }
+    // the members that add the terms other than Coulomb / LJ (all of them on a lone warp)
+    const bool own_hyd = tw == 1 % tn, own_ion = tw == 2 % tn, own_hb = tw == 3 % tn;
     DS acc[PXD_NUM_TERMS - 1];
 #pragma unroll
     for (int k = 0; k < PXD_NUM_TERMS - 1; ++k) acc[k] = DS{0.f, 0.f};
@@ -110,7 +123,7 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
     // search) arithmetic instead of load latency. The pairs are the same; their sum runs
     // in another order.
     if (coul || vdw) {
-        for (int j = lane; j < rs.n_all; j += kWarp) {
+        for (int j = lane + tw * kWarp; j < rs.n_all; j += tn * kWarp) {
             const float4 rj = __ldg(&rs.all_xyzq[j]);
             const int l = __ldg(&rs.all_local[j]);
             const float3 xj = l >= 0 ? xyz(loc_xyz[l]) : xyz(rj);
@@ -135,7 +148,7 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
         }
     }
     // hydrophobic contacts (scorer.cpp:278-311)
-    if (sf.coef[PXD_TERM_HYDROPHOBIC] != 0.f) {
+    if (own_hyd && sf.coef[PXD_TERM_HYDROPHOBIC] != 0.f) {
         for (int a = 0; a < ls.n_hyd; ++a) {
             const int i = __ldg(&ls.hyd[a]);
             const float3 xi = xyz(X[i]);
@@ -150,7 +163,7 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
         }
     }
     // ionic (scorer.cpp:313-368): ligand cations x receptor anions, receptor cations x ligand anions
-    if (sf.coef[PXD_TERM_IONIC] != 0.f) {
+    if (own_ion && sf.coef[PXD_TERM_IONIC] != 0.f) {
         float e = 0.f;
         for (int a = 0; a < ls.n_cat; ++a) {
             const float3 xi = xyz(X[__ldg(&ls.cat[a])]);
@@ -167,7 +180,7 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
         ds_add(acc[PXD_TERM_IONIC], e);
     }
     // cation-pi (scorer.cpp:370-462)
-    if (sf.coef[PXD_TERM_PI_CATION] != 0.f) {
+    if (own_ion && sf.coef[PXD_TERM_PI_CATION] != 0.f) {
         float e = 0.f;
         for (int a = 0; a < ls.n_cat; ++a) {
             const float3 xi = xyz(X[__ldg(&ls.cat[a])]);
@@ -189,7 +202,7 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
     }
     // pi stacking, face-to-face (centre 0) and edge-to-face (centre 90) (scorer.cpp:638-724)
     for (int w = 0; w < 2; ++w) {
-        if (sf.coef[PXD_TERM_F2F + w] == 0.f) continue;
+        if (!own_ion || sf.coef[PXD_TERM_F2F + w] == 0.f) continue;
         const float center = w == 0 ? 0.f : 90.f;
         float e = 0.f;
         for (int r = 0; r < ls.n_r5 + ls.n_r6; ++r) {
@@ -208,7 +221,7 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
         ds_add(acc[PXD_TERM_F2F + w], e);
     }
     // hydrogen bonds, 8 donor/acceptor classes (scorer.cpp:464-577)
-    if (sf.coef[PXD_TERM_HBOND] != 0.f) {
+    if (own_hb && sf.coef[PXD_TERM_HBOND] != 0.f) {
         float e = 0.f;
         for (int c = 0; c < 2; ++c) {  // ligand donors (charged, neutral)
             const int nd = c == 0 ? ls.n_donc : ls.n_donn;
@@ -248,7 +261,7 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
         ds_add(acc[PXD_TERM_HBOND], e * sf.hbond_scale);
     }
     // torsion strain (scorer.cpp:579-613)
-    if (sf.coef[PXD_TERM_TSTRAIN] != 0.f) {
+    if (own_hb && sf.coef[PXD_TERM_TSTRAIN] != 0.f) {
         for (int t = lane; t < ls.n_ts; t += kWarp) {
             const float4 co = __ldg(&ls.ts_coef[t]);
             const int2 rg = __ldg(&ls.ts_range[t]);
@@ -266,8 +279,26 @@ static __device__ double score_pose(const ScoreEnv& env, const DevLigand& L, con
     }
     double total = 0.0;
     double vals[PXD_NUM_TERMS];
+    if (kTeam && tn > 1) {
 #pragma unroll
-    for (int k = 0; k < PXD_NUM_TERMS - 1; ++k) vals[k] = ds_warp_sum(acc[k]);
+        for (int k = 0; k < PXD_NUM_TERMS - 1; ++k) {
+            const DS r = ds_warp_reduce(acc[k]);
+            if (lane == 0) ts->terms[tw][k] = make_float2(r.hi, r.lo);
+        }
+        const bool ok = team_sync(ts, tn, lane);
+#pragma unroll
+        for (int k = 0; k < PXD_NUM_TERMS - 1; ++k) {
+            DS t{ts->terms[0][k].x, ts->terms[0][k].y};
+            for (int u = 1; u < tn; ++u) ds_add_ds(t, DS{ts->terms[u][k].x, ts->terms[u][k].y});
+            vals[k] = static_cast<double>(t.hi) + static_cast<double>(t.lo);
+        }
+        // read by every member before any member writes its next partials; an aborted
+        // team scores NaN
+        if (!team_sync(ts, tn, lane) || !ok) return __longlong_as_double(0x7ff8000000000000LL);
+    } else {
+#pragma unroll
+        for (int k = 0; k < PXD_NUM_TERMS - 1; ++k) vals[k] = ds_warp_sum(acc[k]);
+    }
     vals[PXD_TERM_VDW] *= sf.vdw_scale;
     vals[PXD_TERM_HYDROPHOBIC] *= sf.hydro_scale;
     vals[PXD_TERM_ROTATABLE] = sf.coef[PXD_TERM_ROTATABLE] != 0.f ? -1.0 / (2.620643 + ls.n_rot) : 0.0;

@@ -226,7 +226,7 @@ __device__ double mc_pscore(const McArgs& a, const DevLigand& L, const float* x,
         b.loc_xyz[l] = make_float4(p.x, p.y, p.z, 0.f);
     }
     __syncwarp();
-    return score_pose(a.senv, L, L.score, b.lig_xyz, b.loc_xyz, lane, nullptr);
+    return score_pose<true>(a.senv, L, L.score, b.lig_xyz, b.loc_xyz, lane, nullptr, b.team_w, b.team_n, b.ts);
 }
 
 __device__ void atomic_min_double(double* p, double v) {
