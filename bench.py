@@ -1103,12 +1103,20 @@ def main():
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_dev = float(tt.item())
     value = world * N_POSES * args.steps / t_dev
-    # end to end through the host-buffer C-ABI call (copies in the timed region)
+    # end to end through the host-buffer C-ABI call, in place on the caller's FP64 arrays as
+    # the reference's optimiser call works (host <-> device copies and conversions in the
+    # timed region; restoring the starts into the work arrays is not)
     e2e_times = []
+    work = np.empty_like(np.ascontiguousarray(poses, np.float64))
+    w_tors = np.zeros((N_POSES, ctx.n_rotors))
+    w_e, w_nev, w_st = np.zeros(N_POSES), np.zeros(N_POSES, np.int32), np.zeros(N_POSES, np.int32)
     for k in range(max(1, min(args.steps, 3))):
+        np.copyto(work, poses)
+        w_tors[:] = 0.0
         t1 = time.perf_counter()
-        out = ctx.lbfgs(p, lid, poses)
+        ctx.lbfgs_inplace(p, lid, work, w_tors, w_e, w_nev, w_st)
         e2e_times.append(time.perf_counter() - t1)
+    out = dict(xyz=work, torsions=w_tors, energy=w_e, nevals=w_nev, status=w_st)
     t_e2e = float(np.mean(e2e_times))
     if dist:
         tt = torch.tensor([t_e2e], device=dev)

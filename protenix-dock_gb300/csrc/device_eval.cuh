@@ -221,11 +221,134 @@ __device__ __forceinline__ float3 pair_grad(float4 p, float4 xi, float4 xj, floa
 // slots (-1) compute nothing. Every loop runs a multiple of 32 slots, so all lanes
 // meet every barrier. The caller sums the arrays. Matches
 // intra_molecular_interactions::put_gradients.
+__device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, float4* G, int gs, DS& e,
+                                           int lane) {
+    float4* G0 = G;
+    float4* G1 = G + gs;
+    float4* G2 = G + 2 * gs;
+    float4* G3 = G + 3 * gs;
+    __syncwarp();
+    // harmonic bonds (interaction.cpp:27-47)
+    for (int s = lane; s < t.n_bond_slots; s += kWarp) {
+        const int2 ij = __ldg(&t.bond_ij[s]);
+        if (ij.x >= 0) {
+            const float2 p = __ldg(&t.bond_p[s]);
+            const float3 d = sub3(xyz(X[ij.y]), xyz(X[ij.x]));
+            const float r = sqrtf(dot3(d, d));
+            const float dr = r - p.y;
+            ds_add(e, 0.5f * p.x * (dr * dr));
+            const float de_dr = p.x * (1.f - __fdividef(p.y, r + kEpsF));
+            const float3 g = mul3(d, de_dr);
+            sub_rec(&G0[ij.x], g);
+            add_rec(&G1[ij.y], g);
+        }
+        __syncwarp();
+    }
+    // harmonic angles (interaction.cpp:49-74, math.cpp:96-110)
+    for (int s = lane; s < t.n_angle_slots; s += kWarp) {
+        const int4 ijk = __ldg(&t.angle_ijk[s]);
+        if (ijk.x >= 0) {
+            const float2 p = __ldg(&t.angle_p[s]);
+            const float3 xi = xyz(X[ijk.x]), xj = xyz(X[ijk.y]), xk = xyz(X[ijk.z]);
+            const float3 v0 = sub3(xj, xi), v1 = sub3(xj, xk);
+            const float3 c = cross3(v0, v1);
+            const float rp = sqrtf(dot3(c, c));
+            float3 gi = cross3(v0, c), gk = cross3(c, v1);
+            gi = mul3(gi, -__fdividef(1.f, dot3(v0, v0) * rp + kEpsF));
+            gk = mul3(gk, -__fdividef(1.f, dot3(v1, v1) * rp + kEpsF));
+            const float theta = atan2f(rp, dot3(v0, v1) + kEpsF);
+            const float delta = theta - p.y;
+            ds_add(e, 0.5f * p.x * (delta * delta));
+            const float de = p.x * delta;
+            const float3 fi = mul3(gi, de), fk = mul3(gk, de);
+            add_rec(&G0[ijk.x], fi);
+            sub_rec(&G1[ijk.y], add3(fi, fk));
+            add_rec(&G2[ijk.z], fk);
+        }
+        __syncwarp();
+    }
+    // Fourier dihedrals, impropers then propers (interaction.cpp:76-117, math.cpp:130-167)
+    for (int s = lane; s < t.n_dih_slots; s += kWarp) {
+        const int4 q = __ldg(&t.dih_ijkl[s]);
+        if (q.x >= 0) {
+            const float3 pi = xyz(X[q.x]), pj = xyz(X[q.y]), pk = xyz(X[q.z]), pl = xyz(X[q.w]);
+            const float3 rij = sub3(pj, pi), rkj = sub3(pj, pk), rkl = sub3(pl, pk);
+            const float3 m = cross3(rij, rkj), n = cross3(rkj, rkl);
+            const float3 w = cross3(m, n);
+            const float wlen = sqrtf(dot3(w, w));
+            const float phi = atan2f(wlen, dot3(m, n) + kEpsF);
+            const float theta = dot3(rij, n) < 0.f ? phi : -phi;
+            const float nrkj2 = dot3(rkj, rkj);
+            const float nrkj_1 = __fdividef(1.f, sqrtf(nrkj2) + kEpsF);
+            const float nrkj_2 = nrkj_1 * nrkj_1;
+            const float nrkj = nrkj2 * nrkj_1;
+            // + kEpsF: a collapsed dihedral (m or n = 0, possible in FP32 only for a pose
+            // flung ~1e11 A out of the box, where coordinates resolve to ~1e4 A) gives a zero
+            // gradient instead of 0 * inf = NaN; resolvable geometries are unaffected
+            const float a = -__fdividef(nrkj, dot3(m, m) + kEpsF);
+            const float b = __fdividef(nrkj, dot3(n, n) + kEpsF);
+            const float3 gi = mul3(m, -a), gl = mul3(n, -b);
+            const float pp = dot3(rij, rkj) * nrkj_2, qq = dot3(rkj, rkl) * nrkj_2;
+            const float3 sv = sub3(mul3(gi, pp), mul3(gl, qq));
+            const float3 gj = mul3(sub3(gi, sv), -1.f), gk = mul3(add3(gl, sv), -1.f);
+            const int2 tr = __ldg(&t.dih_terms[s]);
+            float de = 0.f, et = 0.f;
+            for (int u = 0; u < tr.y; ++u) {
+                const float4 term = __ldg(&t.dih_term[tr.x + u]);  // k, periodicity, phase
+                const float delta = theta * term.y - term.z;
+                float sd, cd;
+                __sincosf(delta, &sd, &cd);  // |delta| <= 7 pi: fast path within FP32 parity
+                et += term.x * (1.f + cd);
+                de += term.x * term.y * sd;
+            }
+            ds_add(e, et);
+            add_rec(&G0[q.x], mul3(gi, -de));
+            add_rec(&G1[q.y], mul3(gj, -de));
+            add_rec(&G2[q.z], mul3(gk, -de));
+            add_rec(&G3[q.w], mul3(gl, -de));
+        }
+        __syncwarp();
+    }
+    // 1-4 and all other pairs: Coulomb + LJ 12-6 (interaction.cpp:127-168, pair.h:25-60).
+    // The next round's record is loaded while this round computes, so its L1/L2 latency
+    // is not exposed at the round's barrier (the pair rounds are the most numerous).
+    int2 ij_n = lane < t.n_pair_slots ? __ldg(&t.pair_ij[lane]) : make_int2(-1, -1);
+    float4 p_n = lane < t.n_pair_slots ? __ldg(&t.pair_p[lane]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = lane; s < t.n_pair_slots; s += kWarp) {
+        const int2 ij = ij_n;
+        const float4 pp = p_n;
+        if (s + kWarp < t.n_pair_slots) {
+            ij_n = __ldg(&t.pair_ij[s + kWarp]);
+            p_n = __ldg(&t.pair_p[s + kWarp]);
+        }
+        if (ij.x >= 0) {
+            float en;
+            const float3 g = pair_grad(pp, X[ij.x], X[ij.y], en);
+            ds_add(e, en);
+            sub_rec(&G0[ij.x], g);
+            add_rec(&G1[ij.y], g);
+        }
+        __syncwarp();
+    }
+}
+
+// topo_terms for a team of nw warps (warp w of them), which split the rounds: warp w takes
+// rounds w, w + nw, ... into its own arrays G. Kept apart from topo_terms so that the
+// one-warp kernels compile exactly as before.
+//
+// Adds the bonded and non-bonded terms of `t` over coordinates `X`. The gradient of
+// the atom in position k of a term goes to array k: G[k * gs + atom] (shared memory).
+// Within a round the atoms of each position are distinct (host scheduling), so the
+// lanes of a round update distinct records with plain loads and stores; a warp
+// barrier between rounds orders a record's updates from different rounds. Padded
+// slots (-1) compute nothing. Every loop runs a multiple of 32 slots, so all lanes
+// meet every barrier. The caller sums the arrays. Matches
+// intra_molecular_interactions::put_gradients.
 //
 // A team of nw warps (warp w of them) splits the rounds: warp w takes rounds w, w + nw, ...
 // into its own arrays G (nw = 1: every round).
-__device__ __forceinline__ void topo_terms(const DevTopo& t, const float4* X, float4* G, int gs, DS& e,
-                                           int lane, int w = 0, int nw = 1) {
+__device__ __forceinline__ void topo_terms_split(const DevTopo& t, const float4* X, float4* G, int gs, DS& e,
+                                           int lane, int w, int nw) {
     float4* G0 = G;
     float4* G1 = G + gs;
     float4* G2 = G + 2 * gs;
@@ -468,9 +591,13 @@ struct PoseBufs {
     float4* loc_grad;  // [4][n_local]
     float4* mov_jac;   // [n_mov]
     int lig_gs, loc_gs;  // array strides
-    // team evaluation: this warp's index, the team's size, the float4 distance between
-    // members' slices and the team's shared state (team_n = 1: a warp alone)
-    int team_w, team_n, team_f4;
+};
+
+// A warp's place in a team evaluation: its index, the team's size, the float4 distance
+// between members' slices and the team's shared state. Kept out of PoseBufs, which the
+// batched optimiser reads from its stack frame on every evaluation.
+struct Team {
+    int w, n, f4;
     TeamShared* ts;
 };
 
@@ -484,7 +611,6 @@ struct EvalEnv {
 // directional derivative), accumulated while the flat gradient is written. Replaces
 // binding_system_interactions::put_gradients as the optimiser's closure calls it
 // (optimizer.cpp:155-167).
-template <bool kTeam = false>
 __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLigand& L, const float* x0,
                                                 const float* d, float t, float* gout, const PoseBufs& b,
                                                 int lane, const float* gdir = nullptr, double* gdot = nullptr) {
@@ -523,11 +649,166 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
         for (int k = 0; k < 4; ++k) b.loc_grad[k * b.loc_gs + l] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
-    // a team splits the terms, lookups and explicit pairs among its warps (tw of tn)
-    const int tw = kTeam ? b.team_w : 0, tn = kTeam ? b.team_n : 1;
     DS e{0.f, 0.f};
-    topo_terms(L.topo, b.lig_xyz, b.lig_grad, b.lig_gs, e, lane, tw, tn);
-    if (R.n_local > 0) topo_terms(R.intra, b.loc_xyz, b.loc_grad, b.loc_gs, e, lane, tw, tn);
+    topo_terms(L.topo, b.lig_xyz, b.lig_grad, b.lig_gs, e, lane);
+    if (R.n_local > 0) topo_terms(R.intra, b.loc_xyz, b.loc_grad, b.loc_gs, e, lane);
+    // grid lookups (inter_molecular_interactions, cached branch)
+    if (env.grid.has_grid) {
+        for (int a = lane; a < N; a += kWarp) {
+            float3 g = make_float3(0.f, 0.f, 0.f);
+            const float ea = grid_lookup(env.grid, __ldg(&L.map_slot[a]), __ldg(&L.charge[a]),
+                                         xyz(b.lig_xyz[a]), g);
+            ds_add(e, ea);
+            add_rec(&b.lig_grad[a], g);  // one lane per atom; topo_terms ended on a barrier
+        }
+        __syncwarp();  // the explicit pairs below add to the same records atomically
+    }
+    // explicit inter pairs (rotor atoms with maps, every receptor atom without)
+    const int M = R.n_explicit;
+    if (M >= kWarp) {
+        for (int i = 0; i < N; ++i) {
+            const float3 xi = xyz(b.lig_xyz[i]);
+            const float qi = __ldg(&L.charge[i]);
+            const float2 sei = __ldg(&L.se[i]);
+            float3 gi = make_float3(0.f, 0.f, 0.f);
+            for (int j = lane; j < M; j += kWarp) {
+                const int loc = __ldg(&R.ex_local[j]);
+                const float4 rj = __ldg(&R.ex_xyzq[j]);
+                const float3 xj = loc >= 0 ? xyz(b.loc_xyz[loc]) : xyz(rj);
+                const float2 sej = __ldg(&R.ex_se[j]);
+                const float3 rij = sub3(xj, xi);
+                const float r2 = fmaxf(dot3(rij, rij), kPairR2Floor);
+                const float rinv = rsqrtf(r2);
+                const float rinv2 = rinv * rinv;
+                const float s = (sei.x + sej.x) * 0.5f;
+                const float xx = s * s * rinv2;
+                const float u6 = xx * xx * xx, u12 = u6 * u6;
+                const float C = sqrtf(sei.y * sej.y) * 4.f;
+                const float ec = kCoulombF * qi * rj.w * rinv;
+                ds_add(e, ec);
+                ds_add(e, C * (u12 - u6));
+                const float3 g = mul3(rij, (C * (6.f * u6 - 12.f * u12) - ec) * rinv2);
+                gi = sub3(gi, g);
+                if (loc >= 0) atomic_add3(&b.loc_grad[loc], g);
+            }
+            gi.x = warp_sum_f(gi.x);
+            gi.y = warp_sum_f(gi.y);
+            gi.z = warp_sum_f(gi.z);
+            if (lane == 0) atomic_add3(&b.lig_grad[i], gi);
+        }
+    } else if (M > 0) {
+        for (int i = lane; i < N; i += kWarp) {
+            const float3 xi = xyz(b.lig_xyz[i]);
+            const float qi = __ldg(&L.charge[i]);
+            const float2 sei = __ldg(&L.se[i]);
+            float3 gi = make_float3(0.f, 0.f, 0.f);
+            for (int j = 0; j < M; ++j) {
+                const int loc = __ldg(&R.ex_local[j]);
+                const float4 rj = __ldg(&R.ex_xyzq[j]);
+                const float3 xj = loc >= 0 ? xyz(b.loc_xyz[loc]) : xyz(rj);
+                const float2 sej = __ldg(&R.ex_se[j]);
+                const float3 rij = sub3(xj, xi);
+                const float r2 = fmaxf(dot3(rij, rij), kPairR2Floor);
+                const float rinv = rsqrtf(r2);
+                const float rinv2 = rinv * rinv;
+                const float s = (sei.x + sej.x) * 0.5f;
+                const float xx = s * s * rinv2;
+                const float u6 = xx * xx * xx, u12 = u6 * u6;
+                const float C = sqrtf(sei.y * sej.y) * 4.f;
+                const float ec = kCoulombF * qi * rj.w * rinv;
+                ds_add(e, ec);
+                ds_add(e, C * (u12 - u6));
+                const float3 g = mul3(rij, (C * (6.f * u6 - 12.f * u12) - ec) * rinv2);
+                gi = sub3(gi, g);
+                if (loc >= 0) atomic_add3(&b.loc_grad[loc], g);
+            }
+            atomic_add3(&b.lig_grad[i], gi);
+        }
+    }
+    __syncwarp();
+    // flat gradient and the receptor-torsion chain rule (interaction.cpp:338-350)
+    DS gd{0.f, 0.f};
+    for (int a = lane; a < N; a += kWarp) {
+        const float4 g0 = b.lig_grad[a], g1 = b.lig_grad[b.lig_gs + a];
+        const float4 g2 = b.lig_grad[2 * b.lig_gs + a], g3 = b.lig_grad[3 * b.lig_gs + a];
+        const float gx = (g0.x + g1.x) + (g2.x + g3.x);
+        const float gy = (g0.y + g1.y) + (g2.y + g3.y);
+        const float gz = (g0.z + g1.z) + (g2.z + g3.z);
+        gout[3 * a] = gx;
+        gout[3 * a + 1] = gy;
+        gout[3 * a + 2] = gz;
+        if (gdir) {
+            ds_dot_acc(gd, gx, gdir[3 * a]);
+            ds_dot_acc(gd, gy, gdir[3 * a + 1]);
+            ds_dot_acc(gd, gz, gdir[3 * a + 2]);
+        }
+    }
+    for (int r = lane; r < R.n_rotors; r += kWarp) {
+        float acc = 0.f;
+        const int l0 = __ldg(&R.rotor_mov[r]), l1 = __ldg(&R.rotor_mov[r + 1]);
+        for (int l = l0; l < l1; ++l) {
+            const float4 g0 = b.loc_grad[l], g1 = b.loc_grad[b.loc_gs + l];
+            const float4 g2 = b.loc_grad[2 * b.loc_gs + l], g3 = b.loc_grad[3 * b.loc_gs + l];
+            const float3 g = make_float3((g0.x + g1.x) + (g2.x + g3.x), (g0.y + g1.y) + (g2.y + g3.y),
+                                         (g0.z + g1.z) + (g2.z + g3.z));
+            acc += dot3(xyz(b.mov_jac[l]), g);
+        }
+        gout[n3 + r] = acc;
+        if (gdir) ds_dot_acc(gd, acc, gdir[n3 + r]);
+    }
+    __syncwarp();
+    if (gdir) *gdot = ds_warp_sum(gd);
+    return ds_warp_sum(e) + R.e_const;
+}
+
+// eval_pose_body for a team of warps (Team): the members split the terms, lookups and
+// explicit pairs and sum each other's parts in member order. Kept apart from
+// eval_pose_body so that the one-warp kernels compile exactly as before.
+__device__ __forceinline__ double eval_pose_team_body(const EvalEnv& env, const DevLigand& L, const float* x0,
+                                                     const float* d, float t, float* gout, const PoseBufs& b,
+                                                     int lane, const float* gdir, double* gdot, const Team* team) {
+    const int N = L.n_atoms;
+    const int n3 = 3 * N;
+    const DevReceptor& R = env.rec;
+    for (int a = lane; a < N; a += kWarp) {
+        float px = x0[3 * a], py = x0[3 * a + 1], pz = x0[3 * a + 2];
+        if (d) {
+            px = fmaf(d[3 * a], t, px);
+            py = fmaf(d[3 * a + 1], t, py);
+            pz = fmaf(d[3 * a + 2], t, pz);
+        }
+        b.lig_xyz[a] = make_float4(px, py, pz, 0.f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) b.lig_grad[k * b.lig_gs + a] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    // receptor rotors (receptor_torsion2xyz, interaction.cpp:316-336)
+    for (int l = lane; l < R.n_local; l += kWarp) {
+        const float4 v = __ldg(&R.local_xyz0[l]);
+        if (l < R.n_mov) {
+            const int r = __float_as_int(v.w);
+            float th = x0[n3 + r];
+            if (d) th = fmaf(d[n3 + r], t, th);
+            Mat3 Rm, Jm;
+            rotation_and_jacobian(xyz(__ldg(&R.rotor_axis[r])), th, Rm, Jm);
+            const float3 rel = xyz(v);
+            const float3 pos = add3(mat_apply(Rm, rel), xyz(__ldg(&R.rotor_origin[r])));
+            b.loc_xyz[l] = make_float4(pos.x, pos.y, pos.z, 0.f);
+            const float3 jac = mat_apply(Jm, rel);
+            b.mov_jac[l] = make_float4(jac.x, jac.y, jac.z, 0.f);
+        } else {
+            b.loc_xyz[l] = v;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) b.loc_grad[k * b.loc_gs + l] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncwarp();
+    // a team splits the terms, lookups and explicit pairs among its warps (tw of tn)
+    const int tw = team->w, tn = team->n;
+    const int tf4 = team->f4;
+    TeamShared* ts = team->ts;
+    DS e{0.f, 0.f};
+    topo_terms_split(L.topo, b.lig_xyz, b.lig_grad, b.lig_gs, e, lane, tw, tn);
+    if (R.n_local > 0) topo_terms_split(R.intra, b.loc_xyz, b.loc_grad, b.loc_gs, e, lane, tw, tn);
     // grid lookups (inter_molecular_interactions, cached branch)
     if (env.grid.has_grid) {
         for (int a = lane + tw * kWarp; a < N; a += tn * kWarp) {
@@ -603,15 +884,15 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
     }
     __syncwarp();
     DS et = e;  // the pose's energy (the team's partials summed in member order)
-    if (kTeam && tn > 1) {
+    if (tn > 1) {
         const DS ew = ds_warp_reduce(e);
-        if (lane == 0) b.ts->e[tw] = make_float2(ew.hi, ew.lo);
-        if (!team_sync(b.ts, tn, lane)) {  // the team aborted: NaN ends the caller's search
+        if (lane == 0) ts->e[tw] = make_float2(ew.hi, ew.lo);
+        if (!team_sync(ts, tn, lane)) {  // the team aborted: NaN ends the caller's search
             if (gdot) *gdot = __longlong_as_double(0x7ff8000000000000LL);
             return __longlong_as_double(0x7ff8000000000000LL);
         }
-        et = DS{b.ts->e[0].x, b.ts->e[0].y};
-        for (int u = 1; u < tn; ++u) ds_add_ds(et, DS{b.ts->e[u].x, b.ts->e[u].y});
+        et = DS{ts->e[0].x, ts->e[0].y};
+        for (int u = 1; u < tn; ++u) ds_add_ds(et, DS{ts->e[u].x, ts->e[u].y});
     }
     // flat gradient and the receptor-torsion chain rule (interaction.cpp:338-350), the
     // team's arrays summed in member order
@@ -619,7 +900,7 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
     for (int a = lane; a < N; a += kWarp) {
         float gx = 0.f, gy = 0.f, gz = 0.f;
         for (int u = 0; u < tn; ++u) {
-            const float4* G = b.lig_grad + (u - tw) * b.team_f4;
+            const float4* G = b.lig_grad + (u - tw) * tf4;
             const float4 g0 = G[a], g1 = G[b.lig_gs + a];
             const float4 g2 = G[2 * b.lig_gs + a], g3 = G[3 * b.lig_gs + a];
             const float sx = (g0.x + g1.x) + (g2.x + g3.x);
@@ -644,7 +925,7 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
         for (int l = l0; l < l1; ++l) {
             float3 g = make_float3(0.f, 0.f, 0.f);
             for (int u = 0; u < tn; ++u) {
-                const float4* G = b.loc_grad + (u - tw) * b.team_f4;
+                const float4* G = b.loc_grad + (u - tw) * tf4;
                 const float4 g0 = G[l], g1 = G[b.loc_gs + l];
                 const float4 g2 = G[2 * b.loc_gs + l], g3 = G[3 * b.loc_gs + l];
                 const float3 gu = make_float3((g0.x + g1.x) + (g2.x + g3.x), (g0.y + g1.y) + (g2.y + g3.y),
@@ -658,12 +939,12 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
     }
     __syncwarp();
     // no member clears its arrays for the next evaluation before every member has read them
-    if (kTeam && tn > 1 && !team_sync(b.ts, tn, lane)) {
+    if (tn > 1 && !team_sync(ts, tn, lane)) {
         if (gdot) *gdot = __longlong_as_double(0x7ff8000000000000LL);
         return __longlong_as_double(0x7ff8000000000000LL);
     }
     if (gdir) *gdot = ds_warp_sum(gd);
-    if (kTeam && tn > 1) return static_cast<double>(et.hi) + static_cast<double>(et.lo) + R.e_const;
+    if (tn > 1) return static_cast<double>(et.hi) + static_cast<double>(et.lo) + R.e_const;
     return ds_warp_sum(e) + R.e_const;
 }
 
@@ -673,8 +954,11 @@ __device__ __forceinline__ double eval_pose_body(const EvalEnv& env, const DevLi
 template <bool kTeam = false>
 static __device__ __noinline__ double eval_pose(const EvalEnv& env, const DevLigand& L, const float* x0,
                                                 const float* d, float t, float* gout, const PoseBufs& b,
-                                                int lane, double* gdot = nullptr) {
-    return eval_pose_body<kTeam>(env, L, x0, d, t, gout, b, lane, gdot ? d : nullptr, gdot);
+                                                int lane, double* gdot = nullptr, const Team* team = nullptr) {
+    if constexpr (kTeam)
+        return eval_pose_team_body(env, L, x0, d, t, gout, b, lane, gdot ? d : nullptr, gdot, team);
+    else
+        return eval_pose_body(env, L, x0, d, t, gout, b, lane, gdot ? d : nullptr, gdot);
 }
 
 // Shared-memory floats needed by PoseBufs for a ligand of up to n_atoms atoms.
@@ -691,10 +975,6 @@ __device__ inline PoseBufs carve_pose_bufs(float* base, int n_atoms, int n_local
     b.mov_jac = b.loc_grad + 4 * n_local;
     b.lig_gs = n_atoms;
     b.loc_gs = n_local;
-    b.team_w = 0;
-    b.team_n = 1;
-    b.team_f4 = 0;
-    b.ts = nullptr;
     return b;
 }
 

@@ -90,12 +90,14 @@ __device__ __forceinline__ double closure_energy64(Closure& c, const float* x) {
 }
 
 // The same closure evaluated by a team of warps (the single-walker search's team mode).
-struct TeamClosure : Closure {};
+struct TeamClosure : Closure {
+    const Team* team;
+};
 
 __device__ __forceinline__ double closure_eval(TeamClosure& c, double t, const float* d, float* g,
                                                double* gdot = nullptr) {
     ++c.nevals;
-    return eval_pose<true>(*c.env, *c.L, c.x0, d, static_cast<float>(t), g, *c.b, c.lane, gdot);
+    return eval_pose<true>(*c.env, *c.L, c.x0, d, static_cast<float>(t), g, *c.b, c.lane, gdot, c.team);
 }
 
 __device__ __forceinline__ double cubic_interpolate(double x1, double f1, double g1, double x2,

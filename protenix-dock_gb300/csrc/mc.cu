@@ -213,7 +213,7 @@ __device__ double vdw_check(const ScoreEnv& se, const DevLigand& L, const float*
 
 // Pose score of the state [xyz | torsions] in x (root_scorer::combine).
 __device__ double mc_pscore(const McArgs& a, const DevLigand& L, const float* x, const PoseBufs& b,
-                            int lane) {
+                            const Team& tm, int lane) {
     const int N = L.n_atoms;
     const DevReceptor& R = a.env.rec;
     for (int i = lane; i < N; i += kWarp) b.lig_xyz[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], 0.f);
@@ -226,7 +226,7 @@ __device__ double mc_pscore(const McArgs& a, const DevLigand& L, const float* x,
         b.loc_xyz[l] = make_float4(p.x, p.y, p.z, 0.f);
     }
     __syncwarp();
-    return score_pose<true>(a.senv, L, L.score, b.lig_xyz, b.loc_xyz, lane, nullptr, b.team_w, b.team_n, b.ts);
+    return score_pose<true>(a.senv, L, L.score, b.lig_xyz, b.loc_xyz, lane, nullptr, tm.w, tm.n, tm.ts);
 }
 
 __device__ void atomic_min_double(double* p, double v) {
@@ -248,7 +248,7 @@ __device__ void atomic_min_double(double* p, double v) {
 // search one walker together. Every member runs the walker's whole search on its own slice
 // with its own copy of the generator, seeded alike, so all members draw the same numbers and
 // take the same branches; the evaluations split their terms, lookups and explicit pairs
-// among the members and sum the members' parts in member order (eval_pose_body), so every
+// among the members and sum the members' parts in member order (eval_pose_team_body), so every
 // member holds the same energy and gradient. The history slab is the team's: members write
 // the same values to it. Only member 0 takes walkers from the queue, updates the global
 // minimum and writes the outputs, and its queue slot and minimum reach the others through
@@ -264,17 +264,18 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     const bool team = a.team > 1;
     const bool lead = !team || wib == 0;  // the member that takes walkers and writes results
     float* base = smem + static_cast<size_t>(wib) * slice;
-    PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
+    const PoseBufs b = carve_pose_bufs(base, a.max_atoms, a.n_local);
+    Team tm{0, 1, 0, nullptr};
     if (team) {
-        b.team_w = wib;
-        b.team_n = a.team;
-        b.team_f4 = slice / 4;
-        b.ts = reinterpret_cast<TeamShared*>(smem + static_cast<size_t>(a.warps_per_block) * slice);
+        tm.w = wib;
+        tm.n = a.team;
+        tm.f4 = slice / 4;
+        tm.ts = reinterpret_cast<TeamShared*>(smem + static_cast<size_t>(a.warps_per_block) * slice);
         if (threadIdx.x == 0) {
-            b.ts->count = 0;
-            b.ts->gen = 0;
-            b.ts->abort = 0;
-            b.ts->slot = 0;
+            tm.ts->count = 0;
+            tm.ts->gen = 0;
+            tm.ts->abort = 0;
+            tm.ts->slot = 0;
         }
         __syncthreads();
     }
@@ -294,14 +295,15 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
     TeamClosure c;
     c.env = &a.env;
     c.b = &b;
+    c.team = &tm;
     c.lane = lane;
     while (true) {
         int w = 0;
         if (team) {
-            if (threadIdx.x == 0) b.ts->slot = atomicAdd(a.counter, 1);
-            if (!team_sync(b.ts, a.team, lane)) break;
-            w = *reinterpret_cast<volatile int*>(&b.ts->slot);
-            if (!team_sync(b.ts, a.team, lane)) break;  // read by all before the next take
+            if (threadIdx.x == 0) tm.ts->slot = atomicAdd(a.counter, 1);
+            if (!team_sync(tm.ts, a.team, lane)) break;
+            w = *reinterpret_cast<volatile int*>(&tm.ts->slot);
+            if (!team_sync(tm.ts, a.team, lane)) break;  // read by all before the next take
         } else {
             if (lane == 0) w = atomicAdd(a.counter, 1);
             w = __shfl_sync(kFull, w, 0);
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
         double best_e = 0.0;
         lbfgs_pose<true>(c, a.full, v, D, Dp, lane, best_e);
         long total = c.nevals;
-        double best_ps = mc_pscore(a, L, v.x, b, lane);
+        double best_ps = mc_pscore(a, L, v.x, b, tm, lane);
         vcopy(best_x, v.x, D, lane);
         int status = 0;
         if (walker != 0) {
@@ -428,18 +430,18 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                     // optional pruning on the pre-relaxation energy (searcher.cpp:141-157)
                     if (a.threshold > 0.0 && a.gmin) {
                         c.x0 = v.x;
-                        const double pre = eval_pose<true>(a.env, L, v.x, nullptr, 0.f, v.gnew, b, lane);
+                        const double pre = eval_pose<true>(a.env, L, v.x, nullptr, 0.f, v.gnew, b, lane, nullptr, &tm);
                         double gm;
                         if (team) {
                             // the leader's view of the shared minimum, so that every member
                             // takes the same branch
                             if (threadIdx.x == 0) {
                                 atomic_min_double(&a.gmin[lid], pre);
-                                b.ts->gmin = *reinterpret_cast<volatile double*>(&a.gmin[lid]);
+                                tm.ts->gmin = *reinterpret_cast<volatile double*>(&a.gmin[lid]);
                             }
-                            team_sync(b.ts, a.team, lane);
-                            gm = *reinterpret_cast<volatile double*>(&b.ts->gmin);
-                            team_sync(b.ts, a.team, lane);
+                            team_sync(tm.ts, a.team, lane);
+                            gm = *reinterpret_cast<volatile double*>(&tm.ts->gmin);
+                            team_sync(tm.ts, a.team, lane);
                         } else {
                             if (lane == 0) atomic_min_double(&a.gmin[lid], pre);
                             __syncwarp();
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                     double cdd_e = 0.0;  // unused: the step is judged by its pose score
                     lbfgs_pose<true>(c, a.fast, v, D, Dp, lane, cdd_e, false);
                     total += c.nevals;
-                    const double cdd_ps = mc_pscore(a, L, v.x, b, lane);
+                    const double cdd_ps = mc_pscore(a, L, v.x, b, tm, lane);
                     bool accept = step == 0 || cdd_ps < tmp_ps;
                     if (!accept) {
                         if (lane == 0) bc[4] = mt_uniform_real(rng, 0.0, 1.0);
@@ -463,7 +465,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
                             double e2 = 0.0;
                             lbfgs_pose<true>(c, a.full, v, D, Dp, lane, e2);
                             total += c.nevals;
-                            tmp_ps = mc_pscore(a, L, v.x, b, lane);
+                            tmp_ps = mc_pscore(a, L, v.x, b, tm, lane);
                             if (tmp_ps < best_ps) {
                                 best_ps = tmp_ps;
                                 best_e = e2;
@@ -485,7 +487,7 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
             for (int e = lane; e < 3 * N; e += kWarp) ox[e] = best_x[e];
             for (int r = lane; r < R; r += kWarp) a.out_tors[static_cast<size_t>(w) * R + r] = best_x[3 * N + r];
             if (lane == 0) {
-                const bool aborted = team && *reinterpret_cast<volatile int*>(&b.ts->abort);
+                const bool aborted = team && *reinterpret_cast<volatile int*>(&tm.ts->abort);
                 a.out_e[w] = best_e;
                 a.out_ps[w] = best_ps;
                 a.out_nev[w] = static_cast<int>(total);

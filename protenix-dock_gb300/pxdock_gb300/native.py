@@ -292,6 +292,20 @@ class Context:
                                        _p(st, C.c_int32)))
         return dict(xyz=xyz, torsions=tors, energy=e, nevals=nev, status=st)
 
+    def lbfgs_inplace(self, params, lig, xyz, tors, energy, nevals, status):
+        """pxd_lbfgs on the caller's arrays, in place as the C call works (no copies):
+        xyz [n][N][3] float64 C-contiguous (the starts in, the optimised poses out), tors
+        [n][R] float64, energy [n] float64, nevals / status [n] int32."""
+        n = xyz.shape[0]
+        for a, t in ((xyz, np.float64), (tors, np.float64), (energy, np.float64), (nevals, np.int32),
+                     (status, np.int32)):
+            if a.dtype != t or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("lbfgs_inplace needs C-contiguous %s arrays" % np.dtype(t).name)
+        dummy = np.zeros(1)
+        self._check(self.lib.pxd_lbfgs(self.h, C.byref(params), lig, n, _p(xyz),
+                                       _p(tors if tors.size else dummy), _p(energy), _p(nevals, C.c_int32),
+                                       _p(status, C.c_int32)))
+
     def score_grad_dev(self, n_poses, max_atoms, ids_ptr, xyz_ptr, tors_ptr, energy_ptr,
                        lig_grad_ptr, tors_grad_ptr, stream=None):
         """Device-pointer call; pointers are integer device addresses."""

@@ -102,3 +102,32 @@ def test_size_classes_match_single_ligand_launches():
     else:  # another register budget may round differently; trajectories then part
         assert abs(np.median(tuned[1]) - np.median(mixed[1])) <= 0.01 * abs(np.median(mixed[1])) + 1e-3
     ctx.close()
+
+
+def test_inplace_host_call_matches_copying_wrapper():
+    """Context.lbfgs_inplace (pxd_lbfgs on the caller's arrays, as bench.py's end-to-end leg
+    times it) ends where Context.lbfgs (which copies its inputs) ends, bit for bit, and
+    leaves the results in the caller's arrays."""
+    native.load(auto_build=True)
+    rec = model.Receptor.from_json(synth.make_receptor(seed=0, n_heavy=400, cube=16.0, cavity=5.0))
+    lig = model.Ligand.from_json(synth.make_ligand(seed=5))
+    box = model.make_box((0.0, 0.0, 0.0), (12.0, 12.0, 12.0), 0.5)
+    ctx = native.Context(0)
+    ctx.set_receptor(rec)
+    ctx.build_grid(box, sorted(set(int(t) for t in lig.vdw_type)))
+    ctx.set_slope(1e6)
+    lid = ctx.add_ligand(lig)
+    lo = np.array(box.init_xyz)
+    hi = lo + (np.array(box.npoints) - 1) * box.spacing
+    poses = synth.random_poses(lig, lo, hi, 64, seed=9)
+    p = native.lbfgs_params(max_iter=40, history=8)
+    ref = ctx.lbfgs(p, lid, poses)
+    xyz = np.ascontiguousarray(poses, np.float64).copy()
+    tors = np.zeros((64, ctx.n_rotors))
+    e, nev, st = np.zeros(64), np.zeros(64, np.int32), np.zeros(64, np.int32)
+    ctx.lbfgs_inplace(p, lid, xyz, tors, e, nev, st)
+    assert np.array_equal(xyz, ref["xyz"]) and np.array_equal(e, ref["energy"])
+    assert np.array_equal(nev, ref["nevals"]) and np.array_equal(st, ref["status"])
+    with pytest.raises(ValueError):
+        ctx.lbfgs_inplace(p, lid, xyz.astype(np.float32), tors, e, nev, st)
+    ctx.close()
