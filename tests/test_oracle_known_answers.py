@@ -43,7 +43,7 @@ XYZ10 = [[7.908, 27.763, 9.369], [8.890, 26.662, 8.959], [8.190, 25.303, 9.005],
 
 
 def test_vdw_table_matches_reference_header():
-    path = "/root/reference/engine/include/bytedock/core/constant.h"
+    path = os.path.join(O.REF_ENGINE, "include", "bytedock", "core", "constant.h")
     if not os.path.exists(path):
         pytest.skip("reference checkout not present on this host")
     import re
