@@ -256,8 +256,7 @@ static int launch_adjoint(pxd_context* const* ctxs, int32_t n_ctx, int32_t which
     else
         fn = multi ? reinterpret_cast<const void*>(score_adjoint_kernel<false, true, float>)
                    : reinterpret_cast<const void*>(score_adjoint_kernel<false, false, float>);
-    int rc = cuda_check(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  static_cast<int>(smem)), "adjoint smem");
+    int rc = raise_smem_limit(ctx, fn, smem, "adjoint smem");
     if (rc) return rc;
     int per_sm = 0;
     rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kAdjWarps * kWarp, smem),

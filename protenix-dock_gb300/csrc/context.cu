@@ -4,6 +4,8 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -32,6 +34,19 @@ int cuda_check(pxd_context* ctx, cudaError_t e, const char* what) {
     if (e == cudaSuccess) return PXD_OK;
     return set_error(ctx, e == cudaErrorMemoryAllocation ? PXD_ERR_NOMEM : PXD_ERR_CUDA,
                      std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int raise_smem_limit(pxd_context* ctx, const void* fn, size_t bytes, const char* what) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> limit;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = limit[{ctx->device, fn}];
+    if (bytes <= cur) return PXD_OK;
+    const int rc = cuda_check(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        static_cast<int>(bytes)),
+                              what);
+    if (!rc) cur = bytes;
+    return rc;
 }
 
 template <class From, class To>

@@ -301,8 +301,7 @@ int pxd_ligand_pose_multi_dev(pxd_context* const* ctxs, int32_t n_ctx, int32_t n
         pose_backward_multi_kernel<float><<<blocks, kPoseWarps * kWarp, 0, s>>>(a);
     } else {
         const size_t smem = sizeof(float) * kPoseWarps * (4 * max_atoms + sizeof(KinShared) / sizeof(float));
-        rc = cuda_check(ctx, cudaFuncSetAttribute(pose_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  static_cast<int>(smem)), "pose smem");
+        rc = raise_smem_limit(ctx, reinterpret_cast<const void*>(pose_multi_kernel), smem, "pose smem");
         if (!rc) pose_multi_kernel<<<blocks, kPoseWarps * kWarp, smem, s>>>(a);
     }
     if (!rc) rc = cuda_check(ctx, cudaGetLastError(), "pose kinematics launch");

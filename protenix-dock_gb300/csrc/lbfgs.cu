@@ -280,10 +280,7 @@ int launch_score(pxd_context* ctx, int n_poses, int max_atoms, const int* lig_id
     const size_t smem =
         sizeof(float) * kWarpsPerBlock * (pose_bufs_floats(max_atoms, a.n_local) + 2 * a.D_pad);
     if (smem > 48 * 1024) {
-        rc = cuda_check(ctx, cudaFuncSetAttribute(score_kernel,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  static_cast<int>(smem)),
-                        "score smem attribute");
+        rc = raise_smem_limit(ctx, reinterpret_cast<const void*>(score_kernel), smem, "score smem attribute");
         if (rc) return rc;
     }
     const int warps = (n_poses + 0);
@@ -444,23 +441,6 @@ int class_join(pxd_context* ctx, size_t k, cudaStream_t s) {
     return rc;
 }
 
-// Raises a kernel variant's dynamic shared-memory limit to at least `bytes`, never
-// lowering it. The limit is a process-wide property of the kernel on the current device:
-// a launcher on another thread that set a larger limit for its own launch must not see it
-// lowered between its attribute call and its launch.
-static int raise_smem_limit(pxd_context* ctx, LbfgsKernelFn kern, size_t bytes) {
-    static std::mutex mu;
-    static std::map<std::pair<int, const void*>, size_t> limit;
-    std::lock_guard<std::mutex> lock(mu);
-    size_t& cur = limit[{ctx->device, reinterpret_cast<const void*>(kern)}];
-    if (bytes <= cur) return PXD_OK;
-    const int rc = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        static_cast<int>(bytes)),
-                              "lbfgs smem attribute");
-    if (!rc) cur = bytes;
-    return rc;
-}
-
 static void fill_consts(LbfgsArgs& a, const pxd_lbfgs_params& p) {
     a.c.max_iter = p.max_iter;
     a.c.max_eval = p.max_eval;
@@ -532,7 +512,7 @@ int launch_lbfgs(pxd_context* ctx, const pxd_lbfgs_params& p, int n_poses, int m
     std::map<LbfgsKernelFn, size_t> smem_of;
     for (const Plan& q : plan) smem_of[q.kern] = std::max(smem_of[q.kern], q.smem);
     for (const auto& [kern, bytes] : smem_of) {
-        rc = raise_smem_limit(ctx, kern, bytes);
+        rc = raise_smem_limit(ctx, reinterpret_cast<const void*>(kern), bytes, "lbfgs smem attribute");
         if (rc) return rc;
     }
     for (Plan& q : plan) {
@@ -676,7 +656,7 @@ int launch_lbfgs_noalloc(pxd_context* ctx, const pxd_lbfgs_params& p, int n_pose
     a.X_pad = dof_xpad(ctx, max_atoms, dof);
     const size_t smem = lbfgs_block_smem(ctx, max_atoms, p.history, false, dof);
     const LbfgsKernelFn kern = lbfgs_variant(ctx, max_atoms, dof);
-    rc = raise_smem_limit(ctx, kern, smem);
+    rc = raise_smem_limit(ctx, reinterpret_cast<const void*>(kern), smem, "lbfgs smem attribute");
     if (rc) return rc;
     int per_sm = 0;
     rc = cuda_check(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern,
@@ -774,9 +754,7 @@ extern "C" int pxd_score_grad_multi_dev(pxd_context* const* ctxs, int32_t n_ctx,
     a.n_local = max_local;
     a.D_pad = padded(3 * max_atoms + max_rot);
     const size_t smem = sizeof(float) * kWarpsPerBlock * (pose_bufs_floats(max_atoms, a.n_local) + 2 * a.D_pad);
-    rc = cuda_check(ctx, cudaFuncSetAttribute(score_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(smem)),
-                    "score smem attribute");
+    rc = raise_smem_limit(ctx, reinterpret_cast<const void*>(score_multi_kernel), smem, "score smem attribute");
     if (!rc) {
         int blocks = (n_poses + kWarpsPerBlock - 1) / kWarpsPerBlock;
         if (blocks > ctx->n_sm * 16) blocks = ctx->n_sm * 16;

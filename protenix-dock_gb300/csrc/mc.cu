@@ -625,9 +625,7 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     const int wpb = a.warps_per_block;
     const size_t smem = sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history) +
                         (a.team > 1 ? (sizeof(TeamShared) + 15) / 16 * 16 : 0);
-    rc = cuda_check(ctx, cudaFuncSetAttribute(mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(smem)),
-                    "mc smem attribute");
+    rc = raise_smem_limit(ctx, reinterpret_cast<const void*>(mc_kernel), smem, "mc smem attribute");
     if (rc) return rc;
     // One walker per block leaves the SMs nearly empty: ask for the smallest shared-memory carve-out
     // (percent of the SM's shared memory) that still holds the blocks each SM must run at

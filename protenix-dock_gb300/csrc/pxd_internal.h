@@ -233,6 +233,11 @@ namespace pxd {
 
 int set_error(pxd_context* ctx, int code, const std::string& msg);
 int cuda_check(pxd_context* ctx, cudaError_t e, const char* what);
+// Raises kernel fn's dynamic shared-memory limit on the context's device to at least
+// `bytes`, never lowering it. The limit is a process-wide property of the kernel: a
+// launcher on another thread that set a larger limit for its own launch must not see it
+// lowered between its attribute call and its launch.
+int raise_smem_limit(pxd_context* ctx, const void* fn, size_t bytes, const char* what);
 int ensure_scratch(pxd_context* ctx, size_t bytes);
 int sync_ligand_table(pxd_context* ctx);
 int refresh_ligand_slots(pxd_context* ctx);

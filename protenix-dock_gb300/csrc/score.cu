@@ -543,9 +543,7 @@ int pxd_score_dev(pxd_context* ctx, int32_t which, int32_t n_poses, int32_t max_
     const int per_warp = 4 * (max_atoms + ctx->rec.n_mov + 1) + PXD_MAX_RECEPTOR_TORSIONS;
     const size_t smem = sizeof(float) * per_warp * kScoreWarps;
     if (smem > 48 * 1024) {
-        rc = cuda_check(ctx, cudaFuncSetAttribute(empirical_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  static_cast<int>(smem)),
-                        "score smem");
+        rc = raise_smem_limit(ctx, reinterpret_cast<const void*>(empirical_score_kernel), smem, "score smem");
         if (rc) return rc;
     }
     int blocks = (n_poses + kScoreWarps - 1) / kScoreWarps;
