@@ -244,8 +244,8 @@ __device__ void atomic_min_double(double* p, double v) {
 // is usually alone on its SM, where the FP64 operations on each pass's dependent chain are
 // what it waits on.
 //
-// Team mode (a.team = kMcWarps, fewer walkers than SMs' worth of warps): the block's warps
-// search one walker together. Every member runs the walker's whole search on its own slice
+// Team mode (a.team = kMcWarps, at most one walker per SM): the block's warps search one
+// walker together. Every member runs the walker's whole search on its own slice
 // with its own copy of the generator, seeded alike, so all members draw the same numbers and
 // take the same branches; the evaluations split their terms, lookups and explicit pairs
 // among the members and sum the members' parts in member order (eval_pose_team_body), so every
@@ -253,7 +253,8 @@ __device__ void atomic_min_double(double* p, double v) {
 // the same values to it. Only member 0 takes walkers from the queue, updates the global
 // minimum and writes the outputs, and its queue slot and minimum reach the others through
 // the team's shared state. Team barriers spin a bounded number of times; a team that gives
-// up flags the launch (a.error[1]) and leaves its walkers with status 3.
+// up raises the launch's second error flag (a.error[1], reported by the host) and leaves
+// its walker with status 3.
 __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_constant__ McArgs a) {
     extern __shared__ __align__(16) float smem[];
     const int lane = threadIdx.x & (kWarp - 1);
