@@ -6,6 +6,7 @@
 // lane 0 advances the state (kept in a per-warp global slab) and broadcasts the values,
 // so every random start, move and Metropolis test consumes the reference's stream.
 // Relaxations reuse the batched L-BFGS device code, scores the device pose scorer.
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -139,6 +140,7 @@ struct McArgs {
     int n_local, D_pad;
     int warps_per_block;  // kMcWarps
     int team;             // kMcWarps: the block's warps search one walker together; 1: a walker per warp
+    int drop_member;      // test of the bounded team barriers: the last member leaves at once
     float* hist;
     size_t hist_stride;
     MtState* rng;
@@ -279,6 +281,9 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
             tm.ts->slot = 0;
         }
         __syncthreads();
+        // failure test (PXD_TEST_TEAM_DROPOUT): a member that never arrives, so that the
+        // others' waits run out and the launch reports it
+        if (a.drop_member && wib == a.team - 1) return;
     }
     float* vb = base + pose_bufs_floats(a.max_atoms, a.n_local);
     Vecs v = carve_vecs(vb, Dp, m);
@@ -302,9 +307,13 @@ __global__ void __launch_bounds__(kMcWarps * kWarp) mc_kernel(const __grid_const
         int w = 0;
         if (team) {
             if (threadIdx.x == 0) tm.ts->slot = atomicAdd(a.counter, 1);
-            if (!team_sync(tm.ts, a.team, lane)) break;
+            bool ok = team_sync(tm.ts, a.team, lane);
             w = *reinterpret_cast<volatile int*>(&tm.ts->slot);
-            if (!team_sync(tm.ts, a.team, lane)) break;  // read by all before the next take
+            ok = ok && team_sync(tm.ts, a.team, lane);  // read by all before the next take
+            if (!ok) {  // the team gave up waiting: its walker is not searched
+                if (lead && lane == 0) atomicExch(a.error + 1, 1);
+                break;
+            }
         } else {
             if (lane == 0) w = atomicAdd(a.counter, 1);
             w = __shfl_sync(kFull, w, 0);
@@ -622,6 +631,10 @@ int pxd_mc_search_dev(pxd_context* ctx, const pxd_mc_params* p, int32_t n_walker
     // slots, and its four schedulers share the evaluations. Fewer walkers than 4 per SM: one
     // warp per block, so each walker has an SM to itself or shares it with few others.
     a.team = n_walkers <= ctx->n_sm ? kMcWarps : 1;
+    {
+        const char* drop = std::getenv("PXD_TEST_TEAM_DROPOUT");
+        a.drop_member = drop && drop[0] == '1' && a.team > 1 ? 1 : 0;
+    }
     a.warps_per_block = a.team > 1 || n_walkers >= kMcWarps * ctx->n_sm ? kMcWarps : 1;
     const int wpb = a.warps_per_block;
     const size_t smem = sizeof(float) * wpb * mc_warp_floats(max_atoms, a.n_local, a.D_pad, p->lbfgs.history) +

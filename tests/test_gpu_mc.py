@@ -136,6 +136,29 @@ def test_pruning_threshold_runs(mc):
             consistent(c, out, w)
 
 
+def test_team_barrier_timeout_is_reported_and_the_context_recovers(mc):
+    """Failure detection of team mode without a GPU fault: with PXD_TEST_TEAM_DROPOUT=1 the
+    last member of every team leaves before its first barrier, so the other members' waits
+    run out (a bounded spin, about 0.1 s), the team stops and the host reports
+    PXD_ERR_DEVICE_FLAG. The next launch on the same context runs normally."""
+    c = mc
+    W = 4  # at most one walker per SM: team mode
+    p = native.mc_params(c["lo"], c["hi"], seed=4, max_nsteps=2, relax_nsteps=5)
+    starts = np.repeat(c["lig"].poses[0][None], W, axis=0)
+    os.environ["PXD_TEST_TEAM_DROPOUT"] = "1"
+    try:
+        with pytest.raises(native.NativeError, match="stopped waiting") as err:
+            c["ctx"].mc_search(p, c["lid"], starts, np.arange(W))
+        assert err.value.code == 6  # PXD_ERR_DEVICE_FLAG
+    finally:
+        del os.environ["PXD_TEST_TEAM_DROPOUT"]
+    out = c["ctx"].mc_search(p, c["lid"], starts, np.arange(W))
+    assert np.all(out["status"] <= 2) and np.sum(out["status"] == 0) >= 1
+    for w in range(W):
+        if out["status"][w] == 0:
+            consistent(c, out, w)
+
+
 def test_bad_parameters_rejected(mc):
     c = mc
     p = native.mc_params(c["lo"], c["hi"], temperature=0.0)
